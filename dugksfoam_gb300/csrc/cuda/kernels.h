@@ -1,0 +1,42 @@
+// Host-callable launchers of the DUGKS CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device_common.cuh"
+
+namespace dugks {
+
+// ---------------------------------------------------------- reference pipeline
+constexpr int kRefKernels = 8;
+extern const char* const kRefKernelNames[kRefKernels];
+
+struct RefBuffers {
+    double *gT, *hT;     // [nC][Vp]      g~, h~
+    double *gB, *hB;     // [nC][Vp]      gBarPvol, hBarPvol
+    double *gG, *hG;     // [nC][D][Vp]   least-squares gradients
+    double *Gbg, *Gbh;   // [nW][Vp]      lagged fixedGradient gradients
+    double *gS, *hS;     // [nA][Vp]      face distributions
+};
+
+// Launch pass `pass` (0..kRefKernels-1) of one reference-pipeline step.
+void launch_ref_pass(int pass, const StepArgs& a, const RefBuffers& b, int sms, cudaStream_t s);
+
+// ------------------------------------------------------------- fused pipeline
+struct FusedPlanDev;  // defined in fused_pipeline.cu
+
+// -------------------------------------------------------------- common kernels
+// g~,h~ <- gscale * Shakhov(rho,U,T,q=0) and tau <- tau(T,rho) for every cell.
+template <typename S>
+void launch_init_state(const StepArgs& a, S* gT, S* hT, double gscale, int sms, cudaStream_t s);
+// Copy distributions between storage type S (scaled by gscale) and FP64 [nC][nV].
+template <typename S>
+void launch_export_dist(const StepArgs& a, const S* src, double* dst, double inv_gscale, int sms, cudaStream_t s);
+template <typename S>
+void launch_import_dist(const StepArgs& a, const double* src, S* dst, double gscale, int sms, cudaStream_t s);
+// out[0] = max, out[1] = sum over internal faces of deltaCoeff*(|U_f| + sqrt(D) xi_max).
+void launch_conum(const StepArgs& a, const double* dcI, double xi_max, double* out, cudaStream_t s);
+// out = {sum|U-Uo|, sum|U|, sum|T-To|, sum T, sum|rho-rhoo|, sum rho}; then old <- current.
+void launch_residual(const StepArgs& a, double* Uo, double* To, double* rhoo, double* out, cudaStream_t s);
+
+}  // namespace dugks

@@ -1,0 +1,201 @@
+// extern "C" entry points of libdugks (include/dugks/dugks.h).
+#include <cstring>
+#include <exception>
+#include <memory>
+#include <string>
+
+#include "dugks/dugks.h"
+#include "foam_io.h"
+#include "solver.h"
+
+struct dugks_handle {
+    std::unique_ptr<dugks::Solver> solver;
+    std::string err;
+};
+
+namespace {
+thread_local std::string g_err;
+
+int guard(dugks_handle* h, int rc) {
+    if (h && rc != DUGKS_OK && h->solver) h->err = h->solver->error();
+    return rc;
+}
+
+template <typename F>
+int call(dugks_handle* h, F&& f) {
+    if (!h || !h->solver) return DUGKS_ERR_ARG;
+    try {
+        return guard(h, f(*h->solver));
+    } catch (const std::exception& e) {
+        h->err = e.what();
+        return DUGKS_ERR_ARG;
+    } catch (...) {
+        h->err = "unknown exception";
+        return DUGKS_ERR_ARG;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int dugks_create(const dugks_case_desc* desc, dugks_handle** out) {
+    if (!desc || !out) { g_err = "null argument"; return DUGKS_ERR_ARG; }
+    *out = nullptr;
+    try {
+        std::string err;
+        int code = DUGKS_OK;
+        auto s = dugks::Solver::create(*desc, err, code);
+        if (!s) { g_err = err; return code; }
+        *out = new dugks_handle{std::move(s), std::string()};
+        return DUGKS_OK;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return DUGKS_ERR_ARG;
+    }
+}
+
+int dugks_create_from_case_dir(const char* dir, int32_t precision, dugks_handle** out) {
+    if (!dir || !out) { g_err = "null argument"; return DUGKS_ERR_ARG; }
+    *out = nullptr;
+    dugks::FoamCase c;
+    std::string err;
+    if (!dugks::read_foam_case(dir, c, err)) {
+        g_err = err;
+        return err.find("unsupported") != std::string::npos ? DUGKS_ERR_UNSUPPORTED : DUGKS_ERR_IO;
+    }
+    dugks_case_desc d{};
+    d.n_points = (int32_t)(c.points.size() / 3);
+    d.points = c.points.data();
+    d.n_cells = c.nCells; d.n_faces = c.nFaces; d.n_internal_faces = c.nInternal;
+    d.face_offsets = c.faceOffsets.data(); d.face_verts = c.faceVerts.data();
+    d.owner = c.owner.data(); d.neighbour = c.neighbour.data();
+    d.n_patches = (int32_t)c.patchNames.size();
+    d.patch_start = c.patchStart.data(); d.patch_size = c.patchSize.data(); d.patch_kind = c.patchKind.data();
+    d.wall_U = c.wallU.data(); d.wall_T = c.wallT.data();
+    d.n_xi_per_dim = c.nDV; d.xis = c.xis.data(); d.weights = c.weights.data(); d.xi_max = c.xiMax;
+    d.R = c.R; d.omega = c.omega; d.Tref = c.Tref; d.muRef = c.muRef; d.Pr = c.Pr; d.KInner = c.KInner;
+    d.rho0 = c.rho0.data(); d.U0 = c.U0.data(); d.T0 = c.T0.data();
+    d.precision = precision;
+    d.pipeline = DUGKS_PIPE_AUTO;
+    d.device = 0;
+    int rc = dugks_create(&d, out);
+    if (rc == DUGKS_OK && c.deltaT > 0) (*out)->solver->setDt(c.deltaT);
+    return rc;
+}
+
+int dugks_destroy(dugks_handle* h) {
+    delete h;
+    return DUGKS_OK;
+}
+
+const char* dugks_last_error(const dugks_handle* h) {
+    if (!h) return g_err.c_str();
+    return h->err.c_str();
+}
+
+const char* dugks_global_error(void) { return g_err.c_str(); }
+
+int dugks_get_info(dugks_handle* h, dugks_info* info) {
+    if (!info) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int { s.info(*info); return DUGKS_OK; });
+}
+
+int dugks_set_dt(dugks_handle* h, double dt) {
+    return call(h, [&](dugks::Solver& s) -> int {
+        if (!(dt > 0)) return s.fail(DUGKS_ERR_ARG, "dt must be positive");
+        s.setDt(dt);
+        return DUGKS_OK;
+    });
+}
+
+int dugks_get_dt(dugks_handle* h, double* dt) {
+    if (!dt) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int { *dt = s.dt(); return DUGKS_OK; });
+}
+
+int dugks_set_stream(dugks_handle* h, void* stream) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.setStream(static_cast<cudaStream_t>(stream)); });
+}
+
+int dugks_step(dugks_handle* h, int32_t nsteps) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.evolution(nsteps); });
+}
+
+int dugks_synchronize(dugks_handle* h) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.synchronize(); });
+}
+
+int dugks_get_conum(dugks_handle* h, double* max_co, double* mean_co) {
+    if (!max_co || !mean_co) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int { return s.getCoNum(*max_co, *mean_co); });
+}
+
+int dugks_get_macros(dugks_handle* h, double* rho, double* U, double* T, double* q, double* tau) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.macros(rho, U, T, q, tau); });
+}
+
+int dugks_get_face_macros(dugks_handle* h, double* rho, double* U, double* T, double* q, double* tau) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.faceMacros(rho, U, T, q, tau); });
+}
+
+int dugks_get_wall(dugks_handle* h, int32_t patch, double* rho_w, double* q_wall, double* stress_wall) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.wall(patch, rho_w, q_wall, stress_wall); });
+}
+
+int dugks_get_residual(dugks_handle* h, double res[3]) {
+    if (!res) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int { return s.residual(res); });
+}
+
+int dugks_get_dist(dugks_handle* h, double* g, double* hh) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.getDist(g, hh); });
+}
+
+int dugks_set_dist(dugks_handle* h, const double* g, const double* hh) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.setDist(g, hh); });
+}
+
+int dugks_checkpoint_size(dugks_handle* h, size_t* bytes) {
+    if (!bytes) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int { *bytes = s.checkpointSize(); return DUGKS_OK; });
+}
+
+int dugks_checkpoint_save(dugks_handle* h, void* buf, size_t bytes) {
+    if (!buf) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int { return s.checkpointSave(buf, bytes); });
+}
+
+int dugks_checkpoint_load(dugks_handle* h, const void* buf, size_t bytes) {
+    if (!buf) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int { return s.checkpointLoad(buf, bytes); });
+}
+
+int dugks_profile_step(dugks_handle* h, int32_t nsteps, char* names, size_t names_len, double* ms,
+                       int32_t max_kernels, int32_t* n_kernels) {
+    if (nsteps <= 0 || !ms || !n_kernels) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int {
+        std::vector<std::string> nm;
+        std::vector<double> t;
+        int rc = s.profile(nsteps, nm, t);
+        if (rc != DUGKS_OK) return rc;
+        *n_kernels = (int32_t)t.size();
+        std::string joined;
+        for (size_t i = 0; i < t.size(); ++i) {
+            if ((int32_t)i < max_kernels) ms[i] = t[i];
+            joined += nm[i];
+            joined += '\n';
+        }
+        if (names && names_len) {
+            std::strncpy(names, joined.c_str(), names_len - 1);
+            names[names_len - 1] = 0;
+        }
+        return DUGKS_OK;
+    });
+}
+
+int dugks_launches_per_step(dugks_handle* h, int32_t* n) {
+    if (!n) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int { *n = s.launchesPerStep(); return DUGKS_OK; });
+}
+
+}  // extern "C"

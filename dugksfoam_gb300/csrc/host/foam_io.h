@@ -1,0 +1,52 @@
+// OpenFOAM ASCII case I/O for the DUGKS engine.
+//
+// Reads the inputs dugksFoam reads (src/dugksFoam.C:48-54, createFields.H,
+// fvDVM.C:886-933, fvDVM.C:56-117): constant/polyMesh/{points,faces,owner,
+// neighbour,boundary}, 0/{rho,U,T}, constant/DVMProperties,
+// constant/{Xis,weights}, system/controlDict.  Writes volume fields in the
+// same ASCII format (runTime.write(), dugksFoam.C:81).
+#pragma once
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace dugks {
+
+struct FoamCase {
+    // mesh
+    std::vector<double> points;
+    std::vector<int32_t> faceOffsets, faceVerts, owner, neighbour;
+    int nCells = 0, nFaces = 0, nInternal = 0;
+    std::vector<std::string> patchNames, patchTypes;   // polyMesh boundary
+    std::vector<int32_t> patchStart, patchSize;
+    std::vector<std::string> rhoBC;                     // 0/rho patch types
+    std::vector<int32_t> patchKind;                     // dugks_patch_kind
+    // fields
+    std::vector<double> rho0, U0, T0;                   // internal
+    std::vector<double> wallU, wallT;                   // per boundary face
+    // DVMProperties
+    int nDV = 0;
+    double xiMax = 0, xiMin = 0;
+    double R = 0, omega = 0, Tref = 0, muRef = 0, Pr = 0;
+    int KInner = 0;
+    std::string macroFlux = "no";
+    std::vector<double> xis, weights;
+    // controlDict
+    std::map<std::string, std::string> control;
+    double deltaT = 0;
+};
+
+bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err);
+
+// Write a volScalarField / volVectorField file (uniform boundary values
+// given per patch as "calculated" or "fixedValue" entries).
+bool write_vol_scalar(const std::string& path, const std::string& name, const std::string& dims,
+                      const double* v, int n, const FoamCase& c, const std::vector<std::vector<double>>& patchVals,
+                      std::string& err);
+bool write_vol_vector(const std::string& path, const std::string& name, const std::string& dims,
+                      const double* v, int n, const FoamCase& c, const std::vector<std::vector<double>>& patchVals,
+                      std::string& err);
+
+}  // namespace dugks

@@ -1,0 +1,87 @@
+// dugks::Solver -- host-side owner of one DUGKS case on one GPU.
+//
+// Mirrors the reference's Foam::fvDVM (src/fvDVM/fvDVM/fvDVM.H:78-377):
+// evolution(), getCoNum(), rhoVol()/Uvol()/Tvol()/qVol()/tauVol(), with the
+// state resident in device memory and the step run as CUDA kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../cuda/kernels.h"
+#include "dugks/dugks.h"
+#include "mesh.h"
+
+namespace dugks {
+
+class FusedPipeline;  // fused_pipeline.cu
+
+class Solver {
+public:
+    static std::unique_ptr<Solver> create(const dugks_case_desc& d, std::string& err, int& code);
+    ~Solver();
+
+    // fvDVM::evolution() n times (asynchronous)
+    int evolution(int n);
+    int synchronize();
+    int getCoNum(double& maxCo, double& meanCo);
+    int macros(double* rho, double* U, double* T, double* q, double* tau);
+    int faceMacros(double* rho, double* U, double* T, double* q, double* tau);
+    int wall(int patch, double* rhoW, double* qWall, double* stressWall);
+    int residual(double res[3]);
+    int getDist(double* g, double* h);
+    int setDist(const double* g, const double* h);
+    size_t checkpointSize() const;
+    int checkpointSave(void* buf, size_t n);
+    int checkpointLoad(const void* buf, size_t n);
+    int profile(int nsteps, std::vector<std::string>& names, std::vector<double>& ms);
+    int launchesPerStep() const;
+    void info(dugks_info& out) const;
+
+    void setDt(double dt) { dt_ = dt; }
+    double dt() const { return dt_; }
+    int setStream(cudaStream_t s);
+    cudaStream_t stream() const { return stream_; }
+    const std::string& error() const { return err_; }
+    const Mesh& mesh() const { return mesh_; }
+
+    // internal: allocation helper (recorded for release)
+    template <typename T>
+    T* dalloc(size_t n);
+    int fail(int code, const std::string& msg);
+    int checkCuda(cudaError_t e, const char* what);
+
+private:
+    Solver() = default;
+    int init(const dugks_case_desc& d);
+    int runStep(bool timed, std::vector<double>* ms, std::vector<cudaEvent_t>* ev);
+    StepArgs argsNow() const;
+
+    Mesh mesh_;
+    std::string err_;
+    int device_ = 0, sms_ = 132;
+    int precision_ = DUGKS_FP64, pipeline_ = DUGKS_PIPE_REFERENCE;
+    int nV_ = 0, Vp_ = 0, hasH_ = 1;
+    double dt_ = 0.0, xiMax_ = 0.0, gscale_ = 1.0;
+    int64_t steps_ = 0;
+    cudaStream_t ownStream_ = nullptr, stream_ = nullptr;
+    std::vector<void*> allocs_;
+    size_t bytes_ = 0;
+    bool oom_ = false;
+    StepArgs base_{};
+    // mesh-side device arrays not in StepArgs
+    double* dcI_ = nullptr;
+    // reference pipeline buffers (FP64)
+    RefBuffers ref_{};
+    // residual "old" fields and scratch
+    double *Uo_ = nullptr, *To_ = nullptr, *ro_ = nullptr, *red_ = nullptr;
+    // fused pipeline
+    std::unique_ptr<FusedPipeline> fused_;
+    std::vector<int32_t> patchFirstWall_, patchNWall_;
+};
+
+}  // namespace dugks

@@ -1,0 +1,311 @@
+"""Python binding of the GB300 DUGKS engine (ctypes over include/dugks/dugks.h).
+
+``FvDVM`` mirrors the reference solver class Foam::fvDVM
+(src/fvDVM/fvDVM/fvDVM.H:78-377): ``evolution()``, ``getCoNum()``,
+``rhoVol()``, ``Uvol()``, ``Tvol()``, ``qVol()``, ``tauVol()`` keep the
+reference's names and meaning.  There is no CPU fallback: if libdugks.so is
+missing or no CUDA device is present, construction raises ``DugksError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libdugks.so")
+
+FP64 = 0
+FP32_FP64MOM = 1
+PIPE_AUTO, PIPE_REFERENCE, PIPE_FUSED = 0, 1, 2
+PATCH_EMPTY, PATCH_MAXWELL = 0, 1
+
+ERRORS = {0: "OK", 1: "DUGKS_ERR_ARG", 2: "DUGKS_ERR_IO", 3: "DUGKS_ERR_UNSUPPORTED", 4: "DUGKS_ERR_CUDA",
+          5: "DUGKS_ERR_NUMERIC", 6: "DUGKS_ERR_TIMEOUT", 7: "DUGKS_ERR_OOM"}
+
+# Every entry point declared in include/dugks/dugks.h.
+EXPORTS = [
+    "dugks_create", "dugks_create_from_case_dir", "dugks_destroy", "dugks_last_error", "dugks_global_error",
+    "dugks_get_info", "dugks_set_dt", "dugks_get_dt", "dugks_set_stream", "dugks_step", "dugks_synchronize",
+    "dugks_get_conum", "dugks_get_macros", "dugks_get_face_macros", "dugks_get_wall", "dugks_get_residual",
+    "dugks_get_dist", "dugks_set_dist", "dugks_checkpoint_size", "dugks_checkpoint_save",
+    "dugks_checkpoint_load", "dugks_profile_step", "dugks_launches_per_step",
+]
+
+
+class DugksError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int32)
+
+
+class CaseDesc(C.Structure):
+    _fields_ = [
+        ("n_points", C.c_int32), ("points", _dp),
+        ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_internal_faces", C.c_int32),
+        ("face_offsets", _ip), ("face_verts", _ip), ("owner", _ip), ("neighbour", _ip),
+        ("n_patches", C.c_int32), ("patch_start", _ip), ("patch_size", _ip), ("patch_kind", _ip),
+        ("wall_U", _dp), ("wall_T", _dp),
+        ("n_xi_per_dim", C.c_int32), ("xis", _dp), ("weights", _dp), ("xi_max", C.c_double),
+        ("R", C.c_double), ("omega", C.c_double), ("Tref", C.c_double), ("muRef", C.c_double),
+        ("Pr", C.c_double), ("KInner", C.c_int32),
+        ("rho0", _dp), ("U0", _dp), ("T0", _dp),
+        ("precision", C.c_int32), ("pipeline", C.c_int32), ("device", C.c_int32),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_internal_faces", C.c_int32),
+        ("n_wall_faces", C.c_int32), ("n_dv", C.c_int32), ("n_dv_padded", C.c_int32),
+        ("n_solution_d", C.c_int32), ("has_h", C.c_int32), ("precision", C.c_int32), ("pipeline", C.c_int32),
+        ("dt", C.c_double), ("step_count", C.c_int64), ("device_bytes", C.c_size_t),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libdugks.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise DugksError(4, f"{path} not built; run dugksfoam_gb300.build.build()")
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    lib.dugks_create.argtypes = [C.POINTER(CaseDesc), C.POINTER(vp)]
+    lib.dugks_create_from_case_dir.argtypes = [C.c_char_p, C.c_int32, C.POINTER(vp)]
+    lib.dugks_destroy.argtypes = [vp]
+    lib.dugks_last_error.argtypes = [vp]
+    lib.dugks_last_error.restype = C.c_char_p
+    lib.dugks_global_error.restype = C.c_char_p
+    lib.dugks_get_info.argtypes = [vp, C.POINTER(Info)]
+    lib.dugks_set_dt.argtypes = [vp, C.c_double]
+    lib.dugks_get_dt.argtypes = [vp, _dp]
+    lib.dugks_set_stream.argtypes = [vp, vp]
+    lib.dugks_step.argtypes = [vp, C.c_int32]
+    lib.dugks_synchronize.argtypes = [vp]
+    lib.dugks_get_conum.argtypes = [vp, _dp, _dp]
+    lib.dugks_get_macros.argtypes = [vp] + [_dp] * 5
+    lib.dugks_get_face_macros.argtypes = [vp] + [_dp] * 5
+    lib.dugks_get_wall.argtypes = [vp, C.c_int32, _dp, _dp, _dp]
+    lib.dugks_get_residual.argtypes = [vp, _dp]
+    lib.dugks_get_dist.argtypes = [vp, _dp, _dp]
+    lib.dugks_set_dist.argtypes = [vp, _dp, _dp]
+    lib.dugks_checkpoint_size.argtypes = [vp, C.POINTER(C.c_size_t)]
+    lib.dugks_checkpoint_save.argtypes = [vp, C.c_void_p, C.c_size_t]
+    lib.dugks_checkpoint_load.argtypes = [vp, C.c_void_p, C.c_size_t]
+    lib.dugks_profile_step.argtypes = [vp, C.c_int32, C.c_char_p, C.c_size_t, _dp, C.c_int32, _ip]
+    lib.dugks_launches_per_step.argtypes = [vp, _ip]
+    _lib = lib
+    return lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp) if a is not None else None
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+def _kinds(mesh):
+    out = []
+    for p in mesh["patches"]:
+        out.append(PATCH_EMPTY if p["type"] == "empty" else PATCH_MAXWELL)
+    return np.array(out, np.int32)
+
+
+class FvDVM:
+    """One DUGKS case resident on one GPU (the reference's fvDVM)."""
+
+    def __init__(self, case=None, precision=FP64, pipeline=PIPE_AUTO, device=0, _handle=None):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        if _handle is not None:
+            self._h = _handle
+        else:
+            m = case["mesh"]
+            g = case["gas"]
+            keep = dict(
+                points=np.ascontiguousarray(m["points"], np.float64),
+                off=np.ascontiguousarray(m["face_offsets"], np.int32),
+                fv=np.ascontiguousarray(m["face_verts"], np.int32),
+                own=np.ascontiguousarray(m["owner"], np.int32),
+                nei=np.ascontiguousarray(m["neighbour"], np.int32),
+                ps=np.array([p["startFace"] for p in m["patches"]], np.int32),
+                pn=np.array([p["nFaces"] for p in m["patches"]], np.int32),
+                pk=_kinds(m),
+                Ub=np.ascontiguousarray(case["Ub"], np.float64),
+                Tb=np.ascontiguousarray(case["Tb"], np.float64),
+                xis=np.ascontiguousarray(case["xis"], np.float64),
+                w=np.ascontiguousarray(case["weights"], np.float64),
+                rho0=np.ascontiguousarray(case["rho0"], np.float64),
+                U0=np.ascontiguousarray(case["U0"], np.float64),
+                T0=np.ascontiguousarray(case["T0"], np.float64),
+            )
+            d = CaseDesc(
+                n_points=len(keep["points"]), points=_d(keep["points"]), n_cells=int(m["n_cells"]),
+                n_faces=len(keep["off"]) - 1, n_internal_faces=len(keep["nei"]), face_offsets=_i(keep["off"]),
+                face_verts=_i(keep["fv"]), owner=_i(keep["own"]), neighbour=_i(keep["nei"]),
+                n_patches=len(keep["ps"]), patch_start=_i(keep["ps"]), patch_size=_i(keep["pn"]),
+                patch_kind=_i(keep["pk"]), wall_U=_d(keep["Ub"]), wall_T=_d(keep["Tb"]),
+                n_xi_per_dim=len(keep["xis"]), xis=_d(keep["xis"]), weights=_d(keep["w"]),
+                xi_max=float(case["xi_max"]), R=g["R"], omega=g["omega"], Tref=g["Tref"], muRef=g["muRef"],
+                Pr=g["Pr"], KInner=int(g["KInner"]), rho0=_d(keep["rho0"]), U0=_d(keep["U0"]), T0=_d(keep["T0"]),
+                precision=int(precision), pipeline=int(pipeline), device=int(device),
+            )
+            rc = self._lib.dugks_create(C.byref(d), C.byref(self._h))
+            if rc != 0:
+                raise DugksError(rc, self._lib.dugks_global_error().decode())
+        info = self.info()
+        self.nCells = info["n_cells"]
+        self.nDV = info["n_dv"]
+        self.nFaceMacros = info["n_internal_faces"] + info["n_wall_faces"]
+
+    @classmethod
+    def from_case_dir(cls, path, precision=FP64):
+        lib = load_library()
+        h = C.c_void_p()
+        rc = lib.dugks_create_from_case_dir(str(path).encode(), int(precision), C.byref(h))
+        if rc != 0:
+            raise DugksError(rc, lib.dugks_global_error().decode())
+        return cls(_handle=h)
+
+    # ------------------------------------------------------------ lifecycle
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.dugks_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc != 0:
+            raise DugksError(rc, self._lib.dugks_last_error(self._h).decode())
+
+    # ------------------------------------------------------------- controls
+    def info(self):
+        i = Info()
+        self._check(self._lib.dugks_get_info(self._h, C.byref(i)))
+        return {k: getattr(i, k) for k, _ in Info._fields_}
+
+    def set_dt(self, dt):
+        self._check(self._lib.dugks_set_dt(self._h, float(dt)))
+
+    @property
+    def dt(self):
+        v = C.c_double()
+        self._check(self._lib.dugks_get_dt(self._h, C.byref(v)))
+        return v.value
+
+    def set_stream(self, stream_ptr):
+        self._check(self._lib.dugks_set_stream(self._h, C.c_void_p(stream_ptr)))
+
+    def evolution(self, nsteps=1):
+        """fvDVM::evolution() ``nsteps`` times (asynchronous)."""
+        self._check(self._lib.dugks_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        self._check(self._lib.dugks_synchronize(self._h))
+
+    def getCoNum(self):
+        a, b = C.c_double(), C.c_double()
+        self._check(self._lib.dugks_get_conum(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    # ------------------------------------------------------------ accessors
+    def macros(self):
+        n = self.nCells
+        out = dict(rho=np.empty(n), U=np.empty((n, 3)), T=np.empty(n), q=np.empty((n, 3)), tau=np.empty(n))
+        self._check(self._lib.dugks_get_macros(self._h, *(_d(out[k]) for k in ("rho", "U", "T", "q", "tau"))))
+        return out
+
+    def macros_into(self, rho, U, T, q):
+        """Copy cell macros into caller-owned (e.g. pinned) float64 buffers."""
+        self._check(self._lib.dugks_get_macros(self._h, _d(rho), _d(U), _d(T), _d(q), None))
+
+    def rhoVol(self):
+        return self.macros()["rho"]
+
+    def Uvol(self):
+        return self.macros()["U"]
+
+    def Tvol(self):
+        return self.macros()["T"]
+
+    def qVol(self):
+        return self.macros()["q"]
+
+    def tauVol(self):
+        return self.macros()["tau"]
+
+    def face_macros(self):
+        n = self.nFaceMacros
+        out = dict(rho=np.empty(n), U=np.empty((n, 3)), T=np.empty(n), q=np.empty((n, 3)), tau=np.empty(n))
+        self._check(self._lib.dugks_get_face_macros(self._h, *(_d(out[k]) for k in ("rho", "U", "T", "q", "tau"))))
+        return out
+
+    def wall(self, patch, n_faces):
+        out = dict(rhoW=np.empty(n_faces), qWall=np.empty((n_faces, 3)), stressWall=np.empty((n_faces, 9)))
+        self._check(self._lib.dugks_get_wall(self._h, int(patch), _d(out["rhoW"]), _d(out["qWall"]),
+                                             _d(out["stressWall"])))
+        return out
+
+    def residual(self):
+        r = np.empty(3)
+        self._check(self._lib.dugks_get_residual(self._h, _d(r)))
+        return dict(U=r[0], T=r[1], rho=r[2])
+
+    def dist(self):
+        g = np.empty((self.nCells, self.nDV))
+        h = np.empty((self.nCells, self.nDV))
+        self._check(self._lib.dugks_get_dist(self._h, _d(g), _d(h)))
+        return g, h
+
+    def set_dist(self, g, h=None):
+        g = np.ascontiguousarray(g, np.float64)
+        h = None if h is None else np.ascontiguousarray(h, np.float64)
+        self._check(self._lib.dugks_set_dist(self._h, _d(g), _d(h)))
+
+    def checkpoint(self) -> bytes:
+        n = C.c_size_t()
+        self._check(self._lib.dugks_checkpoint_size(self._h, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self._check(self._lib.dugks_checkpoint_save(self._h, buf, n.value))
+        return buf.raw
+
+    def restore(self, data: bytes):
+        buf = C.create_string_buffer(data, len(data))
+        self._check(self._lib.dugks_checkpoint_load(self._h, buf, len(data)))
+
+    def profile(self, nsteps=3):
+        names = C.create_string_buffer(4096)
+        ms = np.zeros(64)
+        nk = C.c_int32()
+        self._check(self._lib.dugks_profile_step(self._h, int(nsteps), names, 4096, _d(ms), 64, C.byref(nk)))
+        nm = names.value.decode().strip().split("\n")
+        return dict(zip(nm, ms[: nk.value].tolist()))
+
+    def launches_per_step(self):
+        n = C.c_int32()
+        self._check(self._lib.dugks_launches_per_step(self._h, C.byref(n)))
+        return n.value

@@ -1,0 +1,183 @@
+/*
+ * dugks.h -- C ABI of the GB300 DUGKS time-step engine.
+ *
+ * Drop-in for the per-time-step engine of dugksFoam, class Foam::fvDVM
+ * (src/fvDVM/fvDVM/fvDVM.H:78-377).  Each entry point names the reference
+ * interface it replaces.  Plain pointers and sizes only; every call returns
+ * an int status (0 = DUGKS_OK); dugks_last_error() gives the message.
+ *
+ * Ownership: all host pointers passed in are caller-owned and copied during
+ * the call.  Device memory is owned by the handle.  A handle is not
+ * thread-safe; separate handles on separate streams are independent.
+ *
+ * Units and layouts (SI, as in the reference):
+ *   cell fields   rho[nCells], U[nCells][3], T[nCells], q[nCells][3]
+ *   face indices  internal faces 0..nInternal-1 then boundary faces in
+ *                 OpenFOAM order (patch by patch)
+ *   distribution  g[nCells][nDV] (DV index innermost; DV i = iz*M*M+iy*M+ix)
+ */
+#ifndef DUGKS_DUGKS_H
+#define DUGKS_DUGKS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DUGKS_ABI_VERSION 1
+
+typedef struct dugks_handle dugks_handle;
+
+enum dugks_status {
+    DUGKS_OK = 0,
+    DUGKS_ERR_ARG = 1,          /* invalid argument / inconsistent case   */
+    DUGKS_ERR_IO = 2,           /* case-directory parse or file error     */
+    DUGKS_ERR_UNSUPPORTED = 3,  /* boundary type or layout not supported  */
+    DUGKS_ERR_CUDA = 4,         /* CUDA runtime error / no device         */
+    DUGKS_ERR_NUMERIC = 5,      /* NaN/Inf or non-positive rho or T found */
+    DUGKS_ERR_TIMEOUT = 6,      /* a bounded device wait gave up          */
+    DUGKS_ERR_OOM = 7           /* device allocation failed               */
+};
+
+/* Storage/arithmetic precision of the distributions. */
+enum dugks_precision {
+    DUGKS_FP64 = 0,             /* plain FP64 everywhere                         */
+    DUGKS_FP32_FP64MOM = 1      /* FP32 g,h/reconstruction/fluxes; FP64 moments  */
+};
+
+/* Patch kinds: the rho boundary-condition type of 0/rho
+ * (discreteVelocity.C:274-281 maps it to the g/h surface patch type). */
+enum dugks_patch_kind {
+    DUGKS_PATCH_EMPTY = 0,      /* "empty" (2D front/back)                        */
+    DUGKS_PATCH_MAXWELL = 1     /* "calculatedMaxwell" diffuse wall (maxwellWall) */
+};
+
+/* Kernel pipeline selection (both produce the same step). */
+enum dugks_pipeline {
+    DUGKS_PIPE_AUTO = 0,        /* fused tile sweeps when supported              */
+    DUGKS_PIPE_REFERENCE = 1,   /* one kernel per reference pass                 */
+    DUGKS_PIPE_FUSED = 2        /* two fused tile sweeps per step                */
+};
+
+/* In-memory case: replaces the constructor
+ *   fvDVM(volScalarField& rho, volVectorField& U, volScalarField& T,
+ *         int* argc, char*** argv, argList& args)     fvDVM.C:886-1075
+ * plus the mesh, constant/DVMProperties, constant/Xis, constant/weights and
+ * the 0/{rho,U,T} boundary values it reads. */
+typedef struct dugks_case_desc {
+    int32_t n_points;
+    const double* points;            /* [n_points][3]                        */
+    int32_t n_cells, n_faces, n_internal_faces;
+    const int32_t* face_offsets;     /* [n_faces+1] CSR into face_verts      */
+    const int32_t* face_verts;
+    const int32_t* owner;            /* [n_faces]                            */
+    const int32_t* neighbour;        /* [n_internal_faces]                   */
+    int32_t n_patches;
+    const int32_t* patch_start;      /* [n_patches] global face index        */
+    const int32_t* patch_size;
+    const int32_t* patch_kind;       /* dugks_patch_kind                     */
+    const double* wall_U;            /* [n_faces-n_internal_faces][3]        */
+    const double* wall_T;            /* [n_faces-n_internal_faces]           */
+    int32_t n_xi_per_dim;            /* fvDVMparas.nDV                       */
+    const double* xis;               /* [n_xi_per_dim] constant/Xis          */
+    const double* weights;           /* [n_xi_per_dim] constant/weights      */
+    double xi_max;                   /* fvDVMparas.xiMax                     */
+    double R, omega, Tref, muRef, Pr;/* gasProperties                        */
+    int32_t KInner;
+    const double* rho0;              /* [n_cells] initial fields (0/rho ...) */
+    const double* U0;                /* [n_cells][3]                         */
+    const double* T0;                /* [n_cells]                            */
+    int32_t precision;               /* dugks_precision                      */
+    int32_t pipeline;                /* dugks_pipeline                       */
+    int32_t device;                  /* CUDA device ordinal                  */
+} dugks_case_desc;
+
+typedef struct dugks_info {
+    int32_t n_cells, n_faces, n_internal_faces, n_wall_faces;
+    int32_t n_dv, n_dv_padded, n_solution_d, has_h;
+    int32_t precision, pipeline;
+    double dt;
+    int64_t step_count;
+    size_t device_bytes;             /* device memory held by the handle     */
+} dugks_info;
+
+/* fvDVM::fvDVM (fvDVM.C:886-1075): build the engine from an in-memory case.
+ * g~,h~ start at the Shakhov equilibrium of (rho0,U0,T0,q=0)
+ * (discreteVelocity::initDFtoEq, discreteVelocity.C:220-249). */
+int dugks_create(const dugks_case_desc* desc, dugks_handle** out);
+
+/* fvDVM::fvDVM from an OpenFOAM case directory: constant/polyMesh/{points,faces,owner,neighbour,boundary},
+ * constant/DVMProperties, constant/Xis, constant/weights, 0/{rho,U,T},
+ * system/controlDict (deltaT).  rho patch types supported: calculatedMaxwell,
+ * empty. */
+int dugks_create_from_case_dir(const char* case_dir, int32_t precision, dugks_handle** out);
+
+int dugks_destroy(dugks_handle* h);
+const char* dugks_last_error(const dugks_handle* h);   /* never NULL */
+const char* dugks_global_error(void);                  /* last create failure */
+int dugks_get_info(dugks_handle* h, dugks_info* info);
+
+/* Time::setDeltaT as driven by setDeltaTvar.H:34-50. */
+int dugks_set_dt(dugks_handle* h, double dt);
+int dugks_get_dt(dugks_handle* h, double* dt);
+
+/* Run the CUDA work of this handle on an existing stream (cudaStream_t);
+ * NULL restores the handle's own stream. */
+int dugks_set_stream(dugks_handle* h, void* stream);
+
+/* fvDVM::evolution() (fvDVM.C:1086-1108) n times.  Asynchronous on the
+ * handle's stream; the NaN/negative-state check runs on the device and is
+ * reported by the next synchronising call (get_* / dugks_synchronize). */
+int dugks_step(dugks_handle* h, int32_t nsteps);
+int dugks_synchronize(dugks_handle* h);
+
+/* fvDVM::getCoNum (fvDVM.C:1111-1119): max and mean Courant number over
+ * internal faces with the current face velocity. */
+int dugks_get_conum(dugks_handle* h, double* max_co, double* mean_co);
+
+/* Accessors rhoVol(), Uvol(), Tvol(), qVol(), tauVol() (fvDVMI.H:26-155).
+ * Any pointer may be NULL. */
+int dugks_get_macros(dugks_handle* h, double* rho, double* U, double* T, double* q, double* tau);
+
+/* rhoSurf(), Usurf(), Tsurf(), qSurf(), tauSurf() for internal faces then
+ * wall faces (face order); empty-patch faces are not stored.  Any may be NULL. */
+int dugks_get_face_macros(dugks_handle* h, double* rho, double* U, double* T, double* q, double* tau);
+
+/* Boundary state of one patch (patch index as in the case): Maxwell-wall
+ * density rho_w (calculatedMaxwellFvPatchField value), qWall[3] and
+ * stressWall[9] per face (fvDVM.C:539-581).  Any pointer may be NULL. */
+int dugks_get_wall(dugks_handle* h, int32_t patch, double* rho_w, double* q_wall, double* stress_wall);
+
+/* Steady-state residuals of dugksFoam.C:88-107: sum|U-Uold|/sum|U|,
+ * sum|T-Told|/sum T, sum|rho-rhoOld|/sum rho against the fields saved by the
+ * previous call (or creation); then saves the current fields.
+ * res = {Uchange, TemperatureChange, rhoChange}. */
+int dugks_get_residual(dugks_handle* h, double res[3]);
+
+/* Distribution functions g~, h~ as FP64 [n_cells][n_dv] (h may be NULL).
+ * gTildeVol()/hTildeVol() of every discreteVelocity (discreteVelocity.H:85-103). */
+int dugks_get_dist(dugks_handle* h, double* g, double* hh);
+int dugks_set_dist(dugks_handle* h, const double* g, const double* hh);
+
+/* Exact-restart checkpoint: g~, h~, lagged boundary gradients, cell macros,
+ * face velocities and dt.  The reference restarts inexactly (g~ is NO_WRITE,
+ * discreteVelocity.C:76-83); this fixes it. */
+int dugks_checkpoint_size(dugks_handle* h, size_t* bytes);
+int dugks_checkpoint_save(dugks_handle* h, void* buf, size_t bytes);
+int dugks_checkpoint_load(dugks_handle* h, const void* buf, size_t bytes);
+
+/* Per-kernel device time of one step, measured with CUDA events around each
+ * launch over nsteps steps (blocking).  names receives a '\n'-separated list;
+ * ms[i] is the mean per-step time of kernel i. */
+int dugks_profile_step(dugks_handle* h, int32_t nsteps, char* names, size_t names_len,
+                       double* ms, int32_t max_kernels, int32_t* n_kernels);
+
+/* Number of kernel launches one dugks_step(h, 1) issues. */
+int dugks_launches_per_step(dugks_handle* h, int32_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

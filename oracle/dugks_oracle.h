@@ -1,0 +1,80 @@
+/*
+ * dugks_oracle.h -- TEST INFRASTRUCTURE ONLY.
+ *
+ * Plain-C FP64 restatement of dugksFoam's DUGKS time step (fvDVM::evolution,
+ * src/fvDVM/fvDVM/fvDVM.C:1086-1108) used as the parity checker for the CUDA
+ * engine and as the timed CPU baseline.  Only tests, the smoke check and the
+ * benchmark's CPU leg may load it; the product never links it.
+ *
+ * Parity status: UNPINNED at the OpenFOAM boundary.  The reference ships no
+ * tests, golden vectors or recorded outputs, and it cannot be built without
+ * OpenFOAM + MPI.  The restatement follows the reference's operation order;
+ * the OpenFOAM arithmetic it relies on (least-squares vectors, patch deltas,
+ * fixedGradient evaluation, primitiveMesh geometry) is restated from
+ * OpenFOAM >= 2.3 semantics and documented in dugks_oracle.c.
+ */
+#ifndef DUGKS_ORACLE_H
+#define DUGKS_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Patch kinds understood by the oracle (rho boundary-condition types). */
+enum {
+    ORACLE_PATCH_EMPTY = 0,              /* OpenFOAM "empty" (2D front/back) */
+    ORACLE_PATCH_MAXWELL = 1             /* rho "calculatedMaxwell" diffuse wall */
+};
+
+typedef struct oracle_case {
+    int nPoints;
+    const double* points;                /* [nPoints][3] */
+    int nCells, nFaces, nInternalFaces;
+    const int* faceOffsets;              /* [nFaces+1] */
+    const int* faceVerts;
+    const int* owner;                    /* [nFaces] */
+    const int* neighbour;                /* [nInternalFaces] */
+    int nPatches;
+    const int* patchStart;               /* [nPatches] global face index */
+    const int* patchSize;
+    const int* patchKind;                /* ORACLE_PATCH_* */
+    const double* Ub;                    /* [nFaces-nInternalFaces][3] wall U */
+    const double* Tb;                    /* [nFaces-nInternalFaces]    wall T */
+    int nXiPerDim;
+    const double* xis;                   /* [nXiPerDim] 1-D nodes  (constant/Xis) */
+    const double* weights;               /* [nXiPerDim] 1-D weights (constant/weights) */
+    double xiMax;                        /* DVMProperties fvDVMparas.xiMax */
+    double R, omega, Tref, muRef, Pr;
+    int KInner;
+    const double* rho0;                  /* [nCells] */
+    const double* U0;                    /* [nCells][3] */
+    const double* T0;                    /* [nCells] */
+} oracle_case;
+
+void* oracle_create(const oracle_case* c);
+void  oracle_destroy(void* h);
+void  oracle_set_threads(int n);
+int   oracle_nsolutiond(void* h);
+int   oracle_ndv(void* h);
+/* One or more DUGKS steps with a fixed dt (fvDVM::evolution per step). */
+void  oracle_step(void* h, double dt, int nsteps);
+void  oracle_get_cell(void* h, double* rho, double* U, double* T, double* q, double* tau);
+/* Face macros for internal faces followed by every boundary face (empty ones zero). */
+void  oracle_get_face(void* h, double* rho, double* U, double* T, double* q, double* tau);
+/* Per boundary face: rho boundary value (Maxwell-wall density), qWall, stressWall[9]. */
+void  oracle_get_wall(void* h, double* rhoW, double* qWall, double* stressWall);
+/* g~, h~ in DV-outer layout [nDV][nCells]. */
+void  oracle_get_dist(void* h, double* g, double* hh);
+void  oracle_set_dist(void* h, const double* g, const double* hh);
+/* Geometry as the fv layer sees it (for host-geometry parity tests). */
+void  oracle_get_geometry(void* h, double* C, double* V, double* Cf, double* Sf,
+                          double* pVec, double* nVec, double* bVec, double* deltaCoeffs);
+/* Discrete velocity set as built by fvDVM::initialiseDV. */
+void  oracle_get_dv(void* h, double* xi, double* w);
+/* fvDVM::getCoNum over internal faces with the current face velocity. */
+void  oracle_conum(void* h, double dt, double* maxCo, double* meanCo);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,165 @@
+"""GPU parity: the CUDA engine through the C ABI vs the FP64 CPU oracle.
+
+Tolerances (field-normalised, vector fields by magnitude of the difference):
+  plain FP64 path                 <= 1e-12 (L-inf and L2) on rho, U, T, q
+  FP32 bulk / FP64 moments path   <= 1e-5
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("rho", "U", "T", "q")
+TOL64 = 1e-12
+TOL32 = 1e-5
+
+
+def _small_cases():
+    from dugksfoam_gb300 import cases
+
+    return {
+        "quad12": (cases.cavity2d(n=12, nxi=8), 20),
+        "tri": (cases.make_case(cases.delaunay_mesh(300, 12, seed=3), *cases.gas_from_kn(0.05), 8,
+                                4.0 * np.sqrt(2 * 208.0 * 273.0)), 20),
+        "hex5": (cases.cavity3d(n=5, nxi=6), 10),
+    }
+
+
+def _run_pair(case, steps, precision, pipeline=0):
+    from dugksfoam_gb300 import cases, solver
+    from oracle.oracle import Oracle
+
+    dt = cases.stable_dt(case)
+    ref = Oracle(case)
+    ref.step(dt, steps)
+    s = solver.FvDVM(case, precision=precision, pipeline=pipeline)
+    s.set_dt(dt)
+    s.evolution(steps)
+    return s, ref
+
+
+@pytest.mark.parametrize("name", ["quad12", "tri", "hex5"])
+def test_fp64_reference_pipeline_matches_oracle(built_lib, oracle_lib, name):
+    from dugksfoam_gb300 import solver
+
+    case, steps = _small_cases()[name]
+    s, ref = _run_pair(case, steps, solver.FP64, solver.PIPE_REFERENCE)
+    got, want = s.macros(), ref.cell()
+    for k in FIELDS:
+        einf, el2 = rel_err(got[k], want[k])
+        assert einf <= TOL64 and el2 <= TOL64, (name, k, einf, el2)
+    # face macros and wall state
+    fm = s.face_macros()
+    of = ref.face()
+    nI = len(case["mesh"]["neighbour"])
+    wall_faces = [p for p in case["mesh"]["patches"] if p["type"] == "wall"]
+    glob = list(range(nI)) + [f for p in wall_faces for f in range(p["startFace"], p["startFace"] + p["nFaces"])]
+    for k in ("rho", "T"):
+        einf, _ = rel_err(fm[k], of[k][glob])
+        assert einf <= TOL64, ("face", k, einf)
+    ow = ref.wall()
+    for pi, p in enumerate(case["mesh"]["patches"]):
+        if p["type"] != "wall":
+            continue
+        w = s.wall(pi, p["nFaces"])
+        sl = slice(p["startFace"] - nI, p["startFace"] - nI + p["nFaces"])
+        assert rel_err(w["rhoW"], ow["rhoW"][sl])[0] <= TOL64
+        assert rel_err(w["qWall"], ow["qWall"][sl])[0] <= 1e-11
+        assert rel_err(w["stressWall"], ow["stressWall"][sl])[0] <= TOL64
+    s.close()
+
+
+def test_fp64_distribution_matches_oracle(built_lib, oracle_lib):
+    from dugksfoam_gb300 import solver
+
+    case, _ = _small_cases()["quad12"]
+    s, ref = _run_pair(case, 7, solver.FP64, solver.PIPE_REFERENCE)
+    g, h = s.dist()
+    og, oh = ref.dist()
+    assert np.abs(g - og.T).max() / np.abs(og).max() <= TOL64
+    assert np.abs(h - oh.T).max() / np.abs(oh).max() <= TOL64
+
+
+def test_conum_and_residual(built_lib, oracle_lib):
+    from dugksfoam_gb300 import cases, solver
+    from oracle.oracle import Oracle
+
+    case = cases.cavity2d(n=12, nxi=8)
+    dt = cases.stable_dt(case)
+    s = solver.FvDVM(case, precision=solver.FP64, pipeline=solver.PIPE_REFERENCE)
+    s.set_dt(dt)
+    ref = Oracle(case)
+    mx, mean = s.getCoNum()
+    omx, omean = ref.conum(dt)
+    assert abs(mx - omx) <= 1e-13 * omx and abs(mean - omean) <= 1e-13 * omean
+    s.evolution(3)
+    ref.step(dt, 3)
+    mx, mean = s.getCoNum()
+    omx, omean = ref.conum(dt)
+    assert abs(mx - omx) <= 1e-12 * omx and abs(mean - omean) <= 1e-12 * omean
+    r = s.residual()
+    m0 = case["U0"], case["T0"], case["rho0"]
+    c = ref.cell()
+    wantU = np.linalg.norm(c["U"] - m0[0], axis=1).sum() / np.linalg.norm(c["U"], axis=1).sum()
+    wantT = np.abs(c["T"] - m0[1]).sum() / c["T"].sum()
+    assert abs(r["U"] - wantU) <= 1e-10 * wantU
+    assert abs(r["T"] - wantT) <= 1e-10 * wantT
+    s.close()
+
+
+def test_checkpoint_restart_is_exact(built_lib):
+    from dugksfoam_gb300 import cases, solver
+
+    case = cases.cavity2d(n=10, nxi=8)
+    dt = cases.stable_dt(case)
+    a = solver.FvDVM(case, precision=solver.FP64, pipeline=solver.PIPE_REFERENCE)
+    a.set_dt(dt)
+    a.evolution(5)
+    ck = a.checkpoint()
+    a.evolution(5)
+    want = a.macros()
+    b = solver.FvDVM(case, precision=solver.FP64, pipeline=solver.PIPE_REFERENCE)
+    b.restore(ck)
+    assert b.dt == dt
+    b.evolution(5)
+    got = b.macros()
+    for k in FIELDS:
+        assert np.array_equal(got[k], want[k]), k
+
+
+def test_dist_roundtrip_and_determinism(built_lib):
+    from dugksfoam_gb300 import cases, solver
+
+    case = cases.cavity2d(n=8, nxi=8)
+    dt = cases.stable_dt(case)
+    runs = []
+    for _ in range(2):
+        s = solver.FvDVM(case, precision=solver.FP64, pipeline=solver.PIPE_REFERENCE)
+        s.set_dt(dt)
+        s.evolution(4)
+        runs.append(s.macros())
+        g, h = s.dist()
+        s.set_dist(g, h)
+        g2, h2 = s.dist()
+        assert np.array_equal(g, g2) and np.array_equal(h, h2)
+        s.close()
+    for k in FIELDS:
+        assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+def test_nan_state_is_reported(built_lib):
+    from dugksfoam_gb300 import cases, solver
+
+    case = cases.cavity2d(n=6, nxi=6)
+    s = solver.FvDVM(case, precision=solver.FP64, pipeline=solver.PIPE_REFERENCE)
+    s.set_dt(cases.stable_dt(case))
+    g, h = s.dist()
+    g[3, :] = np.nan
+    s.set_dist(g, h)
+    s.evolution(1)
+    with pytest.raises(solver.DugksError) as ei:
+        s.synchronize()
+    assert ei.value.code == 5
+    s.close()
