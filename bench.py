@@ -1,0 +1,316 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 DUGKS engine (one JSON line on stdout).
+
+Workload: the 2D unstructured lid-driven cavity -- ~100k seeded Delaunay
+triangles (prisms), 32x32 discrete velocities, Kn 0.01 -- advanced with the
+FP32-bulk / FP64-moment fused pipeline.  A "step" is one fvDVM::evolution()
+(src/fvDVM/fvDVM/fvDVM.C:1086-1108) over every cell and velocity.
+
+  value      cell*DV updates/s with the state resident in HBM (CUDA events on
+             the engine's stream, max over ranks; the state, 819 MB of FP32 g
+             and h, is larger than L2, so no flush is needed between steps)
+  e2e        the same metric through the C ABI as dugksFoam's time loop uses
+             the engine: per step dugks_get_conum (D2H), dugks_set_dt (H2D),
+             dugks_step, dugks_get_macros into pinned host buffers (D2H)
+  fp64_plain the plain FP64 pipeline on the same workload (fewer steps)
+  roofline   the dominant kernel (k_sweep_cell) against measured HBM bandwidth
+  cpu_baseline the FP64 CPU oracle (a restatement of the reference step) on a
+             bounded sample of the same workload, all host threads
+
+--impl reference times that CPU restatement alone (the reference solver
+itself needs OpenFOAM + MPI, which are not available).
+Multi-GPU: the step does not shard across GPUs in this engine; --gpus N runs
+N independent replicas (weak scaling), one per rank.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell*DV updates/s FP32+FP64-moment vs plain FP64, same GB300, <=1e-5 rel err"
+UNIT = "cell*DV updates/s"
+ALG_BYTES = {"k_sweep_cell": 16, "k_sweep_face": 8}  # FP32 g,h per cell*DV: read (+write)
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                if out.returncode == 0 and out.stdout.strip():
+                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _allreduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def make_case(args):
+    from dugksfoam_gb300 import cases
+
+    if args.workload == "delaunay2d":
+        return cases.delaunay2d(), "delaunay2d: ~100k Delaunay triangles (seed 0), 32x32 DV, Kn 0.01"
+    if args.workload == "cavity2d":
+        return cases.cavity2d(61, nxi=28), "cavity2d: 61x61 quads, 28x28 DV, Kn 0.075"
+    if args.workload == "cavity3d":
+        return cases.cavity3d(48, nxi=20), "cavity3d: 48^3 hexes, 20^3 DV, Kn 0.1"
+    raise SystemExit(f"unknown workload {args.workload}")
+
+
+def run_reference(args):
+    """CPU restatement of the reference step (FP64 oracle) on a bounded sample."""
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import Oracle
+
+    case, desc = make_case(args)
+    threads = os.cpu_count() or 1
+    o = Oracle(case, threads=threads)
+    dt = cases.case_dt(case)
+    n = o.nC * o.nV
+    for _ in range(args.warmup):
+        o.step(dt, 1)
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        o.step(dt, 1)
+    el = time.perf_counter() - t
+    v = n * args.steps / el
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": desc, "cells": o.nC, "dvs": o.nV},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full steps of the workload (FP64 oracle, OpenMP)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(case, seconds=15.0):
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import Oracle
+
+    threads = os.cpu_count() or 1
+    o = Oracle(case, threads=threads)
+    dt = cases.case_dt(case)
+    o.step(dt, 1)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        o.step(dt, 1)
+        steps += 1
+        if time.perf_counter() - t0 > seconds or steps >= 20:
+            break
+    el = time.perf_counter() - t0
+    return {"value": o.nC * o.nV * steps / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{steps} full steps of the same workload after 1 warm-up step (FP64 oracle, OpenMP)"}
+
+
+def run_engine(args):
+    import torch
+
+    from dugksfoam_gb300 import cases, solver
+
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    case, desc = make_case(args)
+    dt = cases.case_dt(case)
+    s = solver.FvDVM(case, precision=solver.FP32_FP64MOM, pipeline=solver.PIPE_FUSED, device=local)
+    stream = torch.cuda.Stream()
+    s.set_stream(stream.cuda_stream)
+    s.set_dt(dt)
+    info = s.info()
+    n_upd = s.nCells * s.nDV
+    # warm-up
+    s.evolution(args.warmup)
+    s.synchronize()
+    # ---- device-resident throughput (CUDA events on the engine's stream)
+    _barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk, torch.cuda.stream(stream):
+        e0.record(stream)
+        s.evolution(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    _barrier(world)
+    ms = e0.elapsed_time(e1)
+    ms = _allreduce_max(ms, world)
+    s.synchronize()
+    value = n_upd * args.steps * world / (ms / 1e3)
+    # ---- per-kernel times (CUDA events around each launch) for the roofline
+    prof = s.profile(3)
+    # ---- end to end through the C ABI with host buffers (pinned)
+    nC = s.nCells
+    hb = {k: torch.empty(sz, dtype=torch.float64, pin_memory=True).numpy()
+          for k, sz in (("rho", nC), ("U", 3 * nC), ("T", nC), ("q", 3 * nC))}
+    ek = max(3, args.steps // 2)
+    _barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ek):
+        s.getCoNum()
+        s.set_dt(dt)
+        s.evolution(1)
+        s.macros_into(hb["rho"], hb["U"], hb["T"], hb["q"])
+    t_e2e = _allreduce_max(time.perf_counter() - t0, world)
+    e2e = n_upd * ek * world / t_e2e
+    d2h = sum(a.nbytes for a in hb.values()) + 16
+    # ---- plain FP64 pipeline on the same workload (rank 0 only)
+    fp64 = None
+    if rank == 0 and not args.skip_fp64:
+        s64 = solver.FvDVM(case, precision=solver.FP64, pipeline=solver.PIPE_REFERENCE, device=local)
+        st64 = torch.cuda.Stream()
+        s64.set_stream(st64.cuda_stream)
+        s64.set_dt(dt)
+        s64.evolution(1)
+        s64.synchronize()
+        k64 = max(2, args.steps // 5)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(st64)
+        s64.evolution(k64)
+        a1.record(st64)
+        a1.synchronize()
+        ms64 = a0.elapsed_time(a1)
+        fp64 = {"value": n_upd * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
+                "pipeline": "reference (one FP64 kernel per fvDVM pass)"}
+        s64.close()
+    if rank != 0:
+        return
+    peak, peak_kind = _peaks()
+    dom = max(prof, key=prof.get)
+    alg = ALG_BYTES.get(dom, 16) * n_upd
+    achieved = alg / (prof[dom] / 1e3) / 1e9
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic_per_cell_dv.json")
+    if os.path.exists(tfile):
+        try:
+            tb = json.load(open(tfile)).get(dom)
+            traffic = tb * n_upd if tb else None
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 distributions, f64 moments", "data": "synthetic",
+        "config": {"workload": desc, "cells": s.nCells, "dvs": s.nDV, "dv_padded": info["n_dv_padded"],
+                   "state_bytes": int(2 * 4 * s.nCells * info["n_dv_padded"]),
+                   "l2": "state larger than the 129 MB L2; no flush needed", "dt": dt,
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                     "alg_bytes_per_cell_dv": ALG_BYTES.get(dom, 16),
+                     "step_frac": 16 * value / world / 1e9 / peak},
+        "kernels_ms": prof,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8, "d2h_bytes_per_step": d2h},
+        "gpu_launches": s.launches_per_step() * args.steps,
+        "clocks": clk.summary(),
+        "fp64_plain": fp64,
+        "speedup_vs_fp64_plain": (value / world / fp64["value"]) if fp64 else None,
+    }
+    s.close()
+    if not args.skip_cpu:
+        line["cpu_baseline"] = cpu_baseline(case, seconds=args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--workload", default="delaunay2d", choices=["delaunay2d", "cavity2d", "cavity3d"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

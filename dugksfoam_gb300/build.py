@@ -17,6 +17,13 @@ ROOT = os.path.dirname(PKG)
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libdugks.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# FP64 translation units are built without FMA contraction so the plain FP64
+# path performs the same roundings as the CPU oracle, operation by operation.
+EXTRA = {
+    "ref_pipeline.cu": ["-fmad=false"],
+    "common_kernels.cu": ["-fmad=false"],
+    "fused_fp64.cu": ["-fmad=false"],
+}
 
 
 def _nvcc():
@@ -54,7 +61,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
             cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xptxas", "-v" if verbose else "-O3",
-                   *inc, "-c", src, "-o", obj]
+                   *EXTRA.get(os.path.basename(src), []), *inc, "-c", src, "-o", obj]
             jobs.append(cmd)
     for src in cpp:
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")

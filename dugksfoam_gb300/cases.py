@@ -32,7 +32,7 @@ from .dvgrid import gauss_hermite_half_range, newton_cotes
 
 __all__ = [
     "gas_from_kn", "structured_mesh", "delaunay_mesh", "make_case", "cavity2d",
-    "delaunay2d", "cavity3d", "batch_instances", "stable_dt", "mesh_info",
+    "delaunay2d", "cavity3d", "batch_instances", "stable_dt", "cell_stable_dt", "case_dt", "mesh_info",
 ]
 
 K_BOLTZ = 1.38066e-23
@@ -329,6 +329,37 @@ def stable_dt(case, cfl=0.5):
     return cfl / (dc.max() * math.sqrt(D) * case["xi_max"])
 
 
+def cell_stable_dt(case, cfl=0.5):
+    """dt with a cell-based Courant number: cfl * min_c(V_c / sum_f |S_f|) / (sqrt(D) xi_max).
+
+    Used for unstructured meshes, where the centroid-distance Courant number of
+    fvDVM::getCoNum under-estimates the stiffness of sliver cells (random
+    Delaunay triangulations are unstable at the reference rule, even at 1/4).
+    """
+    from .geometry import cell_centres_volumes, face_centres_areas
+
+    mesh = case["mesh"]
+    _, V = cell_centres_volumes(mesh)
+    _, Sf = face_centres_areas(mesh)
+    nI = len(mesh["neighbour"])
+    own = np.asarray(mesh["owner"])
+    active = np.ones(len(own), bool)
+    for p in mesh["patches"]:
+        if p["type"] == "empty":
+            active[p["startFace"]:p["startFace"] + p["nFaces"]] = False
+    A = np.linalg.norm(Sf, axis=1)
+    area = np.zeros(mesh["n_cells"])
+    np.add.at(area, own[active], A[active])
+    np.add.at(area, np.asarray(mesh["neighbour"]), A[:nI])
+    D = 2 if case["two_d"] else 3
+    return cfl * (V / area).min() / (math.sqrt(D) * case["xi_max"])
+
+
+def case_dt(case, cfl=0.5):
+    """The time step a workload runs at: cell-based for unstructured meshes."""
+    return cell_stable_dt(case, cfl) if case.get("unstructured") else stable_dt(case, cfl)
+
+
 def cavity2d(n=61, Kn=0.075, nxi=28, bottom_patch=False, lid_u=50.0, Tw=None):
     """2D lid-driven cavity on n x n quads (default: the 61^2, 28^2-DV case)."""
     gas, rho0 = gas_from_kn(Kn)
@@ -342,7 +373,9 @@ def delaunay2d(n_interior=49200, n_side=400, seed=0, Kn=0.01, nxi=32):
     gas, rho0 = gas_from_kn(Kn)
     xi_max = 4.0 * math.sqrt(2 * gas["R"] * 273.0)
     mesh = delaunay_mesh(n_interior, n_side, seed)
-    return make_case(mesh, gas, rho0, nxi, xi_max, two_d=True)
+    case = make_case(mesh, gas, rho0, nxi, xi_max, two_d=True)
+    case["unstructured"] = True
+    return case
 
 
 def cavity3d(n=48, Kn=0.1, nxi=20):

@@ -1,0 +1,431 @@
+// Fused tile sweeps of one DUGKS step (fvDVM::evolution, fvDVM.C:1086-1108).
+//
+// One CTA owns one tile T of cells plus its two-ring halo (H1, H2) and walks
+// the discrete-velocity axis in chunks of KC = 32*NPL velocities (lane <-> DV,
+// the DV index is innermost in HBM so every row load is coalesced).
+//
+// Sweep A (k_sweep_face): per chunk
+//   1. g~ rows of T u H1 u H2 -> gbar+ = (1-a) g~ + a g^S(cell macros) in smem
+//      (P1 updateGHbarPvol, discreteVelocity.C:346-410);
+//   2. for every face owned by T: least-squares gradient of the upwind cell
+//      recomputed from smem (P2, discreteVelocity.C:420-470), upwind linear
+//      reconstruction with the -xi dt/2 shift (P3, :472-691), lagged boundary
+//      gradient update on walls, and the face moments (per-lane products,
+//      warp reduce-scatter, compensated accumulation per face in smem).
+//   After the chunk loop (FP64): Maxwell-wall density (P4, fvDVM.C:347-367),
+//   incoming wall moments rho_w * M (P5), face macros rho,U,T,tau,q (P6, :456-582).
+// Sweep B (k_sweep_cell): per chunk
+//   1. gbar+ rows again; g~new partial = -1/3 g~ + 4/3 gbar+ for T;
+//   2. face values again, relaxed toward the face Shakhov equilibrium
+//      (P7, discreteVelocity.C:819-932; incoming wall DVs stay unrelaxed),
+//      flux (xi.S) g_f dt/V scattered into T's rows colour by colour (no two
+//      faces of a colour share a cell: deterministic, no atomics) (P8, :934-978);
+//   3. g~new written to HBM, cell moments accumulated (P9, fvDVM.C:597-728).
+//   After the chunk loop (FP64): cell macros rho,U,T,tau,q for the next step.
+//
+// Moments are accumulated about a reference velocity Uref (previous face /
+// cell velocity, or the wall velocity), so the heat flux needs one pass:
+//   q_i = 1/2 [M3_i - 2 M2_ij d_j + M1_i |d|^2 - d_i tr M2 + 2 d_i (M1.d)
+//              - d_i |d|^2 M0] + 1/2 (H1_i - d_i H0),   d = M1/M0 = U - Uref.
+//
+// FP32 path: no FP64 instruction runs inside the chunk loops (GB300 issues
+// FP64 at 1/64 of the FP32 rate); per-chunk warp totals are added into an
+// FP32 Kahan pair per face/cell and finished in FP64.
+#pragma once
+
+#include "../host/tile_plan.h"
+#include "device_common.cuh"
+#include "fused.h"
+
+namespace dugks {
+
+// float coefficient block of one cell or face equilibrium (FP32 path)
+constexpr int kNCoef = 12;  // U[3], kexp, invRT, qk[3], A, RT, tau, pad
+
+template <typename S>
+struct FusedArgs {
+    StepArgs b;                 // FP64 geometry, current macros, walls
+    S dt;                       // dt in storage precision
+    // tile plan
+    const TileHdr* hdr;
+    const int* cells;
+    const TileFace* faces;
+    const int* colorOff;
+    const int* colorPerm;
+    // stencils: FP32 packs (Lx, Ly, Lz, other) in a float4; FP64 uses stEnt/stL
+    const float4* st4;
+    const int* stEnt;
+    const double* stL;
+    // face geometry: FP32 [rec][3] float4 {S,1/Vo} {dO,1/Vn} {dN or wall normal};
+    // FP64 [rec][9] S, dO, dN
+    const float4* fg4;
+    const double* fgeo;
+    // discrete velocities
+    const S* xi;                // [3][Vp]
+    const S* w;                 // [Vp]
+    // distributions
+    const S* gT;
+    const S* hT;
+    S* gTn;
+    S* hTn;
+    const S* Gbg;               // [nW][Vp] lagged gradient (current)
+    const S* Gbh;
+    S* Gbgn;                    // next
+    S* Gbhn;
+    const S* Mw;                // [nW][Vp] wall Maxwellian / rho
+    const double* Min;          // [nW][NS] incoming moments of Mw about Uw
+    // FP32 side data
+    const float4* wall4;        // [nW] {R Tw (K+3-D), 1/deltaCoeff, 0, 0}
+    float* rhoWs;               // [nW] scaled rho_w (written by sweep A)
+    float4* uref4;              // [nA] face reference velocity (walls: U_w)
+    const float* cc;            // [nC][kNCoef] current cell equilibrium block
+    float* ccn;                 // next
+    float* fc;                  // [nA][kNCoef] face equilibrium (written by sweep A)
+    // macros of the next step
+    double *rhoN, *UN, *TN, *qN, *tauN;
+    double gscale, invGscale;
+};
+
+template <int D, bool H>
+struct Slots {
+    static constexpr int NM = 1 + D + D * (D + 1) / 2 + D + (H ? 1 + D : 0);
+    static constexpr int NS = NM + 1 <= 16 ? 16 : 32;   // + outgoing wall flux
+    static constexpr int M1 = 1;
+    static constexpr int M2 = 1 + D;                   // xx,xy,(xz),yy,(yz),(zz)
+    static constexpr int M3 = M2 + D * (D + 1) / 2;
+    static constexpr int H0 = M3 + D;
+    static constexpr int H1 = H0 + 1;
+    static constexpr int FLUX = NM;
+};
+
+// symmetric index of M2 component (i<=j) in the packed order
+template <int D>
+__host__ __device__ __forceinline__ constexpr int sym(int i, int j) {
+    return D == 2 ? (i == 0 ? j : 2) : (i == 0 ? j : (i == 1 ? 2 + j : 5));
+}
+
+// Reduce NS per-lane values over the warp; afterwards lane holds the total of
+// slot slot_of(lane) (lanes 2k and 2k+1 hold the same slot when NS == 16).
+template <int NS, typename T>
+__device__ __forceinline__ T reduce_scatter(T (&v)[NS], int lane) {
+#pragma unroll
+    for (int half = NS / 2, xm = 16; half >= 1; half >>= 1, xm >>= 1) {
+        const bool up = lane & xm;
+#pragma unroll
+        for (int i = 0; i < half; ++i) {
+            T send = up ? v[i] : v[i + half];
+            T keep = up ? v[i + half] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, xm);
+        }
+    }
+    T r = v[0];
+    if (NS == 16) r += __shfl_xor_sync(0xffffffffu, r, 1);
+    return r;
+}
+template <int NS>
+__device__ __forceinline__ int slot_of(int lane) {
+    return NS == 16 ? (((lane >> 4) & 1) << 3) | (((lane >> 3) & 1) << 2) | (((lane >> 2) & 1) << 1) |
+                          ((lane >> 1) & 1)
+                    : (((lane >> 4) & 1) << 4) | (((lane >> 3) & 1) << 3) | (((lane >> 2) & 1) << 2) |
+                          (((lane >> 1) & 1) << 1) | (lane & 1);
+}
+
+// Moment accumulator cell in smem: FP64 for the FP64 path, Kahan pair for FP32.
+template <typename S>
+struct Acc;
+template <>
+struct Acc<double> {
+    double s;
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ double value() const { return s; }
+    __device__ __forceinline__ void zero() { s = 0.0; }
+};
+template <>
+struct Acc<float> {
+    float s, c;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    __device__ __forceinline__ void zero() { s = 0.0f; c = 0.0f; }
+};
+
+// ---------------------------------------------------------------- equilibria
+// Relaxation toward the Shakhov equilibrium of a cell (weight 1.5dt/(2tau+dt))
+// or a face (weight h/(2tau+h), h = dt/2): out = (1-a) in + a g^S.
+template <typename S, int D, bool H>
+struct Relax;
+
+template <int D, bool H>
+struct Relax<double, D, H> {
+    double rho, U[3], T, q[3], a;
+    double R, Pr;
+    int K;
+    __device__ __forceinline__ void loadCell(const FusedArgs<double>& A, int c) {
+        const StepArgs& b = A.b;
+        const double dt = b.dt;
+        rho = b.rho[c]; T = b.T[c];
+        for (int k = 0; k < 3; ++k) { U[k] = b.U[3 * c + k]; q[k] = b.q[3 * c + k]; }
+        a = 1.5 * dt / (2.0 * b.tau[c] + dt);
+        R = b.R; Pr = b.Pr; K = b.K;
+    }
+    __device__ __forceinline__ void loadFace(const FusedArgs<double>& A, int f) {
+        const StepArgs& b = A.b;
+        rho = b.rhoF[f]; T = b.TF[f];
+        for (int k = 0; k < 3; ++k) { U[k] = b.UF[3 * f + k]; q[k] = b.qF[3 * f + k]; }
+        const double hh = 0.5 * b.dt;
+        a = hh / (2 * b.tauF[f] + hh);
+        R = b.R; Pr = b.Pr; K = b.K;
+    }
+    __device__ __forceinline__ void apply(const double* xi, double& g, double& h) const {
+        double ge, he;
+        shakhov_ref(rho, U[0], U[1], U[2], T, q[0], q[1], q[2], xi[0], xi[1], D == 3 ? xi[2] : 0.0, R, Pr, D, K,
+                    ge, he);
+        g = (1.0 - a) * g + a * ge;
+        if (H) h = (1.0 - a) * h + a * he;
+    }
+};
+
+template <int D, bool H>
+struct Relax<float, D, H> {
+    float U[3], kexp, invRT, qk[3], a, aA, RT;
+    float KD, K2;
+    __device__ __forceinline__ void loadBlock(const float* blk, float aw, int K) {
+        const float4 b0 = reinterpret_cast<const float4*>(blk)[0];
+        const float4 b1 = reinterpret_cast<const float4*>(blk)[1];
+        const float4 b2 = reinterpret_cast<const float4*>(blk)[2];
+        U[0] = b0.x; U[1] = b0.y; U[2] = b0.z; kexp = b0.w;
+        invRT = b1.x; qk[0] = b1.y; qk[1] = b1.z; qk[2] = b1.w;
+        RT = b2.y;
+        a = aw;
+        aA = aw * b2.x;
+        KD = (float)(K + 3 - D);
+        K2 = -2.0f * (float)K;
+    }
+    __device__ __forceinline__ void loadCell(const FusedArgs<float>& A, int c) {
+        const float* blk = A.cc + (size_t)c * kNCoef;
+        const float tau = blk[10];
+        loadBlock(blk, 1.5f * A.dt / (2.0f * tau + A.dt), A.b.K);
+    }
+    __device__ __forceinline__ void loadFace(const FusedArgs<float>& A, int f) {
+        const float* blk = A.fc + (size_t)f * kNCoef;
+        const float tau = blk[10];
+        const float hh = 0.5f * A.dt;
+        loadBlock(blk, hh / (2.0f * tau + hh), A.b.K);
+    }
+    // g <- g - a g + a g^S: the weight 1-a is never formed, so a state already
+    // at equilibrium is a fixed point in FP32 (no per-step mass bias).
+    __device__ __forceinline__ void apply(const float* xi, float& g, float& h) const {
+        const float cx = xi[0] - U[0], cy = xi[1] - U[1];
+        const float cz = D == 3 ? xi[2] - U[2] : 0.0f;
+        const float c2 = D == 3 ? fmaf(cz, cz, fmaf(cy, cy, cx * cx)) : fmaf(cy, cy, cx * cx);
+        const float e = exp2f(kexp * c2) * aA;
+        const float phi = D == 3 ? fmaf(cz, qk[2], fmaf(cy, qk[1], cx * qk[0])) : fmaf(cy, qk[1], cx * qk[0]);
+        const float c2n = c2 * invRT;
+        g = fmaf(-a, g, g) + fmaf(e * phi, c2n - (float)(D + 2), e);
+        if (H) {
+            const float eh = e * RT;
+            h = fmaf(-a, h, h) + fmaf(eh * phi, fmaf(c2n - (float)D, KD, K2), eh * KD);
+        }
+    }
+};
+
+// ------------------------------------------------------------- gradient
+// Least-squares gradient of gbar+ at a local cell from its stencil entries
+// [e0, e1) (global face order), smem column col.
+template <typename S, int D, bool H>
+__device__ __forceinline__ void stencil_grad(const FusedArgs<S>& A, int e0, int e1, S gc, S hc, const S* sg,
+                                             const S* sh, int KC, int col, int v, S* gg, S* hg) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) { gg[k] = S(0); if (H) hg[k] = S(0); }
+    for (int e = e0; e < e1; ++e) {
+        if constexpr (sizeof(S) == 4) {
+            const float4 ent = A.st4[e];
+            const int o = __float_as_int(ent.w);
+            float dg, dh = 0.0f;
+            if (o >= 0) {
+                dg = sg[o * KC + col] - gc;
+                if (H) dh = sh[o * KC + col] - hc;
+            } else {
+                const int wf = -o - 1;
+                const float idc = A.wall4[wf].y;
+                dg = A.Gbg[(size_t)wf * A.b.Vp + v] * idc;
+                if (H) dh = A.Gbh[(size_t)wf * A.b.Vp + v] * idc;
+            }
+            gg[0] = fmaf(ent.x, dg, gg[0]);
+            gg[1] = fmaf(ent.y, dg, gg[1]);
+            if (D == 3) gg[2] = fmaf(ent.z, dg, gg[2]);
+            if (H) {
+                hg[0] = fmaf(ent.x, dh, hg[0]);
+                hg[1] = fmaf(ent.y, dh, hg[1]);
+                if (D == 3) hg[2] = fmaf(ent.z, dh, hg[2]);
+            }
+        } else {
+            const int o = A.stEnt[e];
+            double dg, dh = 0.0;
+            if (o >= 0) {
+                dg = sg[o * KC + col] - gc;
+                if (H) dh = sh[o * KC + col] - hc;
+            } else {  // fixedGradient evaluate, then difference (reference order)
+                const int wf = -o - 1;
+                const size_t wi = (size_t)wf * A.b.Vp + v;
+                const double dc = A.b.dcW[wf];
+                dg = (gc + A.Gbg[wi] / dc) - gc;
+                if (H) dh = (hc + A.Gbh[wi] / dc) - hc;
+            }
+            const double* L = A.stL + 3 * (size_t)e;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                gg[k] += L[k] * dg;
+                if (H) hg[k] += L[k] * dh;
+            }
+        }
+    }
+}
+
+// gbar+ + grad . (d - xi dt/2)
+template <typename S, int D>
+__device__ __forceinline__ S recon(S base, const S* grad, const S* d, const S* xi, S dt) {
+    S acc = S(0);
+#pragma unroll
+    for (int k = 0; k < D; ++k) acc += grad[k] * (d[k] - S(0.5) * xi[k] * dt);
+    return base + acc;
+}
+
+// Face data of one tile-face record in registers.
+template <typename S>
+struct FaceGeo {
+    S Sv[3], dO[3], dN[3];
+    S invVo, invVn;
+    __device__ __forceinline__ void load(const FusedArgs<S>& A, int rec) {
+        if constexpr (sizeof(S) == 4) {
+            const float4 a = A.fg4[3 * (size_t)rec], b = A.fg4[3 * (size_t)rec + 1], c = A.fg4[3 * (size_t)rec + 2];
+            Sv[0] = a.x; Sv[1] = a.y; Sv[2] = a.z; invVo = a.w;
+            dO[0] = b.x; dO[1] = b.y; dO[2] = b.z; invVn = b.w;
+            dN[0] = c.x; dN[1] = c.y; dN[2] = c.z;
+        } else {
+            const double* g = A.fgeo + 9 * (size_t)rec;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) { Sv[k] = g[k]; dO[k] = g[3 + k]; dN[k] = g[6 + k]; }
+            invVo = invVn = 0.0;
+        }
+    }
+};
+
+// Face value gbar_f (and hbar_f) for one DV of face record r.  For walls with
+// xi.S <= 0 nothing is computed (the value is rho_w * M) and false is returned.
+template <typename S, int D, bool H>
+__device__ __forceinline__ bool face_value(const FusedArgs<S>& A, const TileFace& r, const FaceGeo<S>& fg,
+                                           const S* sg, const S* sh, int KC, int col, int v, const S* xi, S xs,
+                                           S& gf, S& hf) {
+    S gg[D], hg[D];
+    const S dt = A.dt;
+    if (r.w >= 0) {
+        if (!(xs > S(0))) return false;
+        const S gc = sg[r.ownL * KC + col], hc = H ? sh[r.ownL * KC + col] : S(0);
+        stencil_grad<S, D, H>(A, r.stO0, r.stO1, gc, hc, sg, sh, KC, col, v, gg, hg);
+        gf = recon<S, D>(gc, gg, fg.dO, xi, dt);
+        if (H) hf = recon<S, D>(hc, hg, fg.dO, xi, dt);
+        return true;
+    }
+    bool fromOwn, fromNei;
+    if constexpr (sizeof(S) == 8) {
+        fromOwn = xs >= kVSmall;
+        fromNei = xs < -kVSmall;
+    } else {
+        fromOwn = xs > S(0);
+        fromNei = xs < S(0);
+    }
+    if (fromOwn || fromNei) {
+        const int u = fromOwn ? r.ownL : r.neiL;
+        const int e0 = fromOwn ? r.stO0 : r.stN0, e1 = fromOwn ? r.stO1 : r.stN1;
+        const S* d = fromOwn ? fg.dO : fg.dN;
+        const S gc = sg[u * KC + col], hc = H ? sh[u * KC + col] : S(0);
+        stencil_grad<S, D, H>(A, e0, e1, gc, hc, sg, sh, KC, col, v, gg, hg);
+        gf = recon<S, D>(gc, gg, d, xi, dt);
+        if (H) hf = recon<S, D>(hc, hg, d, xi, dt);
+    } else {
+        S gc = sg[r.neiL * KC + col], hc = H ? sh[r.neiL * KC + col] : S(0);
+        stencil_grad<S, D, H>(A, r.stN0, r.stN1, gc, hc, sg, sh, KC, col, v, gg, hg);
+        const S gn = recon<S, D>(gc, gg, fg.dN, xi, dt);
+        const S hn = H ? recon<S, D>(hc, hg, fg.dN, xi, dt) : S(0);
+        gc = sg[r.ownL * KC + col];
+        hc = H ? sh[r.ownL * KC + col] : S(0);
+        stencil_grad<S, D, H>(A, r.stO0, r.stO1, gc, hc, sg, sh, KC, col, v, gg, hg);
+        gf = S(0.5) * (gn + recon<S, D>(gc, gg, fg.dO, xi, dt));
+        if (H) hf = S(0.5) * (hn + recon<S, D>(hc, hg, fg.dO, xi, dt));
+    }
+    return true;
+}
+
+// Per-DV moment terms about Uref added into the lane's slots.
+template <typename S, int D, bool H, int NS, typename T>
+__device__ __forceinline__ void add_moments(T (&m)[NS], S w, S g, S h, const S* c) {
+    using SL = Slots<D, H>;
+    const T wg = (T)(w * g);
+    m[0] += wg;
+    T c2 = T(0);
+#pragma unroll
+    for (int i = 0; i < D; ++i) c2 += (T)c[i] * (T)c[i];
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+        const T t = wg * (T)c[i];
+        m[SL::M1 + i] += t;
+#pragma unroll
+        for (int j = i; j < D; ++j) m[SL::M2 + sym<D>(i, j)] += t * (T)c[j];
+        m[SL::M3 + i] += t * c2;
+    }
+    if (H) {
+        const T wh = (T)(w * h);
+        m[SL::H0] += wh;
+#pragma unroll
+        for (int i = 0; i < D; ++i) m[SL::H1 + i] += wh * (T)c[i];
+    }
+}
+
+// Macros from moments about Uref (FP64): rho, U, T, tau and the raw heat flux.
+template <int D, bool H>
+__device__ __forceinline__ void macros_from_moments(const double* M, const double* Uref, const StepArgs& b,
+                                                    double& rho, double* U, double& T, double& tau, double* qraw) {
+    using SL = Slots<D, H>;
+    rho = M[0];
+    double d[3] = {0, 0, 0};
+    for (int i = 0; i < D; ++i) d[i] = M[SL::M1 + i] / rho;
+    for (int i = 0; i < 3; ++i) U[i] = Uref[i] + d[i];
+    double tr = 0, m1d = 0, dd = 0;
+    for (int i = 0; i < D; ++i) {
+        tr += M[SL::M2 + sym<D>(i, i)];
+        m1d += M[SL::M1 + i] * d[i];
+        dd += d[i] * d[i];
+    }
+    const double h0 = H ? M[SL::H0] : 0.0;
+    const double eint = 0.5 * (tr - m1d + h0);  // sum w |c|^2 g = tr M2 - |M1|^2/M0
+    T = eint / ((b.K + 3) / 2.0 * b.R * rho);
+    tau = tau_ref(T, rho, b.muRef, b.omega, b.Tref, b.R);
+    for (int i = 0; i < 3; ++i) qraw[i] = 0.0;
+    for (int i = 0; i < D; ++i) {
+        double m2d = 0;
+        for (int j = 0; j < D; ++j) m2d += M[SL::M2 + (i <= j ? sym<D>(i, j) : sym<D>(j, i))] * d[j];
+        double s = M[SL::M3 + i] - 2.0 * m2d + M[SL::M1 + i] * dd - d[i] * tr + 2.0 * d[i] * m1d - d[i] * dd * rho;
+        if (H) s += M[SL::H1 + i] - d[i] * h0;
+        qraw[i] = 0.5 * s;
+    }
+}
+
+// FP32 equilibrium coefficient block from FP64 macros (density scaled by gs).
+template <int D>
+__device__ __forceinline__ void write_coef(float* blk, double rho, const double* U, double T, const double* q,
+                                           double tau, const StepArgs& b, double gs) {
+    const double RT = b.R * T;
+    const double pw = D == 2 ? 2.0 * kPi * RT : (D == 3 ? pow(2.0 * kPi * RT, 1.5) : sqrt(2.0 * kPi * RT));
+    const double qs = (1.0 - b.Pr) / (5.0 * rho * RT * RT);
+    float4* o = reinterpret_cast<float4*>(blk);
+    o[0] = make_float4((float)U[0], (float)U[1], (float)U[2], (float)(-1.4426950408889634 / (2.0 * RT)));
+    o[1] = make_float4((float)(1.0 / RT), (float)(q[0] * qs), (float)(q[1] * qs), (float)(q[2] * qs));
+    o[2] = make_float4((float)(rho * gs / pw), (float)RT, (float)tau, 0.0f);
+}
+
+}  // namespace dugks

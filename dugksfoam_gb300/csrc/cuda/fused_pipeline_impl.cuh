@@ -1,0 +1,287 @@
+// FusedPipelineT<S>: owns the tile plan and the double-buffered state of the
+// fused sweeps; included once per storage type (fused_fp32.cu, fused_fp64.cu).
+#pragma once
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../host/solver.h"
+#include "../host/tile_plan.h"
+#include "fused_kernels.cuh"
+#include "kernels.h"
+
+namespace dugks {
+
+template <typename S>
+class FusedPipelineT final : public FusedPipeline {
+public:
+    using KernelFn = void (*)(FusedArgs<S>);
+
+    ~FusedPipelineT() override {
+        for (void* p : allocs_) cudaFree(p);
+    }
+
+    bool init(Solver& solver, const StepArgs& a, std::string& err) {
+        const Mesh& m = solver.mesh();
+        D_ = a.D;
+        H_ = a.hasH != 0;
+        if (D_ != 2 && D_ != 3) { err = "fused pipeline supports 2D and 3D meshes"; return false; }
+        const char* envN = std::getenv("DUGKS_NPL");
+        npl_ = envN ? std::atoi(envN) : 1;
+        if (npl_ != 1 && npl_ != 2) npl_ = 1;
+        const int KC = 32 * npl_;
+        if (a.Vp % KC != 0) { err = "padded DV count is not a multiple of the DV chunk"; return false; }
+        pick();
+        // ---- tile plan, sized to the shared-memory budget
+        int dev = 0;
+        cudaGetDevice(&dev);
+        int maxSmem = 0;
+        cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        const size_t budget = (size_t)maxSmem - 2048;
+        const char* envT = std::getenv("DUGKS_TILE_CELLS");
+        std::vector<int> cand = {1024, 768, 640, 512, 448, 384, 320, 256, 192, 160, 128, 96, 64, 48, 32, 24, 16, 8, 4, 2, 1};
+        if (envT) cand.insert(cand.begin(), std::atoi(envT));
+        bool ok = false;
+        for (int tc : cand) {
+            if (tc < 1) continue;
+            std::string perr;
+            if (!build_tile_plan(m, tc, plan_, perr)) { err = perr; return false; }
+            size_t sf = 0, sc = 0;
+            for (const TileHdr& h : plan_.hdr) {
+                sf = std::max(sf, smemFace(h.nT2, h.nFA));
+                sc = std::max(sc, smemCell(h.nT2, h.nT));
+            }
+            if (sf <= budget && sc <= budget) { smemA_ = sf; smemB_ = sc; ok = true; break; }
+        }
+        if (!ok) { err = "no tile size fits the shared-memory budget"; return false; }
+        cudaFuncSetAttribute(kFace_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemA_);
+        cudaFuncSetAttribute(kCell_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
+
+        // ---- upload plan
+        args_.hdr = upload(plan_.hdr);
+        args_.cells = upload(plan_.cells);
+        args_.faces = upload(plan_.faces);
+        args_.colorOff = upload(plan_.colorOff);
+        args_.colorPerm = upload(plan_.colorPerm);
+        const size_t nRec = plan_.faces.size();
+        if (sizeof(S) == 4) {
+            std::vector<float4> st4(plan_.stEnt.size());
+            for (size_t e = 0; e < st4.size(); ++e) {
+                int o = plan_.stEnt[e];
+                float ow;
+                std::memcpy(&ow, &o, 4);
+                st4[e] = make_float4((float)plan_.stL[3 * e], (float)plan_.stL[3 * e + 1], (float)plan_.stL[3 * e + 2], ow);
+            }
+            args_.st4 = upload(st4);
+            std::vector<float4> fg4(3 * nRec);
+            for (size_t k = 0; k < nRec; ++k) {
+                const TileFace& r = plan_.faces[k];
+                const int f = r.a < m.nI ? r.a : m.wallFace[r.a - m.nI];
+                const int o = m.owner[f];
+                double Sv[3], dO[3], dN[3] = {0, 0, 0};
+                for (int q = 0; q < 3; ++q) {
+                    Sv[q] = m.Sf[3 * (size_t)f + q];
+                    dO[q] = m.Cf[3 * (size_t)f + q] - m.C[3 * (size_t)o + q];
+                    if (r.a < m.nI) dN[q] = m.Cf[3 * (size_t)f + q] - m.C[3 * (size_t)m.neighbour[f] + q];
+                    else dN[q] = m.nHatW[3 * (size_t)r.w + q];  // wall: unit normal
+                }
+                const double iVo = 1.0 / m.V[o], iVn = r.a < m.nI ? 1.0 / m.V[m.neighbour[f]] : 0.0;
+                fg4[3 * k] = make_float4((float)Sv[0], (float)Sv[1], (float)Sv[2], (float)iVo);
+                fg4[3 * k + 1] = make_float4((float)dO[0], (float)dO[1], (float)dO[2], (float)iVn);
+                fg4[3 * k + 2] = make_float4((float)dN[0], (float)dN[1], (float)dN[2], 0.0f);
+            }
+            args_.fg4 = upload(fg4);
+            std::vector<float4> w4(std::max(a.nW, 1), make_float4(0, 0, 0, 0));
+            std::vector<double> Tw(a.nW);
+            if (a.nW) cudaMemcpy(Tw.data(), a.Tw, a.nW * 8, cudaMemcpyDeviceToHost);
+            for (int w = 0; w < a.nW; ++w)
+                w4[w] = make_float4((float)((a.R * Tw[w]) * (a.K + 3 - a.D)), (float)(1.0 / m.dcW[w]), 0.f, 0.f);
+            args_.wall4 = upload(w4);
+            args_.rhoWs = alloc<float>(std::max(a.nW, 1));
+            args_.uref4 = alloc<float4>(a.nA);
+        } else {
+            args_.stEnt = upload(plan_.stEnt);
+            args_.stL = upload(plan_.stL);
+            std::vector<double> fgeo(9 * nRec);
+            for (size_t k = 0; k < nRec; ++k) {
+                const TileFace& r = plan_.faces[k];
+                const int f = r.a < m.nI ? r.a : m.wallFace[r.a - m.nI];
+                const int o = m.owner[f];
+                for (int q = 0; q < 3; ++q) {
+                    fgeo[9 * k + q] = m.Sf[3 * (size_t)f + q];
+                    fgeo[9 * k + 3 + q] = m.Cf[3 * (size_t)f + q] - m.C[3 * (size_t)o + q];
+                    fgeo[9 * k + 6 + q] =
+                        r.a < m.nI ? m.Cf[3 * (size_t)f + q] - m.C[3 * (size_t)m.neighbour[f] + q] : 0.0;
+                }
+            }
+            args_.fgeo = upload(fgeo);
+        }
+        // ---- DV arrays in storage precision
+        std::vector<double> xh(3 * (size_t)a.Vp), wh(a.Vp);
+        cudaMemcpy(xh.data(), a.xi, xh.size() * 8, cudaMemcpyDeviceToHost);
+        cudaMemcpy(wh.data(), a.w, wh.size() * 8, cudaMemcpyDeviceToHost);
+        args_.xi = upload(std::vector<S>(xh.begin(), xh.end()));
+        args_.w = upload(std::vector<S>(wh.begin(), wh.end()));
+        // ---- state
+        const size_t nCV = (size_t)a.nC * a.Vp, nWV = (size_t)std::max(a.nW, 1) * a.Vp;
+        for (int i = 0; i < 2; ++i) {
+            gT_[i] = alloc<S>(nCV);
+            hT_[i] = H_ ? alloc<S>(nCV) : nullptr;
+            Gg_[i] = alloc<S>(nWV);
+            Gh_[i] = H_ ? alloc<S>(nWV) : nullptr;
+            cc_[i] = sizeof(S) == 4 ? alloc<float>((size_t)a.nC * kNCoef) : nullptr;
+        }
+        args_.Mw = mw_ = alloc<S>(nWV);
+        min_ = alloc<double>((size_t)std::max(a.nW, 1) * 32);
+        args_.Min = min_;
+        args_.fc = sizeof(S) == 4 ? alloc<float>((size_t)a.nA * kNCoef) : nullptr;
+        rhoN_ = alloc<double>(a.nC); UN_ = alloc<double>(3 * (size_t)a.nC); TN_ = alloc<double>(a.nC);
+        qN_ = alloc<double>(3 * (size_t)a.nC); tauN_ = alloc<double>(a.nC);
+        if (oom_) { err = "fused pipeline: device allocation failed"; return false; }
+        // density scale of the stored distributions: O(1) values in FP32
+        if (sizeof(S) == 4) {
+            std::vector<double> r0(a.nC), t0(a.nC);
+            cudaMemcpy(r0.data(), a.rho, a.nC * 8, cudaMemcpyDeviceToHost);
+            cudaMemcpy(t0.data(), a.T, a.nC * 8, cudaMemcpyDeviceToHost);
+            double rs = 0, ts = 0;
+            for (int c = 0; c < a.nC; ++c) { rs += r0[c]; ts += t0[c]; }
+            rs /= a.nC; ts /= a.nC;
+            gscale_ = std::pow(2.0 * 3.14159265358979323846 * a.R * ts, 0.5 * D_) / rs;
+        } else {
+            gscale_ = 1.0;
+        }
+        args_.gscale = gscale_;
+        args_.invGscale = 1.0 / gscale_;
+        return true;
+    }
+
+    double gscale() const override { return gscale_; }
+
+    void initState(const StepArgs& a, int sms, cudaStream_t s) override {
+        launch_init_state<S>(a, gT_[0], hT_[0], gscale_, sms, s);
+        if (sizeof(S) == 4) {
+            if (D_ == 2) k_cell_coef<2><<<sms * 4, 256, 0, s>>>(a, cc_[0], gscale_);
+            else k_cell_coef<3><<<sms * 4, 256, 0, s>>>(a, cc_[0], gscale_);
+        }
+        if (a.nW > 0) kTables_<<<a.nW, 128, 0, s>>>(a, mw_, min_);
+        if (sizeof(S) == 4) k_face_uref<<<sms * 2, 256, 0, s>>>(a, args_.uref4);
+    }
+
+    int nKernels() const override { return 2; }
+    const char* kernelName(int k) const override { return k == 0 ? "k_sweep_face" : "k_sweep_cell"; }
+
+    void launch(int k, const StepArgs& a, int sms, cudaStream_t s) override {
+        (void)sms;
+        FusedArgs<S> A = args_;
+        A.b = a;
+        A.dt = (S)a.dt;
+        A.gT = gT_[cur_]; A.hT = hT_[cur_];
+        A.gTn = gT_[1 - cur_]; A.hTn = hT_[1 - cur_];
+        A.Gbg = Gg_[cur_]; A.Gbh = Gh_[cur_];
+        A.Gbgn = Gg_[1 - cur_]; A.Gbhn = Gh_[1 - cur_];
+        A.cc = cc_[cur_]; A.ccn = cc_[1 - cur_];
+        A.rhoN = rhoN_; A.UN = UN_; A.TN = TN_; A.qN = qN_; A.tauN = tauN_;
+        if (k == 0) kFace_<<<plan_.nTiles, kNW * 32, smemA_, s>>>(A);
+        else kCell_<<<plan_.nTiles, kNW * 32, smemB_, s>>>(A);
+    }
+
+    void endStep(StepArgs& base) override {
+        cur_ = 1 - cur_;
+        std::swap(base.rho, rhoN_);
+        std::swap(base.U, UN_);
+        std::swap(base.T, TN_);
+        std::swap(base.q, qN_);
+        std::swap(base.tau, tauN_);
+    }
+
+    void refreshDerived(const StepArgs& a, int sms, cudaStream_t s) override {
+        if (sizeof(S) == 4) {
+            if (D_ == 2) k_cell_coef<2><<<sms * 4, 256, 0, s>>>(a, cc_[cur_], gscale_);
+            else k_cell_coef<3><<<sms * 4, 256, 0, s>>>(a, cc_[cur_], gscale_);
+            k_face_uref<<<sms * 2, 256, 0, s>>>(a, args_.uref4);
+        }
+    }
+
+    void exportDist(const StepArgs& a, int which, double* dst, int sms, cudaStream_t s) override {
+        launch_export_dist<S>(a, which ? hT_[cur_] : gT_[cur_], dst, 1.0 / gscale_, sms, s);
+    }
+    void importDist(const StepArgs& a, int which, const double* src, int sms, cudaStream_t s) override {
+        launch_import_dist<S>(a, src, which ? hT_[cur_] : gT_[cur_], gscale_, sms, s);
+    }
+    void* distPtr(int which) override { return which ? (void*)hT_[cur_] : (void*)gT_[cur_]; }
+    void* gradBPtr(int which) override { return which ? (void*)Gh_[cur_] : (void*)Gg_[cur_]; }
+    size_t bytes() const override { return bytes_; }
+    std::string describe() const override {
+        char buf[256];
+        snprintf(buf, sizeof(buf), "tiles=%d tileCells=%d maxT2=%d maxFB=%d npl=%d smemA=%zu smemB=%zu", plan_.nTiles,
+                 plan_.tileCells, plan_.maxT2, plan_.maxFB, npl_, smemA_, smemB_);
+        return buf;
+    }
+
+private:
+    static constexpr int kNW = 16;
+
+    template <typename T>
+    T* alloc(size_t n) {
+        void* p = nullptr;
+        const size_t by = std::max<size_t>(n, 1) * sizeof(T);
+        if (cudaMalloc(&p, by) != cudaSuccess) { cudaGetLastError(); oom_ = true; return nullptr; }
+        cudaMemset(p, 0, by);
+        allocs_.push_back(p);
+        bytes_ += by;
+        return static_cast<T*>(p);
+    }
+    template <typename T>
+    T* upload(const std::vector<T>& v) {
+        T* p = alloc<T>(v.size());
+        if (p && !v.empty()) cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+        return p;
+    }
+
+    template <int D, bool H, int NPL>
+    void set() {
+        kFace_ = k_sweep_face<S, D, H, NPL, kNW>;
+        kCell_ = k_sweep_cell<S, D, H, NPL, kNW>;
+        kTables_ = k_wall_tables<S, D, H>;
+        smemFaceFn_ = &SmemLayout<S, D, H, NPL>::face;
+        smemCellFn_ = &SmemLayout<S, D, H, NPL>::cell;
+    }
+    void pick() {
+        if (D_ == 2) {
+            if (H_) { npl_ == 2 ? set<2, true, 2>() : set<2, true, 1>(); }
+            else { npl_ == 2 ? set<2, false, 2>() : set<2, false, 1>(); }
+        } else {
+            if (H_) { npl_ == 2 ? set<3, true, 2>() : set<3, true, 1>(); }
+            else { npl_ == 2 ? set<3, false, 2>() : set<3, false, 1>(); }
+        }
+    }
+    size_t smemFace(int nT2, int nFA) const { return smemFaceFn_(nT2, nFA); }
+    size_t smemCell(int nT2, int nT) const { return smemCellFn_(nT2, nT); }
+
+    int D_ = 2, npl_ = 1;
+    bool H_ = true;
+    TilePlan plan_;
+    FusedArgs<S> args_{};
+    KernelFn kFace_ = nullptr, kCell_ = nullptr;
+    void (*kTables_)(StepArgs, S*, double*) = nullptr;
+    size_t (*smemFaceFn_)(int, int) = nullptr;
+    size_t (*smemCellFn_)(int, int) = nullptr;
+    size_t smemA_ = 0, smemB_ = 0;
+    S* gT_[2] = {nullptr, nullptr};
+    S* hT_[2] = {nullptr, nullptr};
+    S* Gg_[2] = {nullptr, nullptr};
+    S* Gh_[2] = {nullptr, nullptr};
+    float* cc_[2] = {nullptr, nullptr};
+    S* mw_ = nullptr;
+    double* min_ = nullptr;
+    double *rhoN_ = nullptr, *UN_ = nullptr, *TN_ = nullptr, *qN_ = nullptr, *tauN_ = nullptr;
+    double gscale_ = 1.0;
+    int cur_ = 0;
+    std::vector<void*> allocs_;
+    size_t bytes_ = 0;
+    bool oom_ = false;
+};
+
+}  // namespace dugks

@@ -91,7 +91,8 @@ int Solver::init(const dugks_case_desc& d) {
     // ---- DV set, fvDVM::initialiseDV (fvDVM.C:140-221)
     const int M = d.n_xi_per_dim;
     nV_ = D == 3 ? M * M * M : (D == 2 ? M * M : M);
-    Vp_ = (nV_ + 7) / 8 * 8;
+    const int granule = pipeline_ == DUGKS_PIPE_FUSED ? fused_dv_granule() : 8;
+    Vp_ = (nV_ + granule - 1) / granule * granule;
     const int Vp = Vp_;
     std::vector<double> xi(3 * (size_t)Vp, 0.0), w(Vp, 0.0);
     {
@@ -290,6 +291,7 @@ int Solver::runStep(bool timed, std::vector<double>* ms, std::vector<cudaEvent_t
             fused_->launch(k, a, sms_, stream_);
         if (timed) cudaEventRecord((*ev)[2 * k + 1], stream_);
     }
+    if (pipeline_ != DUGKS_PIPE_REFERENCE) fused_->endStep(base_);
     (void)ms;
     return checkCuda(cudaGetLastError(), "step launch");
 }
@@ -506,6 +508,8 @@ int Solver::checkpointLoad(const void* buf, size_t n) {
     put(base_.UF, (size_t)base_.nA * 3 * 8);
     dt_ = hd.dt;
     steps_ = hd.steps;
+    if (ce == cudaSuccess && fused_) fused_->refreshDerived(argsNow(), sms_, stream_);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream_);
     return checkCuda(ce, "checkpoint load");
 }
 
@@ -537,7 +541,8 @@ int Solver::profile(int nsteps, std::vector<std::string>& names, std::vector<dou
 void Solver::info(dugks_info& o) const {
     o.n_cells = mesh_.nC; o.n_faces = mesh_.nF; o.n_internal_faces = mesh_.nI; o.n_wall_faces = mesh_.nW;
     o.n_dv = nV_; o.n_dv_padded = Vp_; o.n_solution_d = mesh_.D; o.has_h = hasH_;
-    o.precision = precision_; o.pipeline = pipeline_; o.dt = dt_; o.step_count = steps_; o.device_bytes = bytes_;
+    o.precision = precision_; o.pipeline = pipeline_; o.dt = dt_; o.step_count = steps_;
+    o.device_bytes = bytes_ + (fused_ ? fused_->bytes() : 0);
 }
 
 template double* Solver::dalloc<double>(size_t);

@@ -1,8 +1,13 @@
 """GPU parity: the CUDA engine through the C ABI vs the FP64 CPU oracle.
 
-Tolerances (field-normalised, vector fields by magnitude of the difference):
-  plain FP64 path                 <= 1e-12 (L-inf and L2) on rho, U, T, q
-  FP32 bulk / FP64 moments path   <= 1e-5
+Tolerances (field-normalised; vector fields by the magnitude of the difference):
+  plain FP64 path at the stated step count (61x61 cavity, 2000 steps,
+      golden fixture)                  <= 1e-12 (L-inf and L2) on rho, U, T, q
+  plain FP64 path, short runs on tiny meshes: <= max(1e-12, 4 x floor), where
+      floor is how far an independent FP64 restatement (numpy) sits from the
+      oracle on the same run -- early in a transient U and q are near zero in
+      most cells and two correct FP64 codes already differ by ~1e-11 in L2
+  FP32 bulk / FP64 moments path       <= 1e-5
 """
 import numpy as np
 import pytest
@@ -21,17 +26,36 @@ def _small_cases():
 
     return {
         "quad12": (cases.cavity2d(n=12, nxi=8), 20),
-        "tri": (cases.make_case(cases.delaunay_mesh(300, 12, seed=3), *cases.gas_from_kn(0.05), 8,
-                                4.0 * np.sqrt(2 * 208.0 * 273.0)), 20),
+        "tri": (dict(cases.make_case(cases.delaunay_mesh(300, 12, seed=3), *cases.gas_from_kn(0.05), 8,
+                                     4.0 * np.sqrt(2 * 208.0 * 273.0)), unstructured=True), 20),
         "hex5": (cases.cavity3d(n=5, nxi=6), 10),
     }
+
+
+_FLOOR = {}
+
+
+def _noise_floor(name):
+    """Distance between two independent FP64 restatements (C oracle vs numpy)."""
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import NumpyOracle, Oracle
+
+    if name not in _FLOOR:
+        case, steps = _small_cases()[name]
+        dt = cases.case_dt(case)
+        a, b = Oracle(case), NumpyOracle(case)
+        a.step(dt, steps)
+        b.step(dt, steps)
+        ca, cb = a.cell(), b.cell()
+        _FLOOR[name] = {k: rel_err(cb[k], ca[k]) for k in FIELDS}
+    return _FLOOR[name]
 
 
 def _run_pair(case, steps, precision, pipeline=0):
     from dugksfoam_gb300 import cases, solver
     from oracle.oracle import Oracle
 
-    dt = cases.stable_dt(case)
+    dt = cases.case_dt(case)
     ref = Oracle(case)
     ref.step(dt, steps)
     s = solver.FvDVM(case, precision=precision, pipeline=pipeline)
@@ -47,9 +71,11 @@ def test_fp64_reference_pipeline_matches_oracle(built_lib, oracle_lib, name):
     case, steps = _small_cases()[name]
     s, ref = _run_pair(case, steps, solver.FP64, solver.PIPE_REFERENCE)
     got, want = s.macros(), ref.cell()
+    floor = _noise_floor(name)
     for k in FIELDS:
         einf, el2 = rel_err(got[k], want[k])
-        assert einf <= TOL64 and el2 <= TOL64, (name, k, einf, el2)
+        tinf, tl2 = max(TOL64, 4 * floor[k][0]), max(TOL64, 4 * floor[k][1])
+        assert einf <= tinf and el2 <= tl2, (name, k, einf, el2, floor[k])
     # face macros and wall state
     fm = s.face_macros()
     of = ref.face()
@@ -162,4 +188,57 @@ def test_nan_state_is_reported(built_lib):
     with pytest.raises(solver.DugksError) as ei:
         s.synchronize()
     assert ei.value.code == 5
+    s.close()
+
+
+@pytest.mark.parametrize("name", ["quad12", "tri", "hex5"])
+def test_fused_fp64_matches_oracle(built_lib, oracle_lib, name):
+    from dugksfoam_gb300 import solver
+
+    case, steps = _small_cases()[name]
+    s, ref = _run_pair(case, steps, solver.FP64, solver.PIPE_FUSED)
+    got, want = s.macros(), ref.cell()
+    floor = _noise_floor(name)
+    for k in FIELDS:
+        einf, el2 = rel_err(got[k], want[k])
+        # one-pass central moments and colour-ordered flux sums: rounding-level
+        tinf, tl2 = max(1e-11, 10 * floor[k][0]), max(1e-11, 10 * floor[k][1])
+        assert einf <= tinf and el2 <= tl2, (name, k, einf, el2, floor[k])
+    s.close()
+
+
+@pytest.mark.parametrize("name", ["quad12", "tri", "hex5"])
+def test_fused_fp32_matches_oracle(built_lib, oracle_lib, name):
+    from dugksfoam_gb300 import solver
+
+    case, steps = _small_cases()[name]
+    s, ref = _run_pair(case, steps, solver.FP32_FP64MOM, solver.PIPE_FUSED)
+    got, want = s.macros(), ref.cell()
+    for k in FIELDS:
+        einf, el2 = rel_err(got[k], want[k])
+        assert einf <= TOL32 and el2 <= TOL32, (name, k, einf, el2)
+    s.close()
+
+
+def _golden(name):
+    import os
+
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", name))
+
+
+@pytest.mark.parametrize("precision,pipeline,tol", [(0, 1, TOL64), (0, 2, 1e-11), (1, 2, TOL32)])
+def test_cavity61_2000_steps_against_golden(built_lib, precision, pipeline, tol):
+    """The CPU-runnable workload at its stated step count: 61x61 quads,
+    28x28 DVs, 2000 steps, against the committed FP64 oracle fields."""
+    from dugksfoam_gb300 import cases, solver
+
+    ref = _golden("cavity61_2000.npz")
+    case = cases.cavity2d(n=61, nxi=28)
+    s = solver.FvDVM(case, precision=precision, pipeline=pipeline)
+    s.set_dt(float(ref["dt"]))
+    s.evolution(int(ref["steps"]))
+    got = s.macros()
+    for k in FIELDS:
+        einf, el2 = rel_err(got[k], ref[k])
+        assert einf <= tol and el2 <= tol, (k, einf, el2)
     s.close()
