@@ -33,8 +33,10 @@ public:
     virtual std::string describe() const = 0;
 };
 
+// DVs per lane of the fused kernels for a precision (FP32: DUGKS_NPL, default 4).
+int fused_npl(int precision);
 // DV chunk granularity the fused kernels need (the padded DV count must be a multiple).
-int fused_dv_granule();
+int fused_dv_granule(int precision);
 
 std::unique_ptr<FusedPipeline> make_fused_pipeline(Solver& s, const StepArgs& a, int precision, std::string& err);
 std::unique_ptr<FusedPipeline> make_fused_fp32(Solver& s, const StepArgs& a, std::string& err);

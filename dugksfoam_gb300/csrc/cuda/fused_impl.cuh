@@ -81,6 +81,11 @@ struct FusedArgs {
     const float* cc;            // [nC][kNCoef] current cell equilibrium block
     float* ccn;                 // next
     float* fc;                  // [nA][kNCoef] face equilibrium (written by sweep A)
+    // FP32 deviation storage: G = gscale g - Mref, H = gscale h - Mref hrefFac
+    const float* mref;          // [Vp] exp(-|xi|^2/(2 R T0))
+    float hrefFac;              // R T0 (K+3-D)
+    const double* refMom;       // [NS] raw moments of Mref (scaled)
+    const double* wallRefOut;   // [nW][NS] Mref moments over outgoing DVs about U_w (+ flux)
     // macros of the next step
     double *rhoN, *UN, *TN, *qN, *tauN;
     double gscale, invGscale;

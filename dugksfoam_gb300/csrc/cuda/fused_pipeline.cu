@@ -6,11 +6,14 @@
 
 namespace dugks {
 
-int fused_dv_granule() {
+int fused_npl(int precision) {
+    if (precision == DUGKS_FP64) return 1;
     const char* e = std::getenv("DUGKS_NPL");
-    int npl = e ? std::atoi(e) : 1;
-    return 32 * (npl == 2 ? 2 : 1);
+    const int npl = e ? std::atoi(e) : 4;
+    return (npl == 1 || npl == 2 || npl == 4) ? npl : 4;
 }
+
+int fused_dv_granule(int precision) { return 32 * fused_npl(precision); }
 
 std::unique_ptr<FusedPipeline> make_fused_pipeline(Solver& s, const StepArgs& a, int precision, std::string& err) {
     return precision == DUGKS_FP64 ? make_fused_fp64(s, a, err) : make_fused_fp32(s, a, err);

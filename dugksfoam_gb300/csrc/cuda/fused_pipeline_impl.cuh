@@ -9,6 +9,7 @@
 
 #include "../host/solver.h"
 #include "../host/tile_plan.h"
+#include "fused32.cuh"
 #include "fused_kernels.cuh"
 #include "kernels.h"
 
@@ -28,9 +29,7 @@ public:
         D_ = a.D;
         H_ = a.hasH != 0;
         if (D_ != 2 && D_ != 3) { err = "fused pipeline supports 2D and 3D meshes"; return false; }
-        const char* envN = std::getenv("DUGKS_NPL");
-        npl_ = envN ? std::atoi(envN) : 1;
-        if (npl_ != 1 && npl_ != 2) npl_ = 1;
+        npl_ = fused_npl(sizeof(S) == 4 ? DUGKS_FP32_FP64MOM : DUGKS_FP64);
         const int KC = 32 * npl_;
         if (a.Vp % KC != 0) { err = "padded DV count is not a multiple of the DV chunk"; return false; }
         pick();
@@ -137,6 +136,14 @@ public:
         min_ = alloc<double>((size_t)std::max(a.nW, 1) * 32);
         args_.Min = min_;
         args_.fc = sizeof(S) == 4 ? alloc<float>((size_t)a.nA * kNCoef) : nullptr;
+        if (sizeof(S) == 4) {
+            mref_ = alloc<float>(a.Vp);
+            refMom_ = alloc<double>(32);
+            wallRefOut_ = alloc<double>((size_t)std::max(a.nW, 1) * 32);
+            args_.mref = mref_;
+            args_.refMom = refMom_;
+            args_.wallRefOut = wallRefOut_;
+        }
         rhoN_ = alloc<double>(a.nC); UN_ = alloc<double>(3 * (size_t)a.nC); TN_ = alloc<double>(a.nC);
         qN_ = alloc<double>(3 * (size_t)a.nC); tauN_ = alloc<double>(a.nC);
         if (oom_) { err = "fused pipeline: device allocation failed"; return false; }
@@ -149,6 +156,9 @@ public:
             for (int c = 0; c < a.nC; ++c) { rs += r0[c]; ts += t0[c]; }
             rs /= a.nC; ts /= a.nC;
             gscale_ = std::pow(2.0 * 3.14159265358979323846 * a.R * ts, 0.5 * D_) / rs;
+            T0_ = ts;
+            hrefFac_ = a.R * ts * (a.K + 3 - a.D);
+            args_.hrefFac = (float)hrefFac_;
         } else {
             gscale_ = 1.0;
         }
@@ -160,7 +170,12 @@ public:
     double gscale() const override { return gscale_; }
 
     void initState(const StepArgs& a, int sms, cudaStream_t s) override {
-        launch_init_state<S>(a, gT_[0], hT_[0], gscale_, sms, s);
+        if constexpr (sizeof(S) == 4) {
+            kRef_<<<1 + a.nW, 128, 0, s>>>(a, T0_, hrefFac_, mref_, refMom_, wallRefOut_);
+            k_init_dev32<<<sms * 8, 256, 0, s>>>(a, mref_, gscale_, hrefFac_, gT_[0], hT_[0]);
+        } else {
+            launch_init_state<S>(a, gT_[0], hT_[0], gscale_, sms, s);
+        }
         if (sizeof(S) == 4) {
             if (D_ == 2) k_cell_coef<2><<<sms * 4, 256, 0, s>>>(a, cc_[0], gscale_);
             else k_cell_coef<3><<<sms * 4, 256, 0, s>>>(a, cc_[0], gscale_);
@@ -205,10 +220,18 @@ public:
     }
 
     void exportDist(const StepArgs& a, int which, double* dst, int sms, cudaStream_t s) override {
-        launch_export_dist<S>(a, which ? hT_[cur_] : gT_[cur_], dst, 1.0 / gscale_, sms, s);
+        if constexpr (sizeof(S) == 4)
+            k_export_dev32<<<sms * 8, 256, 0, s>>>(a, which ? hT_[cur_] : gT_[cur_], mref_, which ? hrefFac_ : 1.0,
+                                                   1.0 / gscale_, dst);
+        else
+            launch_export_dist<S>(a, which ? hT_[cur_] : gT_[cur_], dst, 1.0 / gscale_, sms, s);
     }
     void importDist(const StepArgs& a, int which, const double* src, int sms, cudaStream_t s) override {
-        launch_import_dist<S>(a, src, which ? hT_[cur_] : gT_[cur_], gscale_, sms, s);
+        if constexpr (sizeof(S) == 4)
+            k_import_dev32<<<sms * 8, 256, 0, s>>>(a, src, mref_, which ? hrefFac_ : 1.0, gscale_,
+                                                   which ? hT_[cur_] : gT_[cur_]);
+        else
+            launch_import_dist<S>(a, src, which ? hT_[cur_] : gT_[cur_], gscale_, sms, s);
     }
     void* distPtr(int which) override { return which ? (void*)hT_[cur_] : (void*)gT_[cur_]; }
     void* gradBPtr(int which) override { return which ? (void*)Gh_[cur_] : (void*)Gg_[cur_]; }
@@ -242,20 +265,31 @@ private:
 
     template <int D, bool H, int NPL>
     void set() {
-        kFace_ = k_sweep_face<S, D, H, NPL, kNW>;
-        kCell_ = k_sweep_cell<S, D, H, NPL, kNW>;
+        if constexpr (sizeof(S) == 4) {
+            kFace_ = k_sweep_face32<D, H, NPL, kNW>;
+            kCell_ = k_sweep_cell32<D, H, NPL, kNW>;
+            kRef_ = k_ref_tables<D, H>;
+        } else {
+            kFace_ = k_sweep_face<S, D, H, NPL, kNW>;
+            kCell_ = k_sweep_cell<S, D, H, NPL, kNW>;
+        }
         kTables_ = k_wall_tables<S, D, H>;
         smemFaceFn_ = &SmemLayout<S, D, H, NPL>::face;
         smemCellFn_ = &SmemLayout<S, D, H, NPL>::cell;
     }
-    void pick() {
-        if (D_ == 2) {
-            if (H_) { npl_ == 2 ? set<2, true, 2>() : set<2, true, 1>(); }
-            else { npl_ == 2 ? set<2, false, 2>() : set<2, false, 1>(); }
+    template <int D, bool H>
+    void setD() {
+        if constexpr (sizeof(S) == 4) {
+            if (npl_ == 4) set<D, H, 4>();
+            else if (npl_ == 2) set<D, H, 2>();
+            else set<D, H, 1>();
         } else {
-            if (H_) { npl_ == 2 ? set<3, true, 2>() : set<3, true, 1>(); }
-            else { npl_ == 2 ? set<3, false, 2>() : set<3, false, 1>(); }
+            set<D, H, 1>();
         }
+    }
+    void pick() {
+        if (D_ == 2) { H_ ? setD<2, true>() : setD<2, false>(); }
+        else { H_ ? setD<3, true>() : setD<3, false>(); }
     }
     size_t smemFace(int nT2, int nFA) const { return smemFaceFn_(nT2, nFA); }
     size_t smemCell(int nT2, int nT) const { return smemCellFn_(nT2, nT); }
@@ -266,6 +300,11 @@ private:
     FusedArgs<S> args_{};
     KernelFn kFace_ = nullptr, kCell_ = nullptr;
     void (*kTables_)(StepArgs, S*, double*) = nullptr;
+    void (*kRef_)(StepArgs, double, double, float*, double*, double*) = nullptr;
+    float* mref_ = nullptr;
+    double* refMom_ = nullptr;
+    double* wallRefOut_ = nullptr;
+    double T0_ = 273.0, hrefFac_ = 0.0;
     size_t (*smemFaceFn_)(int, int) = nullptr;
     size_t (*smemCellFn_)(int, int) = nullptr;
     size_t smemA_ = 0, smemB_ = 0;

@@ -3,6 +3,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "../cuda/fused.h"
@@ -91,7 +93,7 @@ int Solver::init(const dugks_case_desc& d) {
     // ---- DV set, fvDVM::initialiseDV (fvDVM.C:140-221)
     const int M = d.n_xi_per_dim;
     nV_ = D == 3 ? M * M * M : (D == 2 ? M * M : M);
-    const int granule = pipeline_ == DUGKS_PIPE_FUSED ? fused_dv_granule() : 8;
+    const int granule = pipeline_ == DUGKS_PIPE_FUSED ? fused_dv_granule(precision_) : 8;
     Vp_ = (nV_ + granule - 1) / granule * granule;
     const int Vp = Vp_;
     std::vector<double> xi(3 * (size_t)Vp, 0.0), w(Vp, 0.0);
@@ -256,6 +258,7 @@ int Solver::init(const dugks_case_desc& d) {
         fused_ = make_fused_pipeline(*this, a, precision_, ferr);
         if (!fused_) return fail(ferr.find("alloc") != std::string::npos ? DUGKS_ERR_OOM : DUGKS_ERR_UNSUPPORTED, ferr);
         gscale_ = fused_->gscale();
+        if (std::getenv("DUGKS_VERBOSE")) std::fprintf(stderr, "dugks fused pipeline: %s\n", fused_->describe().c_str());
         fused_->initState(a, sms_, stream_);
     }
     if (int e = checkCuda(cudaGetLastError(), "init kernels")) return e;
