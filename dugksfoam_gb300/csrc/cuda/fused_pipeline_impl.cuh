@@ -40,21 +40,16 @@ public:
         cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         const size_t budget = (size_t)maxSmem - 2048;
         const char* envT = std::getenv("DUGKS_TILE_CELLS");
-        std::vector<int> cand = {1024, 768, 640, 512, 448, 384, 320, 256, 192, 160, 128, 96, 64, 48, 32, 24, 16, 8, 4, 2, 1};
-        if (envT) cand.insert(cand.begin(), std::atoi(envT));
-        bool ok = false;
-        for (int tc : cand) {
-            if (tc < 1) continue;
-            std::string perr;
-            if (!build_tile_plan(m, tc, plan_, perr)) { err = perr; return false; }
-            size_t sf = 0, sc = 0;
-            for (const TileHdr& h : plan_.hdr) {
-                sf = std::max(sf, smemFace(h.nT2, h.nFA));
-                sc = std::max(sc, smemCell(h.nT2, h.nT));
-            }
-            if (sf <= budget && sc <= budget) { smemA_ = sf; smemB_ = sc; ok = true; break; }
+        const int maxCells = envT ? std::max(1, std::atoi(envT)) : 4096;
+        const SmemFn fn = [this](int nT, int nT2, int nFA) {
+            return std::max(smemFace(nT2, nFA), smemCell(nT2, nT));
+        };
+        if (!build_tile_plan(m, maxCells, fn, budget, plan_, err)) return false;
+        smemA_ = smemB_ = 0;
+        for (const TileHdr& h : plan_.hdr) {
+            smemA_ = std::max(smemA_, smemFace(h.nT2, h.nFA));
+            smemB_ = std::max(smemB_, smemCell(h.nT2, h.nT));
         }
-        if (!ok) { err = "no tile size fits the shared-memory budget"; return false; }
         cudaFuncSetAttribute(kFace_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemA_);
         cudaFuncSetAttribute(kCell_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
 
@@ -238,8 +233,9 @@ public:
     size_t bytes() const override { return bytes_; }
     std::string describe() const override {
         char buf[256];
-        snprintf(buf, sizeof(buf), "tiles=%d tileCells=%d maxT2=%d maxFB=%d npl=%d smemA=%zu smemB=%zu", plan_.nTiles,
-                 plan_.tileCells, plan_.maxT2, plan_.maxFB, npl_, smemA_, smemB_);
+        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d smemA=%zu smemB=%zu",
+                 plan_.nTiles, plan_.maxT, (double)plan_.sumT / std::max(1, plan_.nTiles),
+                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, smemA_, smemB_);
         return buf;
     }
 

@@ -1,4 +1,12 @@
 // Tile plan construction (see tile_plan.h).
+//
+// Tiles come from recursive coordinate bisection of the cell centres: a range
+// of c cells is split along its longest extent into parts holding whole
+// multiples of the tile size N, so the leaves are box-shaped blobs of N cells
+// and the depth-first leaf order keeps consecutive tiles spatially adjacent
+// (their halo rows are re-read from L2 while both are in flight).  N is the
+// largest size (binary search) for which every tile's shared-memory footprint
+// -- rows of T u H1 u H2 plus face/cell accumulators -- fits the budget.
 #include "tile_plan.h"
 
 #include <algorithm>
@@ -8,73 +16,120 @@
 namespace dugks {
 namespace {
 
-uint64_t spread3(uint64_t v) {  // 21 bits -> every third bit
-    v &= 0x1fffff;
-    v = (v | v << 32) & 0x1f00000000ffffULL;
-    v = (v | v << 16) & 0x1f0000ff0000ffULL;
-    v = (v | v << 8) & 0x100f00f00f00f00fULL;
-    v = (v | v << 4) & 0x10c30c30c30c30c3ULL;
-    v = (v | v << 2) & 0x1249249249249249ULL;
-    return v;
+inline int other(const Mesh& m, int j) {  // neighbour across cell-face entry j (internal faces)
+    const int f = m.cellFace[j];
+    return m.cellSide[j] == 0 ? m.neighbour[f] : m.owner[f];
 }
 
-}  // namespace
-
-bool build_tile_plan(const Mesh& m, int tileCells, TilePlan& p, std::string& err) {
-    const int nC = m.nC, nI = m.nI;
-    if (tileCells < 1) { err = "tile size must be positive"; return false; }
-    p = TilePlan();
-    p.tileCells = tileCells;
-
-    // ---- Morton order of cell centres
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int c = 0; c < nC; ++c)
-        for (int k = 0; k < 3; ++k) {
-            lo[k] = std::min(lo[k], m.C[3 * (size_t)c + k]);
-            hi[k] = std::max(hi[k], m.C[3 * (size_t)c + k]);
-        }
-    std::vector<std::pair<uint64_t, int>> key(nC);
-    for (int c = 0; c < nC; ++c) {
-        uint64_t code = 0;
-        for (int k = 0; k < 3; ++k) {
-            double span = hi[k] - lo[k];
-            double t = span > 0 ? (m.C[3 * (size_t)c + k] - lo[k]) / span : 0.0;
-            uint64_t q = (uint64_t)std::min(2097151.0, std::max(0.0, t * 2097151.0));
-            code |= spread3(q) << k;
-        }
-        key[c] = {code, c};
-    }
-    std::sort(key.begin(), key.end());
-
-    // cell -> (neighbour cell) adjacency through internal faces, per cell in face order
-    std::vector<int> mark(nC, -1), loc(nC, -1);
-    const int nTiles = (nC + tileCells - 1) / tileCells;
-    p.nTiles = nTiles;
-    p.hdr.resize(nTiles);
-    for (int t = 0; t < nTiles; ++t) {
-        TileHdr h{};
-        const int b = t * tileCells, e = std::min(nC, b + tileCells);
-        std::vector<int> lc;  // local cells
-        for (int i = b; i < e; ++i) lc.push_back(key[i].second);
-        for (int c : lc) mark[c] = t * 3;          // T
-        h.nT = (int)lc.size();
+// Sets of a candidate tile: lc = T, then H1, then H2 (stamp-marked).
+struct Sets {
+    std::vector<int> mark;  // stamp*3 + {0,1,2}
+    int stamp = 0;
+    int nT = 0, nT1 = 0, nT2 = 0, nFA = 0;
+    std::vector<int> lc;
+    explicit Sets(int nC) : mark(nC, -1) {}
+    bool in(int c) const { return mark[c] >= stamp * 3 && mark[c] <= stamp * 3 + 2; }
+    bool inT(int c) const { return mark[c] == stamp * 3; }
+    void build(const Mesh& m, const int* cells, int n) {
+        ++stamp;
+        lc.assign(cells, cells + n);
+        for (int i = 0; i < n; ++i) mark[cells[i]] = stamp * 3;
+        nT = n;
         auto ring = [&](int from, int to, int tag) {
             for (int i = from; i < to; ++i) {
-                int c = lc[i];
+                const int c = lc[i];
                 for (int j = m.cellOff[c]; j < m.cellOff[c + 1]; ++j) {
-                    int f = m.cellFace[j];
-                    if (f >= nI) continue;
-                    int o = m.cellSide[j] == 0 ? m.neighbour[f] : m.owner[f];
-                    if (mark[o] >= t * 3 && mark[o] <= t * 3 + 2) continue;
-                    mark[o] = tag;
+                    if (m.cellFace[j] >= m.nI) continue;
+                    const int o = other(m, j);
+                    if (in(o)) continue;
+                    mark[o] = stamp * 3 + tag;
                     lc.push_back(o);
                 }
             }
         };
-        ring(0, h.nT, t * 3 + 1);
-        h.nT1 = (int)lc.size();
-        ring(h.nT, h.nT1, t * 3 + 2);
-        h.nT2 = (int)lc.size();
+        ring(0, nT, 1);
+        nT1 = (int)lc.size();
+        ring(nT, nT1, 2);
+        nT2 = (int)lc.size();
+        nFA = 0;
+        for (int i = 0; i < nT; ++i) {
+            const int c = lc[i];
+            for (int j = m.cellOff[c]; j < m.cellOff[c + 1]; ++j)
+                if (m.cellFace[j] >= m.nI || m.cellSide[j] == 0) ++nFA;
+        }
+    }
+};
+
+}  // namespace
+
+namespace {
+
+void rcb(const Mesh& m, std::vector<int>& cells, int b, int e, int N, std::vector<std::pair<int, int>>& parts) {
+    const int c = e - b;
+    if (c <= N) {
+        parts.push_back({b, e});
+        return;
+    }
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int i = b; i < e; ++i)
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = std::min(lo[k], m.C[3 * (size_t)cells[i] + k]);
+            hi[k] = std::max(hi[k], m.C[3 * (size_t)cells[i] + k]);
+        }
+    int ax = 0;
+    for (int k = 1; k < 3; ++k)
+        if (hi[k] - lo[k] > hi[ax] - lo[ax]) ax = k;
+    const int np = (c + N - 1) / N;
+    const int left = (int)((long long)c * (np / 2) / np);
+    std::nth_element(cells.begin() + b, cells.begin() + b + left, cells.begin() + e, [&](int x, int y) {
+        return m.C[3 * (size_t)x + ax] < m.C[3 * (size_t)y + ax];
+    });
+    rcb(m, cells, b, b + left, N, parts);
+    rcb(m, cells, b + left, e, N, parts);
+}
+
+}  // namespace
+
+bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t budget, TilePlan& p,
+                     std::string& err) {
+    const int nC = m.nC, nI = m.nI;
+    if (maxTileCells < 1) { err = "tile size must be positive"; return false; }
+    p = TilePlan();
+    Sets S(nC);
+    std::vector<int> cells(nC);
+    std::vector<std::pair<int, int>> parts;
+    auto partition = [&](int N) {
+        for (int c = 0; c < nC; ++c) cells[c] = c;
+        parts.clear();
+        rcb(m, cells, 0, nC, N, parts);
+    };
+    auto fits = [&](int N) {
+        partition(N);
+        for (auto& pr : parts) {
+            S.build(m, cells.data() + pr.first, pr.second - pr.first);
+            if (smem(S.nT, S.nT2, S.nFA) > budget) return false;
+        }
+        return true;
+    };
+    int lo = 1, hi = std::min(maxTileCells, nC);
+    if (!fits(lo)) { err = "tile plan: a single cell and its halo exceed the shared-memory budget"; return false; }
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) / 2;
+        if (fits(mid)) lo = mid;
+        else hi = mid - 1;
+    }
+    partition(lo);
+    p.tileCells = lo;
+    std::vector<int> loc(nC, -1);
+    int t = 0;
+    for (auto& pr : parts) {
+        S.build(m, cells.data() + pr.first, pr.second - pr.first);
+        // ---- emit the tile
+        TileHdr h{};
+        const std::vector<int>& lc = S.lc;
+        h.nT = S.nT;
+        h.nT1 = S.nT1;
+        h.nT2 = S.nT2;
         h.cellStart = (int)p.cells.size();
         for (int i = 0; i < h.nT2; ++i) {
             loc[lc[i]] = i;
@@ -83,22 +138,18 @@ bool build_tile_plan(const Mesh& m, int tileCells, TilePlan& p, std::string& err
         // stencils of T u H1, entries in global face order
         h.stStart = (int)p.stOff.size();
         for (int i = 0; i < h.nT1; ++i) {
-            int c = lc[i];
+            const int c = lc[i];
             p.stOff.push_back((int)p.stEnt.size());
             for (int j = m.cellOff[c]; j < m.cellOff[c + 1]; ++j) {
-                int f = m.cellFace[j];
+                const int f = m.cellFace[j];
                 if (f < nI) {
-                    int side = m.cellSide[j];
-                    int o = side == 0 ? m.neighbour[f] : m.owner[f];
-                    if (loc[o] < 0 || mark[o] < t * 3 || mark[o] > t * 3 + 2) {
-                        err = "tile plan: stencil cell outside the two-ring halo";
-                        return false;
-                    }
+                    const int o = other(m, j);
+                    if (!S.in(o)) { err = "tile plan: stencil cell outside the two-ring halo"; return false; }
                     p.stEnt.push_back(loc[o]);
-                    const double* L = side == 0 ? &m.pVec[3 * (size_t)f] : &m.nVec[3 * (size_t)f];
+                    const double* L = m.cellSide[j] == 0 ? &m.pVec[3 * (size_t)f] : &m.nVec[3 * (size_t)f];
                     p.stL.insert(p.stL.end(), L, L + 3);
                 } else {
-                    int w = f - nI;
+                    const int w = f - nI;
                     p.stEnt.push_back(-(w + 1));
                     p.stL.insert(p.stL.end(), &m.bVec[3 * (size_t)w], &m.bVec[3 * (size_t)w] + 3);
                 }
@@ -109,12 +160,12 @@ bool build_tile_plan(const Mesh& m, int tileCells, TilePlan& p, std::string& err
         // internal faces with neighbour in T and owner outside T.
         std::vector<std::pair<int, int>> owned, extra;  // (global face order key, active face)
         for (int i = 0; i < h.nT; ++i) {
-            int c = lc[i];
+            const int c = lc[i];
             for (int j = m.cellOff[c]; j < m.cellOff[c + 1]; ++j) {
-                int f = m.cellFace[j];
+                const int f = m.cellFace[j];
                 if (f < nI) {
                     if (m.cellSide[j] == 0) owned.push_back({f, f});
-                    else if (mark[m.owner[f]] != t * 3) extra.push_back({f, f});
+                    else if (!S.inT(m.owner[f])) extra.push_back({f, f});
                 } else {
                     owned.push_back({m.wallFace[f - nI], f});
                 }
@@ -181,9 +232,13 @@ bool build_tile_plan(const Mesh& m, int tileCells, TilePlan& p, std::string& err
         p.maxT2 = std::max(p.maxT2, h.nT2);
         p.maxFA = std::max(p.maxFA, h.nFA);
         p.maxFB = std::max(p.maxFB, h.nFB);
-        for (int c : lc) { loc[c] = -1; }
-        p.hdr[t] = h;
+        p.sumT += h.nT;
+        p.sumT2 += h.nT2;
+        for (int c : lc) loc[c] = -1;
+        p.hdr.push_back(h);
+        ++t;
     }
+    p.nTiles = t;
     return true;
 }
 

@@ -3,7 +3,9 @@
 // on-chip least-squares gradient and upwind reconstruction need.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -37,6 +39,7 @@ struct TileFace {
 struct TilePlan {
     int nTiles = 0, tileCells = 0;
     int maxT = 0, maxT2 = 0, maxFA = 0, maxFB = 0;
+    long long sumT = 0, sumT2 = 0;  // halo ratio = sumT2 / sumT
     std::vector<TileHdr> hdr;
     std::vector<int32_t> cells;     // local -> global cell
     std::vector<int32_t> stOff;     // per tile (nT1+1) offsets into stEnt (absolute)
@@ -47,7 +50,12 @@ struct TilePlan {
     std::vector<int32_t> colorPerm; // per tile nFB local face ids grouped by colour
 };
 
-// Build the plan with about `tileCells` cells per tile.
-bool build_tile_plan(const Mesh& m, int tileCells, TilePlan& p, std::string& err);
+// Shared-memory bytes a tile needs, from |T|, |T u H1 u H2| and its owned faces.
+using SmemFn = std::function<size_t(int nT, int nT2, int nFA)>;
+
+// Build the plan: compact BFS tiles of at most maxTileCells cells, each the
+// largest that fits `budget` bytes of shared memory.
+bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t budget, TilePlan& p,
+                     std::string& err);
 
 }  // namespace dugks
