@@ -48,6 +48,31 @@ __device__ __forceinline__ void stv(float* p, const float (&d)[NPL]) {
     }
 }
 
+// Streaming (evict-first) access for the g~ rows: they are touched once per
+// sweep, so they should not push the tile's metadata out of L1.
+template <int NPL>
+__device__ __forceinline__ void ldv_cs(float (&d)[NPL], const float* p) {
+    if constexpr (NPL == 4) {
+        const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+        d[0] = t.x; d[1] = t.y; d[2] = t.z; d[3] = t.w;
+    } else if constexpr (NPL == 2) {
+        const float2 t = __ldcs(reinterpret_cast<const float2*>(p));
+        d[0] = t.x; d[1] = t.y;
+    } else {
+        d[0] = __ldcs(p);
+    }
+}
+template <int NPL>
+__device__ __forceinline__ void stv_cs(float* p, const float (&d)[NPL]) {
+    if constexpr (NPL == 4) {
+        __stcs(reinterpret_cast<float4*>(p), make_float4(d[0], d[1], d[2], d[3]));
+    } else if constexpr (NPL == 2) {
+        __stcs(reinterpret_cast<float2*>(p), make_float2(d[0], d[1]));
+    } else {
+        __stcs(p, d[0]);
+    }
+}
+
 // DV constants of this lane's NPL consecutive velocities in the current chunk.
 template <int D, int NPL>
 struct Lane32 {
@@ -113,37 +138,58 @@ __device__ __forceinline__ void eq_face(Eq32<D, H>& e, const FusedArgs<float>& A
 }
 
 // gbar+ rows of T u H1 u H2 (and for sweep B the g~new partial of T's rows).
+// Two rows per warp iteration keep two row loads in flight.
+template <int D, bool H, int NPL, bool PART>
+__device__ __forceinline__ void row32(const FusedArgs<float>& A, const TileHdr& hd, const Lane32<D, NPL>& L, int lc,
+                                      const float (&g0)[NPL], const float (&h0)[NPL], const Eq32<D, H>& eq, int lane,
+                                      float* sg, float* sh, float* sa, float* sah) {
+    constexpr int KC = 32 * NPL;
+    float g[NPL], h[NPL];
+#pragma unroll
+    for (int j = 0; j < NPL; ++j) {
+        g[j] = g0[j];
+        h[j] = H ? h0[j] : 0.0f;
+        eq.relax(L.x[j], L.y[j], L.z[j], L.mr[j], g[j], h[j]);
+    }
+    stv<NPL>(sg + lc * KC + lane * NPL, g);
+    if (H) stv<NPL>(sh + lc * KC + lane * NPL, h);
+    if (PART && lc < hd.nT) {
+        float pa[NPL], ph[NPL];
+#pragma unroll
+        for (int j = 0; j < NPL; ++j) {
+            pa[j] = fmaf(g[j] - g0[j], 1.0f / 3.0f, g[j]);
+            if (H) ph[j] = fmaf(h[j] - h0[j], 1.0f / 3.0f, h[j]);
+        }
+        stv<NPL>(sa + lc * KC + lane * NPL, pa);
+        if (H) stv<NPL>(sah + lc * KC + lane * NPL, ph);
+    }
+}
+
 template <int D, bool H, int NPL, int NW, bool PART>
 __device__ __forceinline__ void rows32(const FusedArgs<float>& A, const TileHdr& hd, const Lane32<D, NPL>& L, int v0,
                                        int lane, int warp, float* sg, float* sh, float* sa, float* sah) {
-    constexpr int KC = 32 * NPL;
     const int Vp = A.b.Vp;
-    for (int lc = warp; lc < hd.nT2; lc += NW) {
-        const int c = A.cells[hd.cellStart + lc];
-        Eq32<D, H> eq;
-        eq_cell<D, H>(eq, A, c);
-        const size_t gi = (size_t)c * Vp + v0 + lane * NPL;
-        float g0[NPL], h0[NPL], g[NPL], h[NPL];
-        ldv<NPL>(g0, A.gT + gi);
-        if (H) ldv<NPL>(h0, A.hT + gi);
+    for (int l0 = warp; l0 < hd.nT2; l0 += 2 * NW) {
+        const int l1 = l0 + NW;
+        const bool two = l1 < hd.nT2;
+        const int c0 = A.cells[hd.cellStart + l0];
+        const int c1 = two ? A.cells[hd.cellStart + l1] : c0;
+        const size_t i0 = (size_t)c0 * Vp + v0 + lane * NPL, i1 = (size_t)c1 * Vp + v0 + lane * NPL;
+        float ga[NPL], ha[NPL], gb[NPL], hb[NPL];
+        ldv_cs<NPL>(ga, A.gT + i0);
+        ldv_cs<NPL>(gb, A.gT + i1);
+        if (H) {
+            ldv_cs<NPL>(ha, A.hT + i0);
+            ldv_cs<NPL>(hb, A.hT + i1);
+        } else {
 #pragma unroll
-        for (int j = 0; j < NPL; ++j) {
-            g[j] = g0[j];
-            h[j] = H ? h0[j] : 0.0f;
-            eq.relax(L.x[j], L.y[j], L.z[j], L.mr[j], g[j], h[j]);
+            for (int j = 0; j < NPL; ++j) { ha[j] = 0.0f; hb[j] = 0.0f; }
         }
-        stv<NPL>(sg + lc * KC + lane * NPL, g);
-        if (H) stv<NPL>(sh + lc * KC + lane * NPL, h);
-        if (PART && lc < hd.nT) {
-            float pa[NPL], ph[NPL];
-#pragma unroll
-            for (int j = 0; j < NPL; ++j) {
-                pa[j] = fmaf(g[j] - g0[j], 1.0f / 3.0f, g[j]);
-                if (H) ph[j] = fmaf(h[j] - h0[j], 1.0f / 3.0f, h[j]);
-            }
-            stv<NPL>(sa + lc * KC + lane * NPL, pa);
-            if (H) stv<NPL>(sah + lc * KC + lane * NPL, ph);
-        }
+        Eq32<D, H> e0, e1;
+        eq_cell<D, H>(e0, A, c0);
+        eq_cell<D, H>(e1, A, c1);
+        row32<D, H, NPL, PART>(A, hd, L, l0, ga, ha, e0, lane, sg, sh, sa, sah);
+        if (two) row32<D, H, NPL, PART>(A, hd, L, l1, gb, hb, e1, lane, sg, sh, sa, sah);
     }
 }
 
@@ -601,8 +647,8 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A)
 #pragma unroll
                 for (int j = 0; j < NPL; ++j) h[j] = 0.0f;
             const size_t gi = (size_t)c * Vp + v0 + col;
-            stv<NPL>(A.gTn + gi, g);
-            if (H) stv<NPL>(A.hTn + gi, h);
+            stv_cs<NPL>(A.gTn + gi, g);
+            if (H) stv_cs<NPL>(A.hTn + gi, h);
             float m[NS];
 #pragma unroll
             for (int s = 0; s < NS; ++s) m[s] = 0.0f;
