@@ -4,6 +4,7 @@
 #include <memory>
 #include <string>
 
+#include "../cuda/noalloc.h"
 #include "dugks/dugks.h"
 #include "foam_io.h"
 #include "solver.h"
@@ -189,6 +190,17 @@ int dugks_profile_step(dugks_handle* h, int32_t nsteps, char* names, size_t name
             std::strncpy(names, joined.c_str(), names_len - 1);
             names[names_len - 1] = 0;
         }
+        return DUGKS_OK;
+    });
+}
+
+int dugks_macros_noalloc(dugks_handle* h, const double* g, const double* hh, double* rho, double* U, double* T,
+                         double* q) {
+    return call(h, [&](dugks::Solver& s) -> int {
+        std::string err;
+        cudaSetDevice(s.device());
+        const int rc = dugks::macros_noalloc(s.stepArgs(), s.device(), s.stream(), g, hh, rho, U, T, q, err);
+        if (rc != DUGKS_OK) return s.fail(rc, err);
         return DUGKS_OK;
     });
 }

@@ -48,6 +48,9 @@ public:
     cudaStream_t stream() const { return stream_; }
     const std::string& error() const { return err_; }
     const Mesh& mesh() const { return mesh_; }
+    // Step arguments with the current dt (device pointers of the handle).
+    StepArgs stepArgs() const { return argsNow(); }
+    int device() const { return device_; }
 
     // internal: allocation helper (recorded for release)
     template <typename T>

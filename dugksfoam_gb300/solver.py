@@ -30,7 +30,7 @@ EXPORTS = [
     "dugks_get_info", "dugks_set_dt", "dugks_get_dt", "dugks_set_stream", "dugks_step", "dugks_synchronize",
     "dugks_get_conum", "dugks_get_macros", "dugks_get_face_macros", "dugks_get_wall", "dugks_get_residual",
     "dugks_get_dist", "dugks_set_dist", "dugks_checkpoint_size", "dugks_checkpoint_save",
-    "dugks_checkpoint_load", "dugks_profile_step", "dugks_launches_per_step",
+    "dugks_checkpoint_load", "dugks_profile_step", "dugks_launches_per_step", "dugks_macros_noalloc",
 ]
 
 
@@ -105,6 +105,7 @@ def load_library(path: str | None = None):
     lib.dugks_checkpoint_load.argtypes = [vp, C.c_void_p, C.c_size_t]
     lib.dugks_profile_step.argtypes = [vp, C.c_int32, C.c_char_p, C.c_size_t, _dp, C.c_int32, _ip]
     lib.dugks_launches_per_step.argtypes = [vp, _ip]
+    lib.dugks_macros_noalloc.argtypes = [vp] + [vp] * 6
     _lib = lib
     return lib
 

@@ -177,6 +177,26 @@ int dugks_profile_step(dugks_handle* h, int32_t nsteps, char* names, size_t name
 /* Number of kernel launches one dugks_step(h, 1) issues. */
 int dugks_launches_per_step(dugks_handle* h, int32_t* n);
 
+/* Cell macros rho, U, T, q of distributions the caller holds on the device,
+ * computed without allocating any memory.  No counterpart in the reference:
+ * it is for callers that cannot allocate device memory where they need it --
+ * code inside a runtime that owns every device allocation, or a time loop
+ * that must not call cudaMalloc/cudaFree (they synchronise the device).
+ * g, hh: device arrays [n_cells][n_dv] in FP64 (the dugks_get_dist layout;
+ * hh may be NULL when the case has no h).  rho[n_cells], U[n_cells][3],
+ * T[n_cells], q[n_cells][3]: device output arrays (any may be NULL).  Uses the
+ * handle's velocity set, gas properties and dt (q is scaled by
+ * 2 tau/(2 tau + dt Pr) as in updateMacroVol, fvDVM.C:597-728) and runs
+ * asynchronously on the handle's stream; the caller orders its own writes of
+ * g/hh before the call and reads the outputs after dugks_synchronize.
+ * Scratch is a static device array shared by all calls: at most 262144 cells
+ * (larger cases are rejected with DUGKS_ERR_ARG); calls whose work overlaps on
+ * the GPU race.  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture. */
+int dugks_macros_noalloc(dugks_handle* h, const double* g, const double* hh, double* rho, double* U, double* T,
+                         double* q);
+
 #ifdef __cplusplus
 }
 #endif
