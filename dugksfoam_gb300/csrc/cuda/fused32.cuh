@@ -25,68 +25,67 @@
 
 namespace dugks {
 
-template <int NPL>
-__device__ __forceinline__ void ldv(float (&d)[NPL], const float* p) {
-    if constexpr (NPL == 4) {
-        const float4 t = *reinterpret_cast<const float4*>(p);
-        d[0] = t.x; d[1] = t.y; d[2] = t.z; d[3] = t.w;
-    } else if constexpr (NPL == 2) {
-        const float2 t = *reinterpret_cast<const float2*>(p);
-        d[0] = t.x; d[1] = t.y;
-    } else {
-        d[0] = *p;
-    }
-}
-template <int NPL>
-__device__ __forceinline__ void stv(float* p, const float (&d)[NPL]) {
-    if constexpr (NPL == 4) {
-        *reinterpret_cast<float4*>(p) = make_float4(d[0], d[1], d[2], d[3]);
-    } else if constexpr (NPL == 2) {
-        *reinterpret_cast<float2*>(p) = make_float2(d[0], d[1]);
-    } else {
-        *p = d[0];
-    }
+
+// Packed FP32 pair arithmetic (sm_100+): each lane's NPL velocities are held
+// as NPL/2 float2 pairs and every per-velocity operation is one packed
+// instruction per pair.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a); }
+__device__ __forceinline__ float2 sel2(bool x0, bool x1, float2 a, float2 b) {  // per element: x ? a : b
+    return make_float2(x0 ? a.x : b.x, x1 ? a.y : b.y);
 }
 
-// Streaming (evict-first) access for the g~ rows: they are touched once per
-// sweep, so they should not push the tile's metadata out of L1.
-template <int NPL>
-__device__ __forceinline__ void ldv_cs(float (&d)[NPL], const float* p) {
-    if constexpr (NPL == 4) {
-        const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
-        d[0] = t.x; d[1] = t.y; d[2] = t.z; d[3] = t.w;
-    } else if constexpr (NPL == 2) {
-        const float2 t = __ldcs(reinterpret_cast<const float2*>(p));
-        d[0] = t.x; d[1] = t.y;
+template <int NP>
+__device__ __forceinline__ void ldp(float2 (&d)[NP], const float* p) {
+    if constexpr (NP == 2) {
+        const float4 t = *reinterpret_cast<const float4*>(p);
+        d[0] = make_float2(t.x, t.y);
+        d[1] = make_float2(t.z, t.w);
     } else {
-        d[0] = __ldcs(p);
+        d[0] = *reinterpret_cast<const float2*>(p);
     }
 }
-template <int NPL>
-__device__ __forceinline__ void stv_cs(float* p, const float (&d)[NPL]) {
-    if constexpr (NPL == 4) {
-        __stcs(reinterpret_cast<float4*>(p), make_float4(d[0], d[1], d[2], d[3]));
-    } else if constexpr (NPL == 2) {
-        __stcs(reinterpret_cast<float2*>(p), make_float2(d[0], d[1]));
+template <int NP>
+__device__ __forceinline__ void stp(float* p, const float2 (&d)[NP]) {
+    if constexpr (NP == 2) *reinterpret_cast<float4*>(p) = make_float4(d[0].x, d[0].y, d[1].x, d[1].y);
+    else *reinterpret_cast<float2*>(p) = d[0];
+}
+// Streaming (evict-first) access for the g~ rows: they are touched once per
+// sweep, so they should not push the tile's metadata out of L1.
+template <int NP>
+__device__ __forceinline__ void ldp_cs(float2 (&d)[NP], const float* p) {
+    if constexpr (NP == 2) {
+        const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
+        d[0] = make_float2(t.x, t.y);
+        d[1] = make_float2(t.z, t.w);
     } else {
-        __stcs(p, d[0]);
+        d[0] = __ldcs(reinterpret_cast<const float2*>(p));
     }
+}
+template <int NP>
+__device__ __forceinline__ void stp_cs(float* p, const float2 (&d)[NP]) {
+    if constexpr (NP == 2) __stcs(reinterpret_cast<float4*>(p), make_float4(d[0].x, d[0].y, d[1].x, d[1].y));
+    else __stcs(reinterpret_cast<float2*>(p), d[0]);
 }
 
 // DV constants of this lane's NPL consecutive velocities in the current chunk.
 template <int D, int NPL>
 struct Lane32 {
-    float x[NPL], y[NPL], z[NPL], w[NPL], mr[NPL];
+    static constexpr int NP = NPL / 2;
+    float2 x[NP], y[NP], z[NP], w[NP], mr[NP];
     __device__ __forceinline__ void load(const FusedArgs<float>& A, int v0, int lane) {
         const int Vp = A.b.Vp, v = v0 + lane * NPL;
-        ldv<NPL>(x, A.xi + v);
-        ldv<NPL>(y, A.xi + Vp + v);
-        if (D == 3) ldv<NPL>(z, A.xi + 2 * Vp + v);
+        ldp<NP>(x, A.xi + v);
+        ldp<NP>(y, A.xi + Vp + v);
+        if (D == 3) ldp<NP>(z, A.xi + 2 * Vp + v);
         else
 #pragma unroll
-            for (int j = 0; j < NPL; ++j) z[j] = 0.0f;
-        ldv<NPL>(w, A.w + v);
-        ldv<NPL>(mr, A.mref + v);
+            for (int p = 0; p < NP; ++p) z[p] = f2(0.0f);
+        ldp<NP>(w, A.w + v);
+        ldp<NP>(mr, A.mref + v);
     }
 };
 
@@ -107,20 +106,26 @@ struct Eq32 {
         K2 = -2.0f * (float)K;
         hf = hrefFac;
     }
-    __device__ __forceinline__ float tau(const float* blk) const { return blk[10]; }
-    __device__ __forceinline__ void relax(float xx, float xy, float xz, float mr, float& g, float& h) const {
-        const float cx = xx - ux, cy = xy - uy;
-        const float cz = D == 3 ? xz - uz : 0.0f;
-        const float c2 = D == 3 ? fmaf(cz, cz, fmaf(cy, cy, cx * cx)) : fmaf(cy, cy, cx * cx);
-        const float e = exp2f(kexp * c2) * aA;
-        const float phi = D == 3 ? fmaf(cz, qz, fmaf(cy, qy, cx * qx)) : fmaf(cy, qy, cx * qx);
-        const float c2n = c2 * invRT;
-        const float ags = fmaf(e * phi, c2n - (float)(D + 2), e);
-        g = fmaf(-a, g + mr, g + ags);
+    template <int NPL>
+    __device__ __forceinline__ void relax(const Lane32<D, NPL>& L, int p, float2& g, float2& h) const {
+        const float2 cx = sub2(L.x[p], f2(ux)), cy = sub2(L.y[p], f2(uy));
+        float2 c2 = fma2(cy, cy, mul2(cx, cx));
+        float2 phi = fma2(cy, f2(qy), mul2(cx, f2(qx)));
+        if (D == 3) {
+            const float2 cz = sub2(L.z[p], f2(uz));
+            c2 = fma2(cz, cz, c2);
+            phi = fma2(cz, f2(qz), phi);
+        }
+        const float2 t = mul2(c2, f2(kexp));
+        const float2 e = mul2(make_float2(exp2f(t.x), exp2f(t.y)), f2(aA));
+        const float2 c2n = mul2(c2, f2(invRT));
+        const float2 ep = mul2(e, phi);
+        const float2 ags = fma2(ep, add2(c2n, f2(-(float)(D + 2))), e);
+        g = fma2(f2(-a), add2(g, L.mr[p]), add2(g, ags));
         if (H) {
-            const float eh = e * RT;
-            const float ahs = fmaf(eh * phi, fmaf(c2n - (float)D, KD, K2), eh * KD);
-            h = fmaf(-a, h + mr * hf, h + ahs);
+            const float2 eh = mul2(e, f2(RT));
+            const float2 ahs = fma2(mul2(ep, f2(RT)), fma2(add2(c2n, f2(-(float)D)), f2(KD), f2(K2)), mul2(eh, f2(KD)));
+            h = fma2(f2(-a), add2(h, mul2(L.mr[p], f2(hf))), add2(h, ahs));
         }
     }
 };
@@ -140,34 +145,35 @@ __device__ __forceinline__ void eq_face(Eq32<D, H>& e, const FusedArgs<float>& A
 // gbar+ rows of T u H1 u H2 (and for sweep B the g~new partial of T's rows).
 // Two rows per warp iteration keep two row loads in flight.
 template <int D, bool H, int NPL, bool PART>
-__device__ __forceinline__ void row32(const FusedArgs<float>& A, const TileHdr& hd, const Lane32<D, NPL>& L, int lc,
-                                      const float (&g0)[NPL], const float (&h0)[NPL], const Eq32<D, H>& eq, int lane,
-                                      float* sg, float* sh, float* sa, float* sah) {
-    constexpr int KC = 32 * NPL;
-    float g[NPL], h[NPL];
+__device__ __forceinline__ void row32(const TileHdr& hd, const Lane32<D, NPL>& L, int lc, const float2* g0,
+                                      const float2* h0, const Eq32<D, H>& eq, int lane, float* sg, float* sh,
+                                      float* sa, float* sah) {
+    constexpr int KC = 32 * NPL, NP = NPL / 2;
+    float2 g[NP], h[NP];
 #pragma unroll
-    for (int j = 0; j < NPL; ++j) {
-        g[j] = g0[j];
-        h[j] = H ? h0[j] : 0.0f;
-        eq.relax(L.x[j], L.y[j], L.z[j], L.mr[j], g[j], h[j]);
+    for (int p = 0; p < NP; ++p) {
+        g[p] = g0[p];
+        h[p] = H ? h0[p] : f2(0.0f);
+        eq.relax(L, p, g[p], h[p]);
     }
-    stv<NPL>(sg + lc * KC + lane * NPL, g);
-    if (H) stv<NPL>(sh + lc * KC + lane * NPL, h);
-    if (PART && lc < hd.nT) {
-        float pa[NPL], ph[NPL];
+    stp<NP>(sg + lc * KC + lane * NPL, g);
+    if (H) stp<NP>(sh + lc * KC + lane * NPL, h);
+    if (PART && lc < hd.nT) {  // g+ + (g+ - g~)/3: exact when g+ == g~ (no FP32 mass bias)
+        float2 pa[NP], ph[NP];
 #pragma unroll
-        for (int j = 0; j < NPL; ++j) {
-            pa[j] = fmaf(g[j] - g0[j], 1.0f / 3.0f, g[j]);
-            if (H) ph[j] = fmaf(h[j] - h0[j], 1.0f / 3.0f, h[j]);
+        for (int p = 0; p < NP; ++p) {
+            pa[p] = fma2(sub2(g[p], g0[p]), f2(1.0f / 3.0f), g[p]);
+            if (H) ph[p] = fma2(sub2(h[p], h0[p]), f2(1.0f / 3.0f), h[p]);
         }
-        stv<NPL>(sa + lc * KC + lane * NPL, pa);
-        if (H) stv<NPL>(sah + lc * KC + lane * NPL, ph);
+        stp<NP>(sa + lc * KC + lane * NPL, pa);
+        if (H) stp<NP>(sah + lc * KC + lane * NPL, ph);
     }
 }
 
 template <int D, bool H, int NPL, int NW, bool PART>
 __device__ __forceinline__ void rows32(const FusedArgs<float>& A, const TileHdr& hd, const Lane32<D, NPL>& L, int v0,
                                        int lane, int warp, float* sg, float* sh, float* sa, float* sah) {
+    constexpr int NP = NPL / 2;
     const int Vp = A.b.Vp;
     for (int l0 = warp; l0 < hd.nT2; l0 += 2 * NW) {
         const int l1 = l0 + NW;
@@ -175,21 +181,18 @@ __device__ __forceinline__ void rows32(const FusedArgs<float>& A, const TileHdr&
         const int c0 = A.cells[hd.cellStart + l0];
         const int c1 = two ? A.cells[hd.cellStart + l1] : c0;
         const size_t i0 = (size_t)c0 * Vp + v0 + lane * NPL, i1 = (size_t)c1 * Vp + v0 + lane * NPL;
-        float ga[NPL], ha[NPL], gb[NPL], hb[NPL];
-        ldv_cs<NPL>(ga, A.gT + i0);
-        ldv_cs<NPL>(gb, A.gT + i1);
+        float2 ga[NP], ha[NP], gb[NP], hb[NP];
+        ldp_cs<NP>(ga, A.gT + i0);
+        ldp_cs<NP>(gb, A.gT + i1);
         if (H) {
-            ldv_cs<NPL>(ha, A.hT + i0);
-            ldv_cs<NPL>(hb, A.hT + i1);
-        } else {
-#pragma unroll
-            for (int j = 0; j < NPL; ++j) { ha[j] = 0.0f; hb[j] = 0.0f; }
+            ldp_cs<NP>(ha, A.hT + i0);
+            ldp_cs<NP>(hb, A.hT + i1);
         }
         Eq32<D, H> e0, e1;
         eq_cell<D, H>(e0, A, c0);
         eq_cell<D, H>(e1, A, c1);
-        row32<D, H, NPL, PART>(A, hd, L, l0, ga, ha, e0, lane, sg, sh, sa, sah);
-        if (two) row32<D, H, NPL, PART>(A, hd, L, l1, gb, hb, e1, lane, sg, sh, sa, sah);
+        row32<D, H, NPL, PART>(hd, L, l0, ga, ha, e0, lane, sg, sh, sa, sah);
+        if (two) row32<D, H, NPL, PART>(hd, L, l1, gb, hb, e1, lane, sg, sh, sa, sah);
     }
 }
 
@@ -207,188 +210,157 @@ struct Face32 {
         dOx = g1.x; dOy = g1.y; dOz = g1.z; iVn = g1.w;
         dNx = g2.x; dNy = g2.y; dNz = g2.z;
     }
+    template <int D, int NPL>
+    __device__ __forceinline__ float2 xs(const Lane32<D, NPL>& L, int p) const {
+        float2 s = fma2(L.y[p], f2(Sy), mul2(L.x[p], f2(Sx)));
+        if (D == 3) s = fma2(L.z[p], f2(Sz), s);
+        return s;
+    }
 };
 
-// Upwind reconstruction gbar_f = gbar+_u + sum_e (L_e.(d_u - xi dt/2)) (gbar+_o(e) - gbar+_u)
-// for this lane's NPL velocities, u = owner (side 0) or neighbour (side 1) per
-// velocity; tie (xi.S == 0) velocities average both sides.  For walls only the
-// owner side exists.  When GRADW is set the owner gradient itself is also
-// returned (lagged boundary gradient of walls).
-template <int D, bool H, int NPL, bool WALL>
-__device__ __forceinline__ void recon32(const FusedArgs<float>& A, const Face32& F, const Lane32<D, NPL>& L,
-                                        const float* sg, const float* sh, int lane, int v0, const float (&xs)[NPL],
-                                        float (&gf)[NPL], float (&hf)[NPL], float (&gw)[D][NPL],
-                                        float (&hw)[D][NPL]) {
-    constexpr int KC = 32 * NPL;
-    const float hdt = 0.5f * A.dt;
-    const int col = lane * NPL;
-    const int Vp = A.b.Vp;
-    // side per velocity: 0 owner, 1 neighbour, 2 tie (both)
-    int side[NPL];
-    bool anyTie = false;
+// One side's reconstruction sum over its stencil entry k:
+//   acc += beta (phi_o - phi_u),  beta = L.(d_u - xi dt/2),
+// with the neighbour row (or the lagged wall gradient) read for all pairs.
+template <int D, bool H, int NP, bool GRAD>
+__device__ __forceinline__ void side_entry(const FusedArgs<float>& A, int e, float dx, float dy, float dz,
+                                           const float2 (&cu)[NP], const float2 (&hu)[NP], const float* sg,
+                                           const float* sh, int col, int v0, const float2* xx, const float2* xy,
+                                           const float2* xz, float2 (&acc)[NP], float2 (&acch)[NP],
+                                           float2 (&gw)[D][NP], float2 (&hw)[D][NP]) {
+    constexpr int KC = 64 * NP;
+    const float4 ent = A.st4[e];
+    const int o = __float_as_int(ent.w);
+    const float hdt = -0.5f * A.dt;
+    float al = fmaf(ent.y, dy, ent.x * dx);
+    if (D == 3) al = fmaf(ent.z, dz, al);
+    const float2 lx = f2(hdt * ent.x), ly = f2(hdt * ent.y), lz = f2(hdt * ent.z);
+    float2 r[NP], q[NP];
+    if (o >= 0) {
+        ldp<NP>(r, sg + o * KC + col);
+        if (H) ldp<NP>(q, sh + o * KC + col);
+    } else {  // wall entry: phi_b - phi_P = G_b / deltaCoeff
+        const int wf = -o - 1;
+        const float idc = A.wall4[wf].y;
+        float2 tg[NP], th[NP];
+        ldp<NP>(tg, A.Gbg + (size_t)wf * A.b.Vp + v0 + col);
+        if (H) ldp<NP>(th, A.Gbh + (size_t)wf * A.b.Vp + v0 + col);
 #pragma unroll
-    for (int j = 0; j < NPL; ++j) {
-        side[j] = WALL ? 0 : (xs[j] > 0.0f ? 0 : (xs[j] < 0.0f ? 1 : 2));
-        anyTie |= side[j] == 2;
-    }
-    float cO[NPL], cN[NPL], hO[NPL], hN[NPL];
-    ldv<NPL>(cO, sg + F.r.ownL * KC + col);
-    if (H) ldv<NPL>(hO, sh + F.r.ownL * KC + col);
-    if (!WALL) {
-        ldv<NPL>(cN, sg + F.r.neiL * KC + col);
-        if (H) ldv<NPL>(hN, sh + F.r.neiL * KC + col);
-    }
-    float accG[NPL], accH[NPL], accG2[NPL], accH2[NPL];
-#pragma unroll
-    for (int j = 0; j < NPL; ++j) {
-        accG[j] = 0.0f; accH[j] = 0.0f; accG2[j] = 0.0f; accH2[j] = 0.0f;
-        if (WALL) {
-#pragma unroll
-            for (int k = 0; k < D; ++k) { gw[k][j] = 0.0f; if (H) hw[k][j] = 0.0f; }
+        for (int p = 0; p < NP; ++p) {
+            r[p] = fma2(tg[p], f2(idc), cu[p]);
+            if (H) q[p] = fma2(th[p], f2(idc), hu[p]);
         }
     }
-    const int nO = F.r.stO1 - F.r.stO0, nN = WALL ? 0 : F.r.stN1 - F.r.stN0;
-    const int nE = nO > nN ? nO : nN;
-    for (int k = 0; k < nE; ++k) {
-        // owner-side entry
-        float LOx = 0.f, LOy = 0.f, LOz = 0.f, aO = 0.f;
-        float rO[NPL], qO[NPL];
 #pragma unroll
-        for (int j = 0; j < NPL; ++j) { rO[j] = cO[j]; qO[j] = H ? hO[j] : 0.f; }
-        if (k < nO) {
-            const float4 e = A.st4[F.r.stO0 + k];
-            const int o = __float_as_int(e.w);
-            LOx = e.x; LOy = e.y; LOz = e.z;
-            aO = fmaf(LOy, F.dOy, LOx * F.dOx);
-            if (D == 3) aO = fmaf(LOz, F.dOz, aO);
-            if (o >= 0) {
-                ldv<NPL>(rO, sg + o * KC + col);
-                if (H) ldv<NPL>(qO, sh + o * KC + col);
-            } else {
-                const int wf = -o - 1;
-                const float idc = A.wall4[wf].y;
-                float tg[NPL], th[NPL];
-                ldv<NPL>(tg, A.Gbg + (size_t)wf * Vp + v0 + col);
-                if (H) ldv<NPL>(th, A.Gbh + (size_t)wf * Vp + v0 + col);
-#pragma unroll
-                for (int j = 0; j < NPL; ++j) {
-                    rO[j] = fmaf(tg[j], idc, cO[j]);
-                    if (H) qO[j] = fmaf(th[j], idc, hO[j]);
-                }
+    for (int p = 0; p < NP; ++p) {
+        float2 beta = fma2(ly, xy[p], fma2(lx, xx[p], f2(al)));
+        if (D == 3) beta = fma2(lz, xz[p], beta);
+        const float2 dg = sub2(r[p], cu[p]);
+        acc[p] = fma2(beta, dg, acc[p]);
+        float2 dh = f2(0.0f);
+        if (H) {
+            dh = sub2(q[p], hu[p]);
+            acch[p] = fma2(beta, dh, acch[p]);
+        }
+        if (GRAD) {
+            gw[0][p] = fma2(f2(ent.x), dg, gw[0][p]);
+            gw[1][p] = fma2(f2(ent.y), dg, gw[1][p]);
+            if (D == 3) gw[2][p] = fma2(f2(ent.z), dg, gw[2][p]);
+            if (H) {
+                hw[0][p] = fma2(f2(ent.x), dh, hw[0][p]);
+                hw[1][p] = fma2(f2(ent.y), dh, hw[1][p]);
+                if (D == 3) hw[2][p] = fma2(f2(ent.z), dh, hw[2][p]);
             }
-        }
-        float LNx = 0.f, LNy = 0.f, LNz = 0.f, aN = 0.f;
-        float rN[NPL], qN[NPL];
-        if (!WALL) {
-#pragma unroll
-            for (int j = 0; j < NPL; ++j) { rN[j] = cN[j]; qN[j] = H ? hN[j] : 0.f; }
-            if (k < nN) {
-                const float4 e = A.st4[F.r.stN0 + k];
-                const int o = __float_as_int(e.w);
-                LNx = e.x; LNy = e.y; LNz = e.z;
-                aN = fmaf(LNy, F.dNy, LNx * F.dNx);
-                if (D == 3) aN = fmaf(LNz, F.dNz, aN);
-                if (o >= 0) {
-                    ldv<NPL>(rN, sg + o * KC + col);
-                    if (H) ldv<NPL>(qN, sh + o * KC + col);
-                } else {
-                    const int wf = -o - 1;
-                    const float idc = A.wall4[wf].y;
-                    float tg[NPL], th[NPL];
-                    ldv<NPL>(tg, A.Gbg + (size_t)wf * Vp + v0 + col);
-                    if (H) ldv<NPL>(th, A.Gbh + (size_t)wf * Vp + v0 + col);
-#pragma unroll
-                    for (int j = 0; j < NPL; ++j) {
-                        rN[j] = fmaf(tg[j], idc, cN[j]);
-                        if (H) qN[j] = fmaf(th[j], idc, hN[j]);
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int j = 0; j < NPL; ++j) {
-            if (WALL) {
-                const float dg = rO[j] - cO[j], dh = H ? qO[j] - hO[j] : 0.f;
-                gw[0][j] = fmaf(LOx, dg, gw[0][j]);
-                gw[1][j] = fmaf(LOy, dg, gw[1][j]);
-                if (D == 3) gw[2][j] = fmaf(LOz, dg, gw[2][j]);
-                if (H) {
-                    hw[0][j] = fmaf(LOx, dh, hw[0][j]);
-                    hw[1][j] = fmaf(LOy, dh, hw[1][j]);
-                    if (D == 3) hw[2][j] = fmaf(LOz, dh, hw[2][j]);
-                }
-                float lx = LOx * L.x[j];
-                lx = fmaf(LOy, L.y[j], lx);
-                if (D == 3) lx = fmaf(LOz, L.z[j], lx);
-                const float beta = fmaf(-hdt, lx, aO);
-                accG[j] = fmaf(beta, dg, accG[j]);
-                if (H) accH[j] = fmaf(beta, dh, accH[j]);
-            } else {
-                const bool n = side[j] == 1;
-                const float Lx = n ? LNx : LOx, Ly = n ? LNy : LOy, Lz = n ? LNz : LOz, al = n ? aN : aO;
-                const float dg = n ? rN[j] - cN[j] : rO[j] - cO[j];
-                const float dh = H ? (n ? qN[j] - hN[j] : qO[j] - hO[j]) : 0.f;
-                float lx = Lx * L.x[j];
-                lx = fmaf(Ly, L.y[j], lx);
-                if (D == 3) lx = fmaf(Lz, L.z[j], lx);
-                const float beta = fmaf(-hdt, lx, al);
-                accG[j] = fmaf(beta, dg, accG[j]);
-                if (H) accH[j] = fmaf(beta, dh, accH[j]);
-                if (anyTie && side[j] == 2) {  // tie: the neighbour side separately
-                    float ln = LNx * L.x[j];
-                    ln = fmaf(LNy, L.y[j], ln);
-                    if (D == 3) ln = fmaf(LNz, L.z[j], ln);
-                    const float bn = fmaf(-hdt, ln, aN);
-                    accG2[j] = fmaf(bn, rN[j] - cN[j], accG2[j]);
-                    if (H) accH2[j] = fmaf(bn, qN[j] - hN[j], accH2[j]);
-                }
-            }
-        }
-    }
-#pragma unroll
-    for (int j = 0; j < NPL; ++j) {
-        if (WALL || side[j] == 0) {
-            gf[j] = cO[j] + accG[j];
-            if (H) hf[j] = hO[j] + accH[j];
-        } else if (side[j] == 1) {
-            gf[j] = cN[j] + accG[j];
-            if (H) hf[j] = hN[j] + accH[j];
-        } else {
-            gf[j] = 0.5f * ((cN[j] + accG2[j]) + (cO[j] + accG[j]));
-            if (H) hf[j] = 0.5f * ((hN[j] + accH2[j]) + (hO[j] + accH[j]));
         }
     }
 }
 
-// Deviation moments of NPL velocities about ur into the lane's slots.
+// Upwind reconstruction gbar_f = gbar+_u + sum_e (L_e.(d_u - xi dt/2)) (gbar+_o(e) - gbar+_u)
+// for the lane's velocities.  Both sides are summed (packed, no per-entry
+// selects) and each velocity takes the owner side when xi.S > 0, the
+// neighbour side when xi.S < 0 and their average when xi.S == 0.  Walls have
+// only the owner side; there the owner gradient itself is also returned.
+template <int D, bool H, int NPL, bool WALL>
+__device__ __forceinline__ void recon32(const FusedArgs<float>& A, const Face32& F, const Lane32<D, NPL>& L,
+                                        const float* sg, const float* sh, int lane, int v0, const float2* xs,
+                                        float2 (&gf)[NPL / 2], float2 (&hf)[NPL / 2], float2 (&gw)[D][NPL / 2],
+                                        float2 (&hw)[D][NPL / 2]) {
+    constexpr int KC = 32 * NPL, NP = NPL / 2;
+    const int col = lane * NPL;
+    float2 cO[NP], hO[NP], cN[NP], hN[NP];
+    float2 aO[NP], ahO[NP], aN[NP], ahN[NP];
+    ldp<NP>(cO, sg + F.r.ownL * KC + col);
+    if (H) ldp<NP>(hO, sh + F.r.ownL * KC + col);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        aO[p] = f2(0.f); ahO[p] = f2(0.f); aN[p] = f2(0.f); ahN[p] = f2(0.f);
+        if (!H) { hO[p] = f2(0.f); hN[p] = f2(0.f); }
+#pragma unroll
+        for (int k = 0; k < D; ++k) { gw[k][p] = f2(0.f); hw[k][p] = f2(0.f); }
+    }
+    for (int e = F.r.stO0; e < F.r.stO1; ++e)
+        side_entry<D, H, NP, WALL>(A, e, F.dOx, F.dOy, F.dOz, cO, hO, sg, sh, col, v0, L.x, L.y, L.z, aO, ahO, gw, hw);
+    if (WALL) {
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            gf[p] = add2(cO[p], aO[p]);
+            if (H) hf[p] = add2(hO[p], ahO[p]);
+        }
+        return;
+    }
+    ldp<NP>(cN, sg + F.r.neiL * KC + col);
+    if (H) ldp<NP>(hN, sh + F.r.neiL * KC + col);
+    float2 dw[D][NP], dhw[D][NP];
+    for (int e = F.r.stN0; e < F.r.stN1; ++e)
+        side_entry<D, H, NP, false>(A, e, F.dNx, F.dNy, F.dNz, cN, hN, sg, sh, col, v0, L.x, L.y, L.z, aN, ahN, dw, dhw);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float2 go = add2(cO[p], aO[p]), gn = add2(cN[p], aN[p]);
+        const float2 ho = H ? add2(hO[p], ahO[p]) : f2(0.f), hn = H ? add2(hN[p], ahN[p]) : f2(0.f);
+        const float2 gt = mul2(add2(gn, go), f2(0.5f)), ht = mul2(add2(hn, ho), f2(0.5f));
+        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f, n0 = xs[p].x < 0.f, n1 = xs[p].y < 0.f;
+        gf[p] = sel2(o0, o1, go, sel2(n0, n1, gn, gt));
+        if (H) hf[p] = sel2(o0, o1, ho, sel2(n0, n1, hn, ht));
+    }
+}
+
+// Deviation moments of the lane's velocities about ur into its slots
+// (mask: per-velocity inclusion, used on walls for the outgoing half).
 template <int D, bool H, int NPL, int NS>
-__device__ __forceinline__ void mom32(float (&m)[NS], const Lane32<D, NPL>& L, const float* ur, const float (&g)[NPL],
-                                      const float (&h)[NPL], const bool* use) {
+__device__ __forceinline__ void mom32(float (&m)[NS], const Lane32<D, NPL>& L, const float* ur,
+                                      const float2 (&g)[NPL / 2], const float2 (&h)[NPL / 2], const float2* mask) {
     using SL = Slots<D, H>;
+    constexpr int NP = NPL / 2;
+    float2 m2[NS];
 #pragma unroll
-    for (int j = 0; j < NPL; ++j) {
-        if (use && !use[j]) continue;
-        const float c[3] = {L.x[j] - ur[0], L.y[j] - ur[1], D == 3 ? L.z[j] - ur[2] : 0.0f};
-        const float wg = L.w[j] * g[j];
-        m[0] += wg;
-        float c2 = c[0] * c[0];
+    for (int s = 0; s < NS; ++s) m2[s] = f2(0.f);
 #pragma unroll
-        for (int i = 1; i < D; ++i) c2 = fmaf(c[i], c[i], c2);
+    for (int p = 0; p < NP; ++p) {
+        const float2 c[3] = {sub2(L.x[p], f2(ur[0])), sub2(L.y[p], f2(ur[1])),
+                             D == 3 ? sub2(L.z[p], f2(ur[2])) : f2(0.f)};
+        float2 wg = mul2(L.w[p], g[p]);
+        if (mask) wg = mul2(wg, mask[p]);
+        m2[0] = add2(m2[0], wg);
+        float2 c2 = mul2(c[0], c[0]);
+#pragma unroll
+        for (int i = 1; i < D; ++i) c2 = fma2(c[i], c[i], c2);
 #pragma unroll
         for (int i = 0; i < D; ++i) {
-            const float t = wg * c[i];
-            m[SL::M1 + i] += t;
+            const float2 t = mul2(wg, c[i]);
+            m2[SL::M1 + i] = add2(m2[SL::M1 + i], t);
 #pragma unroll
-            for (int k = i; k < D; ++k) m[SL::M2 + sym<D>(i, k)] = fmaf(t, c[k], m[SL::M2 + sym<D>(i, k)]);
-            m[SL::M3 + i] = fmaf(t, c2, m[SL::M3 + i]);
+            for (int k = i; k < D; ++k) m2[SL::M2 + sym<D>(i, k)] = fma2(t, c[k], m2[SL::M2 + sym<D>(i, k)]);
+            m2[SL::M3 + i] = fma2(t, c2, m2[SL::M3 + i]);
         }
         if (H) {
-            const float wh = L.w[j] * h[j];
-            m[SL::H0] += wh;
+            float2 wh = mul2(L.w[p], h[p]);
+            if (mask) wh = mul2(wh, mask[p]);
+            m2[SL::H0] = add2(m2[SL::H0], wh);
 #pragma unroll
-            for (int i = 0; i < D; ++i) m[SL::H1 + i] = fmaf(wh, c[i], m[SL::H1 + i]);
+            for (int i = 0; i < D; ++i) m2[SL::H1 + i] = fma2(wh, c[i], m2[SL::H1 + i]);
         }
     }
+#pragma unroll
+    for (int s = 0; s < SL::NM; ++s) m[s] += m2[s].x + m2[s].y;
 }
 
 // Moments of the reference Maxwellian about u (FP64, scaled units) from its raw
@@ -422,7 +394,7 @@ __device__ __forceinline__ void ref_moments_about(const double* R, const double*
 template <int D, bool H, int NPL, int NW>
 __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A) {
     using SL = Slots<D, H>;
-    constexpr int NS = SL::NS, KC = 32 * NPL;
+    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
     extern __shared__ __align__(16) unsigned char smem[];
     const TileHdr hd = A.hdr[blockIdx.x];
     const StepArgs& b = A.b;
@@ -449,36 +421,33 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A)
             F.load(A, hd.faceStart + lf);
             const float4 u4 = A.uref4[F.r.a];
             const float ur[3] = {u4.x, u4.y, u4.z};
-            float xs[NPL];
+            float2 xs[NP];
 #pragma unroll
-            for (int j = 0; j < NPL; ++j) {
-                xs[j] = fmaf(L.y[j], F.Sy, L.x[j] * F.Sx);
-                if (D == 3) xs[j] = fmaf(L.z[j], F.Sz, xs[j]);
-            }
-            float gf[NPL], hf[NPL], gw[D][NPL], hw[D][NPL];
+            for (int p = 0; p < NP; ++p) xs[p] = F.xs<D, NPL>(L, p);
+            float2 gf[NP], hf[NP], gw[D][NP], hw[D][NP];
             float m[NS];
 #pragma unroll
             for (int s = 0; s < NS; ++s) m[s] = 0.0f;
             if (F.r.w >= 0) {
                 recon32<D, H, NPL, true>(A, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
-                float gn[NPL], hn[NPL];
-                bool use[NPL];
+                float2 gn[NP], hn[NP], use[NP];
+                float fl = 0.0f;
 #pragma unroll
-                for (int j = 0; j < NPL; ++j) {
-                    gn[j] = gw[0][j] * F.dNx;
-                    gn[j] = fmaf(gw[1][j], F.dNy, gn[j]);
-                    if (D == 3) gn[j] = fmaf(gw[2][j], F.dNz, gn[j]);
+                for (int p = 0; p < NP; ++p) {
+                    gn[p] = fma2(gw[1][p], f2(F.dNy), mul2(gw[0][p], f2(F.dNx)));
+                    if (D == 3) gn[p] = fma2(gw[2][p], f2(F.dNz), gn[p]);
                     if (H) {
-                        hn[j] = hw[0][j] * F.dNx;
-                        hn[j] = fmaf(hw[1][j], F.dNy, hn[j]);
-                        if (D == 3) hn[j] = fmaf(hw[2][j], F.dNz, hn[j]);
+                        hn[p] = fma2(hw[1][p], f2(F.dNy), mul2(hw[0][p], f2(F.dNx)));
+                        if (D == 3) hn[p] = fma2(hw[2][p], f2(F.dNz), hn[p]);
                     }
-                    use[j] = xs[j] > 0.0f;
-                    if (use[j]) m[SL::FLUX] = fmaf(L.w[j] * xs[j], gf[j], m[SL::FLUX]);
+                    use[p] = make_float2(xs[p].x > 0.f ? 1.f : 0.f, xs[p].y > 0.f ? 1.f : 0.f);
+                    const float2 fx = mul2(mul2(mul2(L.w[p], xs[p]), gf[p]), use[p]);
+                    fl += fx.x + fx.y;
                 }
+                m[SL::FLUX] = fl;
                 const size_t wi = (size_t)F.r.w * Vp + v0 + lane * NPL;
-                stv<NPL>(A.Gbgn + wi, gn);
-                if (H) stv<NPL>(A.Gbhn + wi, hn);
+                stp<NP>(A.Gbgn + wi, gn);
+                if (H) stp<NP>(A.Gbhn + wi, hn);
                 mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
             } else {
                 recon32<D, H, NPL, false>(A, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
@@ -546,7 +515,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A)
 template <int D, bool H, int NPL, int NW>
 __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A) {
     using SL = Slots<D, H>;
-    constexpr int NS = SL::NS, KC = 32 * NPL;
+    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
     extern __shared__ __align__(16) unsigned char smem[];
     const TileHdr hd = A.hdr[blockIdx.x];
     const StepArgs& b = A.b;
@@ -580,58 +549,59 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A)
                 F.load(A, hd.faceStart + lf);
                 Eq32<D, H> eq;
                 eq_face<D, H>(eq, A, F.r.a);
-                float xs[NPL];
+                float2 xs[NP];
 #pragma unroll
-                for (int j = 0; j < NPL; ++j) {
-                    xs[j] = fmaf(L.y[j], F.Sy, L.x[j] * F.Sx);
-                    if (D == 3) xs[j] = fmaf(L.z[j], F.Sz, xs[j]);
-                }
-                float gf[NPL], hf[NPL], gw[D][NPL], hw[D][NPL];
+                for (int p = 0; p < NP; ++p) xs[p] = F.xs<D, NPL>(L, p);
+                float2 gf[NP], hf[NP], gw[D][NP], hw[D][NP];
                 if (F.r.w >= 0) {
                     recon32<D, H, NPL, true>(A, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
                     const float rws = A.rhoWs[F.r.w], hwf = A.wall4[F.r.w].x;
-                    float mw[NPL];
-                    ldv<NPL>(mw, A.Mw + (size_t)F.r.w * Vp + v0 + col);
+                    float2 mw[NP];
+                    ldp<NP>(mw, A.Mw + (size_t)F.r.w * Vp + v0 + col);
 #pragma unroll
-                    for (int j = 0; j < NPL; ++j) {
-                        if (xs[j] > 0.0f) {
-                            eq.relax(L.x[j], L.y[j], L.z[j], L.mr[j], gf[j], hf[j]);
-                        } else {  // incoming: rho_w Mw (deviation), not relaxed
-                            const float gi = rws * mw[j];
-                            gf[j] = gi - L.mr[j];
-                            if (H) hf[j] = gi * hwf - L.mr[j] * A.hrefFac;
-                        }
+                    for (int p = 0; p < NP; ++p) {
+                        float2 go = gf[p], ho = H ? hf[p] : f2(0.f);
+                        eq.relax(L, p, go, ho);                       // outgoing: relaxed
+                        const float2 gi = mul2(f2(rws), mw[p]);       // incoming: rho_w Mw, not relaxed
+                        const float2 gin = sub2(gi, L.mr[p]);
+                        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
+                        gf[p] = sel2(o0, o1, go, gin);
+                        if (H) hf[p] = sel2(o0, o1, ho, sub2(mul2(gi, f2(hwf)), mul2(L.mr[p], f2(A.hrefFac))));
                     }
                 } else {
                     recon32<D, H, NPL, false>(A, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
 #pragma unroll
-                    for (int j = 0; j < NPL; ++j) eq.relax(L.x[j], L.y[j], L.z[j], L.mr[j], gf[j], hf[j]);
+                    for (int p = 0; p < NP; ++p) {
+                        if (!H) hf[p] = f2(0.f);
+                        eq.relax(L, p, gf[p], hf[p]);
+                    }
                 }
                 const bool ownIn = F.r.ownL < hd.nT, neiIn = F.r.neiL >= 0 && F.r.neiL < hd.nT;
-                const float kO = A.dt * F.iVo, kN = A.dt * F.iVn;
                 if (ownIn) {
-                    float t[NPL], th[NPL];
-                    ldv<NPL>(t, sa + F.r.ownL * KC + col);
-                    if (H) ldv<NPL>(th, sah + F.r.ownL * KC + col);
+                    float2 t[NP], th[NP];
+                    ldp<NP>(t, sa + F.r.ownL * KC + col);
+                    if (H) ldp<NP>(th, sah + F.r.ownL * KC + col);
 #pragma unroll
-                    for (int j = 0; j < NPL; ++j) {
-                        t[j] = fmaf(-xs[j] * kO, gf[j], t[j]);
-                        if (H) th[j] = fmaf(-xs[j] * kO, hf[j], th[j]);
+                    for (int p = 0; p < NP; ++p) {
+                        const float2 kx = mul2(xs[p], f2(-A.dt * F.iVo));
+                        t[p] = fma2(kx, gf[p], t[p]);
+                        if (H) th[p] = fma2(kx, hf[p], th[p]);
                     }
-                    stv<NPL>(sa + F.r.ownL * KC + col, t);
-                    if (H) stv<NPL>(sah + F.r.ownL * KC + col, th);
+                    stp<NP>(sa + F.r.ownL * KC + col, t);
+                    if (H) stp<NP>(sah + F.r.ownL * KC + col, th);
                 }
                 if (neiIn) {
-                    float t[NPL], th[NPL];
-                    ldv<NPL>(t, sa + F.r.neiL * KC + col);
-                    if (H) ldv<NPL>(th, sah + F.r.neiL * KC + col);
+                    float2 t[NP], th[NP];
+                    ldp<NP>(t, sa + F.r.neiL * KC + col);
+                    if (H) ldp<NP>(th, sah + F.r.neiL * KC + col);
 #pragma unroll
-                    for (int j = 0; j < NPL; ++j) {
-                        t[j] = fmaf(xs[j] * kN, gf[j], t[j]);
-                        if (H) th[j] = fmaf(xs[j] * kN, hf[j], th[j]);
+                    for (int p = 0; p < NP; ++p) {
+                        const float2 kx = mul2(xs[p], f2(A.dt * F.iVn));
+                        t[p] = fma2(kx, gf[p], t[p]);
+                        if (H) th[p] = fma2(kx, hf[p], th[p]);
                     }
-                    stv<NPL>(sa + F.r.neiL * KC + col, t);
-                    if (H) stv<NPL>(sah + F.r.neiL * KC + col, th);
+                    stp<NP>(sa + F.r.neiL * KC + col, t);
+                    if (H) stp<NP>(sah + F.r.neiL * KC + col, th);
                 }
             }
             __syncthreads();
@@ -640,15 +610,15 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A)
             const int c = A.cells[hd.cellStart + lc];
             const float4 u4 = reinterpret_cast<const float4*>(A.cc + (size_t)c * kNCoef)[0];
             const float ur[3] = {u4.x, u4.y, u4.z};
-            float g[NPL], h[NPL];
-            ldv<NPL>(g, sa + lc * KC + col);
-            if (H) ldv<NPL>(h, sah + lc * KC + col);
+            float2 g[NP], h[NP];
+            ldp<NP>(g, sa + lc * KC + col);
+            if (H) ldp<NP>(h, sah + lc * KC + col);
             else
 #pragma unroll
-                for (int j = 0; j < NPL; ++j) h[j] = 0.0f;
+                for (int p = 0; p < NP; ++p) h[p] = f2(0.f);
             const size_t gi = (size_t)c * Vp + v0 + col;
-            stv_cs<NPL>(A.gTn + gi, g);
-            if (H) stv_cs<NPL>(A.hTn + gi, h);
+            stp_cs<NP>(A.gTn + gi, g);
+            if (H) stp_cs<NP>(A.hTn + gi, h);
             float m[NS];
 #pragma unroll
             for (int s = 0; s < NS; ++s) m[s] = 0.0f;

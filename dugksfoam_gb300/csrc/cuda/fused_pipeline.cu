@@ -10,7 +10,7 @@ int fused_npl(int precision) {
     if (precision == DUGKS_FP64) return 1;
     const char* e = std::getenv("DUGKS_NPL");
     const int npl = e ? std::atoi(e) : 4;
-    return (npl == 1 || npl == 2 || npl == 4) ? npl : 4;
+    return (npl == 2 || npl == 4) ? npl : 4;  // packed pairs: an even count per lane
 }
 
 int fused_dv_granule(int precision) { return 32 * fused_npl(precision); }

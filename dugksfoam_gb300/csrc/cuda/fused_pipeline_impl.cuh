@@ -277,8 +277,7 @@ private:
     void setD() {
         if constexpr (sizeof(S) == 4) {
             if (npl_ == 4) set<D, H, 4>();
-            else if (npl_ == 2) set<D, H, 2>();
-            else set<D, H, 1>();
+            else set<D, H, 2>();
         } else {
             set<D, H, 1>();
         }
