@@ -123,7 +123,9 @@ def make_case(args):
     from dugksfoam_gb300 import cases
 
     if args.workload == "delaunay2d":
-        return cases.delaunay2d(), "delaunay2d: ~100k Delaunay triangles (seed 0), 32x32 DV, Kn 0.01"
+        case = cases.delaunay2d(n_interior=args.delaunay_interior, n_side=args.delaunay_side)
+        return case, (f"delaunay2d: Delaunay triangles from {args.delaunay_interior} interior + "
+                      f"4x{args.delaunay_side} boundary points (seed 0), 32x32 DV, Kn 0.01")
     if args.workload == "cavity2d":
         return cases.cavity2d(61, nxi=28), "cavity2d: 61x61 quads, 28x28 DV, Kn 0.075"
     if args.workload == "cavity3d":
@@ -279,7 +281,7 @@ def run_engine(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                      "alg_bytes_per_cell_dv": ALG_BYTES.get(dom, 16),
-                     "step_frac": 16 * value / world / 1e9 / peak},
+                     "step_frac": sum(ALG_BYTES.values()) * value / world / 1e9 / peak},
         "kernels_ms": prof,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8, "d2h_bytes_per_step": d2h},
         "gpu_launches": s.launches_per_step() * args.steps,
@@ -300,6 +302,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="delaunay2d", choices=["delaunay2d", "cavity2d", "cavity3d"])
+    ap.add_argument("--delaunay-interior", type=int, default=49200,
+                    help="interior points of the delaunay2d mesh (49200 -> ~100k triangles)")
+    ap.add_argument("--delaunay-side", type=int, default=400, help="points per side of the delaunay2d boundary")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

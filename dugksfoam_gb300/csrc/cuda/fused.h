@@ -35,6 +35,8 @@ public:
 
 // DVs per lane of the fused kernels for a precision (FP32: DUGKS_NPL, default 4).
 int fused_npl(int precision);
+// Resident tiles per SM for the FP32 sweeps (DUGKS_CTAS = 1 or 2).
+int fused_ctas_per_sm();
 // DV chunk granularity the fused kernels need (the padded DV count must be a multiple).
 int fused_dv_granule(int precision);
 

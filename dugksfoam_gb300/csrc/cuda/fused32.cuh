@@ -71,6 +71,80 @@ __device__ __forceinline__ void stp_cs(float* p, const float2 (&d)[NP]) {
     else __stcs(reinterpret_cast<float2*>(p), d[0]);
 }
 
+// Per-tile metadata block (int4 units), staged into shared memory once per tile:
+//   [nFB][5]  face record {ownL, neiL, a, w} {stO0, stO1, stN0, stN1} (stencil
+//             ranges relative to the tile's first entry) and geometry
+//             {S, 1/Vo} {dO, 1/Vn} {dN or wall normal}
+//   [nEnt]    stencil entries {Lx, Ly, Lz, other}
+//   cells (nT2), colour order (nFB), colour offsets (nColors + 1), as ints
+//   padded to whole int4.  The bound allows the planner's 64 colours.
+__host__ __device__ constexpr int tile_meta32_bound(int nFB, int nEnt, int nT2) {
+    return 5 * nFB + nEnt + (nT2 + 3) / 4 + (nFB + 3) / 4 + 17;
+}
+
+// Shared memory of the FP32 sweeps (all offsets multiples of 16 bytes):
+//   sweep A: rows(T u H1 u H2) | face moments | metadata | face Uref | cell equilibria
+//   sweep B: rows(T u H1 u H2) | rows(T) | cell moments | metadata | face equilibria | cell equilibria
+template <int D, bool H, int NPL>
+struct SmemLayout32 {
+    static constexpr int KC = 32 * NPL, NS = Slots<D, H>::NS;
+    __host__ __device__ static size_t rows(int n) { return (size_t)n * KC * sizeof(float) * (H ? 2 : 1); }
+    __host__ __device__ static size_t metaA(int nT2, int nFA) { return rows(nT2) + (size_t)nFA * NS * sizeof(Acc<float>); }
+    __host__ __device__ static size_t metaB(int nT2, int nT) {
+        return rows(nT2) + rows(nT) + (size_t)nT * NS * sizeof(Acc<float>);
+    }
+    static size_t face(const TileDims& d) {
+        return metaA(d.nT2, d.nFA) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 16 * (size_t)d.nFA +
+               48 * (size_t)d.nT2;
+    }
+    static size_t cell(const TileDims& d) {
+        return metaB(d.nT2, d.nT) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 48 * (size_t)d.nFB +
+               48 * (size_t)d.nT2;
+    }
+};
+
+struct TileMeta32 {
+    const int4* F;    // face records [nFB][5]
+    const float4* E;  // stencil entries
+    const int* C;     // local -> global cell
+    const int* P;     // faces in colour order
+    const int* O;     // colour offsets
+    float4* dyn;      // per-step tables after the block
+};
+
+// Copy the tile's block into shared memory (caller synchronises).
+template <int NT>
+__device__ __forceinline__ TileMeta32 stage_meta(const FusedArgs<float>& A, const TileHdr& hd, unsigned char* at) {
+    int4* sm = reinterpret_cast<int4*>(at);
+    const int o0 = A.metaOff[blockIdx.x], n16 = A.metaOff[blockIdx.x + 1] - o0;
+    const int4* gm = A.meta + o0;
+    for (int i = threadIdx.x; i < n16; i += NT) sm[i] = __ldg(gm + i);
+    TileMeta32 m;
+    m.F = sm;
+    m.E = reinterpret_cast<const float4*>(sm + 5 * hd.nFB);
+    m.C = reinterpret_cast<const int*>(sm + 5 * hd.nFB + hd.nEnt);
+    m.P = reinterpret_cast<const int*>(sm + 5 * hd.nFB + hd.nEnt + (hd.nT2 + 3) / 4);
+    m.O = m.P + 4 * ((hd.nFB + 3) / 4);
+    m.dyn = reinterpret_cast<float4*>(sm + tile_meta32_bound(hd.nFB, hd.nEnt, hd.nT2));
+    return m;
+}
+
+// Equilibrium table entry {U, kexp} {1/RT, q'} {a, a A, RT, 0} from a
+// coefficient block and the relaxation weight a.
+__device__ __forceinline__ void eq_table(float4* q, const float* blk, float a) {
+    const float4* b = reinterpret_cast<const float4*>(blk);
+    const float4 b2 = b[2];
+    q[0] = b[0];
+    q[1] = b[1];
+    q[2] = make_float4(a, a * b2.x, b2.y, 0.0f);
+}
+// cell weight 1.5dt/(2tau+dt), face weight h/(2tau+h) with h = dt/2
+__device__ __forceinline__ float cell_weight(float dt, const float* blk) { return 1.5f * dt / (2.0f * blk[10] + dt); }
+__device__ __forceinline__ float face_weight(float dt, const float* blk) {
+    const float hh = 0.5f * dt;
+    return hh / (2.0f * blk[10] + hh);
+}
+
 // DV constants of this lane's NPL consecutive velocities in the current chunk.
 template <int D, int NPL>
 struct Lane32 {
@@ -93,15 +167,13 @@ struct Lane32 {
 template <int D, bool H>
 struct Eq32 {
     float ux, uy, uz, kexp, invRT, qx, qy, qz, a, aA, RT, KD, K2, hf;
-    __device__ __forceinline__ void load(const float* blk, float aw, int K, float hrefFac) {
-        const float4 b0 = reinterpret_cast<const float4*>(blk)[0];
-        const float4 b1 = reinterpret_cast<const float4*>(blk)[1];
-        const float4 b2 = reinterpret_cast<const float4*>(blk)[2];
+    __device__ __forceinline__ void load(const float4* q, int K, float hrefFac) {  // an eq_table entry
+        const float4 b0 = q[0], b1 = q[1], b2 = q[2];
         ux = b0.x; uy = b0.y; uz = b0.z; kexp = b0.w;
         invRT = b1.x; qx = b1.y; qy = b1.z; qz = b1.w;
-        RT = b2.y;
-        a = aw;
-        aA = aw * b2.x;
+        a = b2.x;
+        aA = b2.y;
+        RT = b2.z;
         KD = (float)(K + 3 - D);
         K2 = -2.0f * (float)K;
         hf = hrefFac;
@@ -130,17 +202,6 @@ struct Eq32 {
     }
 };
 
-template <int D, bool H>
-__device__ __forceinline__ void eq_cell(Eq32<D, H>& e, const FusedArgs<float>& A, int c) {
-    const float* blk = A.cc + (size_t)c * kNCoef;
-    e.load(blk, 1.5f * A.dt / (2.0f * blk[10] + A.dt), A.b.K, A.hrefFac);
-}
-template <int D, bool H>
-__device__ __forceinline__ void eq_face(Eq32<D, H>& e, const FusedArgs<float>& A, int a) {
-    const float* blk = A.fc + (size_t)a * kNCoef;
-    const float hh = 0.5f * A.dt;
-    e.load(blk, hh / (2.0f * blk[10] + hh), A.b.K, A.hrefFac);
-}
 
 // gbar+ rows of T u H1 u H2 (and for sweep B the g~new partial of T's rows).
 // Two rows per warp iteration keep two row loads in flight.
@@ -171,15 +232,16 @@ __device__ __forceinline__ void row32(const TileHdr& hd, const Lane32<D, NPL>& L
 }
 
 template <int D, bool H, int NPL, int NW, bool PART>
-__device__ __forceinline__ void rows32(const FusedArgs<float>& A, const TileHdr& hd, const Lane32<D, NPL>& L, int v0,
-                                       int lane, int warp, float* sg, float* sh, float* sa, float* sah) {
+__device__ __forceinline__ void rows32(const FusedArgs<float>& A, const TileHdr& hd, const TileMeta32& tm,
+                                       const float4* ceq, const Lane32<D, NPL>& L, int v0, int lane, int warp,
+                                       float* sg, float* sh, float* sa, float* sah) {
     constexpr int NP = NPL / 2;
     const int Vp = A.b.Vp;
     for (int l0 = warp; l0 < hd.nT2; l0 += 2 * NW) {
         const int l1 = l0 + NW;
         const bool two = l1 < hd.nT2;
-        const int c0 = A.cells[hd.cellStart + l0];
-        const int c1 = two ? A.cells[hd.cellStart + l1] : c0;
+        const int c0 = tm.C[l0];
+        const int c1 = two ? tm.C[l1] : c0;
         const size_t i0 = (size_t)c0 * Vp + v0 + lane * NPL, i1 = (size_t)c1 * Vp + v0 + lane * NPL;
         float2 ga[NP], ha[NP], gb[NP], hb[NP];
         ldp_cs<NP>(ga, A.gT + i0);
@@ -189,8 +251,8 @@ __device__ __forceinline__ void rows32(const FusedArgs<float>& A, const TileHdr&
             ldp_cs<NP>(hb, A.hT + i1);
         }
         Eq32<D, H> e0, e1;
-        eq_cell<D, H>(e0, A, c0);
-        eq_cell<D, H>(e1, A, c1);
+        e0.load(ceq + 3 * l0, A.b.K, A.hrefFac);
+        e1.load(ceq + 3 * (two ? l1 : l0), A.b.K, A.hrefFac);
         row32<D, H, NPL, PART>(hd, L, l0, ga, ha, e0, lane, sg, sh, sa, sah);
         if (two) row32<D, H, NPL, PART>(hd, L, l1, gb, hb, e1, lane, sg, sh, sa, sah);
     }
@@ -200,12 +262,12 @@ __device__ __forceinline__ void rows32(const FusedArgs<float>& A, const TileHdr&
 struct Face32 {
     TileFace r;
     float Sx, Sy, Sz, iVo, dOx, dOy, dOz, iVn, dNx, dNy, dNz;
-    __device__ __forceinline__ void load(const FusedArgs<float>& A, int rec) {
-        const int4* p = reinterpret_cast<const int4*>(A.faces + rec);
+    __device__ __forceinline__ void load(const int4* p) {  // a staged face record
         const int4 a = p[0], b = p[1];
         r.ownL = a.x; r.neiL = a.y; r.a = a.z; r.w = a.w;
         r.stO0 = b.x; r.stO1 = b.y; r.stN0 = b.z; r.stN1 = b.w;
-        const float4 g0 = A.fg4[3 * (size_t)rec], g1 = A.fg4[3 * (size_t)rec + 1], g2 = A.fg4[3 * (size_t)rec + 2];
+        const float4* g = reinterpret_cast<const float4*>(p + 2);
+        const float4 g0 = g[0], g1 = g[1], g2 = g[2];
         Sx = g0.x; Sy = g0.y; Sz = g0.z; iVo = g0.w;
         dOx = g1.x; dOy = g1.y; dOz = g1.z; iVn = g1.w;
         dNx = g2.x; dNy = g2.y; dNz = g2.z;
@@ -222,13 +284,13 @@ struct Face32 {
 //   acc += beta (phi_o - phi_u),  beta = L.(d_u - xi dt/2),
 // with the neighbour row (or the lagged wall gradient) read for all pairs.
 template <int D, bool H, int NP, bool GRAD>
-__device__ __forceinline__ void side_entry(const FusedArgs<float>& A, int e, float dx, float dy, float dz,
+__device__ __forceinline__ void side_entry(const FusedArgs<float>& A, const float4* E, int e, float dx, float dy, float dz,
                                            const float2 (&cu)[NP], const float2 (&hu)[NP], const float* sg,
                                            const float* sh, int col, int v0, const float2* xx, const float2* xy,
                                            const float2* xz, float2 (&acc)[NP], float2 (&acch)[NP],
                                            float2 (&gw)[D][NP], float2 (&hw)[D][NP]) {
     constexpr int KC = 64 * NP;
-    const float4 ent = A.st4[e];
+    const float4 ent = E[e];
     const int o = __float_as_int(ent.w);
     const float hdt = -0.5f * A.dt;
     float al = fmaf(ent.y, dy, ent.x * dx);
@@ -280,7 +342,7 @@ __device__ __forceinline__ void side_entry(const FusedArgs<float>& A, int e, flo
 // neighbour side when xi.S < 0 and their average when xi.S == 0.  Walls have
 // only the owner side; there the owner gradient itself is also returned.
 template <int D, bool H, int NPL, bool WALL>
-__device__ __forceinline__ void recon32(const FusedArgs<float>& A, const Face32& F, const Lane32<D, NPL>& L,
+__device__ __forceinline__ void recon32(const FusedArgs<float>& A, const float4* E, const Face32& F, const Lane32<D, NPL>& L,
                                         const float* sg, const float* sh, int lane, int v0, const float2* xs,
                                         float2 (&gf)[NPL / 2], float2 (&hf)[NPL / 2], float2 (&gw)[D][NPL / 2],
                                         float2 (&hw)[D][NPL / 2]) {
@@ -298,7 +360,7 @@ __device__ __forceinline__ void recon32(const FusedArgs<float>& A, const Face32&
         for (int k = 0; k < D; ++k) { gw[k][p] = f2(0.f); hw[k][p] = f2(0.f); }
     }
     for (int e = F.r.stO0; e < F.r.stO1; ++e)
-        side_entry<D, H, NP, WALL>(A, e, F.dOx, F.dOy, F.dOz, cO, hO, sg, sh, col, v0, L.x, L.y, L.z, aO, ahO, gw, hw);
+        side_entry<D, H, NP, WALL>(A, E, e, F.dOx, F.dOy, F.dOz, cO, hO, sg, sh, col, v0, L.x, L.y, L.z, aO, ahO, gw, hw);
     if (WALL) {
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
@@ -311,7 +373,7 @@ __device__ __forceinline__ void recon32(const FusedArgs<float>& A, const Face32&
     if (H) ldp<NP>(hN, sh + F.r.neiL * KC + col);
     float2 dw[D][NP], dhw[D][NP];
     for (int e = F.r.stN0; e < F.r.stN1; ++e)
-        side_entry<D, H, NP, false>(A, e, F.dNx, F.dNy, F.dNz, cN, hN, sg, sh, col, v0, L.x, L.y, L.z, aN, ahN, dw, dhw);
+        side_entry<D, H, NP, false>(A, E, e, F.dNx, F.dNy, F.dNz, cN, hN, sg, sh, col, v0, L.x, L.y, L.z, aN, ahN, dw, dhw);
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
         const float2 go = add2(cO[p], aO[p]), gn = add2(cN[p], aN[p]);
@@ -392,7 +454,7 @@ __device__ __forceinline__ void ref_moments_about(const double* R, const double*
 
 // ---------------------------------------------------------------- sweep A
 template <int D, bool H, int NPL, int NW>
-__global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A) {
+__global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<float> A) {
     using SL = Slots<D, H>;
     constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -400,11 +462,20 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A)
     const StepArgs& b = A.b;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Vp = b.Vp;
-    const size_t rowBytes = (size_t)hd.nT2 * KC * sizeof(float) * (H ? 2 : 1);
+    using LY = SmemLayout32<D, H, NPL>;
     float* sg = reinterpret_cast<float*>(smem);
     float* sh = sg + (size_t)hd.nT2 * KC;
-    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + ((rowBytes + 15) & ~size_t(15)));
+    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + LY::rows(hd.nT2));
     for (int i = threadIdx.x; i < hd.nFA * NS; i += NW * 32) mom[i].zero();
+    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::metaA(hd.nT2, hd.nFA));
+    float4* sU = tm.dyn;             // [nFA] face Uref
+    float4* ceq = tm.dyn + hd.nFA;   // [nT2][3] cell equilibria
+    __syncthreads();
+    for (int i = threadIdx.x; i < hd.nFA; i += NW * 32) sU[i] = A.uref4[tm.F[5 * i].z];
+    for (int i = threadIdx.x; i < hd.nT2; i += NW * 32) {
+        const float* blk = A.cc + (size_t)tm.C[i] * kNCoef;
+        eq_table(ceq + 3 * i, blk, cell_weight(A.dt, blk));
+    }
     const int nChunks = Vp / KC;
     const int myslot = slot_of<NS>(lane);
     const bool writer = NS == 16 ? (lane & 1) == 0 : true;
@@ -414,12 +485,12 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A)
         Lane32<D, NPL> L;
         L.load(A, v0, lane);
         __syncthreads();
-        rows32<D, H, NPL, NW, false>(A, hd, L, v0, lane, warp, sg, sh, nullptr, nullptr);
+        rows32<D, H, NPL, NW, false>(A, hd, tm, ceq, L, v0, lane, warp, sg, sh, nullptr, nullptr);
         __syncthreads();
         for (int lf = warp; lf < hd.nFA; lf += NW) {
             Face32 F;
-            F.load(A, hd.faceStart + lf);
-            const float4 u4 = A.uref4[F.r.a];
+            F.load(tm.F + 5 * lf);
+            const float4 u4 = sU[lf];
             const float ur[3] = {u4.x, u4.y, u4.z};
             float2 xs[NP];
 #pragma unroll
@@ -429,7 +500,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A)
 #pragma unroll
             for (int s = 0; s < NS; ++s) m[s] = 0.0f;
             if (F.r.w >= 0) {
-                recon32<D, H, NPL, true>(A, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
+                recon32<D, H, NPL, true>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
                 float2 gn[NP], hn[NP], use[NP];
                 float fl = 0.0f;
 #pragma unroll
@@ -450,7 +521,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A)
                 if (H) stp<NP>(A.Gbhn + wi, hn);
                 mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
             } else {
-                recon32<D, H, NPL, false>(A, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
+                recon32<D, H, NPL, false>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
                 mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
             }
             const float tot = reduce_scatter<NS, float>(m, lane);
@@ -460,8 +531,9 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A)
     __syncthreads();
     // ---- finalize owned faces (FP64)
     for (int lf = threadIdx.x; lf < hd.nFA; lf += NW * 32) {
-        const TileFace r = A.faces[hd.faceStart + lf];
-        const float4 u4 = A.uref4[r.a];
+        const int4 rr = tm.F[5 * lf];
+        struct { int a, w; } r = {rr.z, rr.w};
+        const float4 u4 = sU[lf];
         const double ur[3] = {u4.x, u4.y, u4.z};
         double M[NS], Rm[NS];
         for (int s = 0; s < NS; ++s) M[s] = mom[lf * NS + s].value();
@@ -513,7 +585,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_face32(FusedArgs<float> A)
 
 // ---------------------------------------------------------------- sweep B
 template <int D, bool H, int NPL, int NW>
-__global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A) {
+__global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_cell32(FusedArgs<float> A) {
     using SL = Slots<D, H>;
     constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
     extern __shared__ __align__(16) unsigned char smem[];
@@ -521,14 +593,25 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A)
     const StepArgs& b = A.b;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Vp = b.Vp;
-    const size_t rb2 = ((size_t)hd.nT2 * KC * sizeof(float) * (H ? 2 : 1) + 15) & ~size_t(15);
-    const size_t rb1 = ((size_t)hd.nT * KC * sizeof(float) * (H ? 2 : 1) + 15) & ~size_t(15);
+    using LY = SmemLayout32<D, H, NPL>;
     float* sg = reinterpret_cast<float*>(smem);
     float* sh = sg + (size_t)hd.nT2 * KC;
-    float* sa = reinterpret_cast<float*>(smem + rb2);
+    float* sa = reinterpret_cast<float*>(smem + LY::rows(hd.nT2));
     float* sah = sa + (size_t)hd.nT * KC;
-    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + rb2 + rb1);
+    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + LY::rows(hd.nT2) + LY::rows(hd.nT));
     for (int i = threadIdx.x; i < hd.nT * NS; i += NW * 32) mom[i].zero();
+    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::metaB(hd.nT2, hd.nT));
+    float4* feq = tm.dyn;                // [nFB][3] face equilibria
+    float4* ceq = tm.dyn + 3 * hd.nFB;   // [nT2][3] cell equilibria
+    __syncthreads();
+    for (int i = threadIdx.x; i < hd.nFB; i += NW * 32) {
+        const float* blk = A.fc + (size_t)tm.F[5 * i].z * kNCoef;
+        eq_table(feq + 3 * i, blk, face_weight(A.dt, blk));
+    }
+    for (int i = threadIdx.x; i < hd.nT2; i += NW * 32) {
+        const float* blk = A.cc + (size_t)tm.C[i] * kNCoef;
+        eq_table(ceq + 3 * i, blk, cell_weight(A.dt, blk));
+    }
     const int nChunks = Vp / KC;
     const int myslot = slot_of<NS>(lane);
     const bool writer = NS == 16 ? (lane & 1) == 0 : true;
@@ -539,22 +622,22 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A)
         Lane32<D, NPL> L;
         L.load(A, v0, lane);
         __syncthreads();
-        rows32<D, H, NPL, NW, true>(A, hd, L, v0, lane, warp, sg, sh, sa, sah);
+        rows32<D, H, NPL, NW, true>(A, hd, tm, ceq, L, v0, lane, warp, sg, sh, sa, sah);
         __syncthreads();
         for (int ci = 0; ci < hd.nColors; ++ci) {
-            const int k0 = A.colorOff[hd.colStart + ci], k1 = A.colorOff[hd.colStart + ci + 1];
+            const int k0 = tm.O[ci], k1 = tm.O[ci + 1];
             for (int k = k0 + warp; k < k1; k += NW) {
-                const int lf = A.colorPerm[hd.permStart + k];
+                const int lf = tm.P[k];
                 Face32 F;
-                F.load(A, hd.faceStart + lf);
+                F.load(tm.F + 5 * lf);
                 Eq32<D, H> eq;
-                eq_face<D, H>(eq, A, F.r.a);
+                eq.load(feq + 3 * lf, A.b.K, A.hrefFac);
                 float2 xs[NP];
 #pragma unroll
                 for (int p = 0; p < NP; ++p) xs[p] = F.xs<D, NPL>(L, p);
                 float2 gf[NP], hf[NP], gw[D][NP], hw[D][NP];
                 if (F.r.w >= 0) {
-                    recon32<D, H, NPL, true>(A, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
+                    recon32<D, H, NPL, true>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
                     const float rws = A.rhoWs[F.r.w], hwf = A.wall4[F.r.w].x;
                     float2 mw[NP];
                     ldp<NP>(mw, A.Mw + (size_t)F.r.w * Vp + v0 + col);
@@ -569,7 +652,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A)
                         if (H) hf[p] = sel2(o0, o1, ho, sub2(mul2(gi, f2(hwf)), mul2(L.mr[p], f2(A.hrefFac))));
                     }
                 } else {
-                    recon32<D, H, NPL, false>(A, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
+                    recon32<D, H, NPL, false>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
 #pragma unroll
                     for (int p = 0; p < NP; ++p) {
                         if (!H) hf[p] = f2(0.f);
@@ -607,8 +690,8 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A)
             __syncthreads();
         }
         for (int lc = warp; lc < hd.nT; lc += NW) {
-            const int c = A.cells[hd.cellStart + lc];
-            const float4 u4 = reinterpret_cast<const float4*>(A.cc + (size_t)c * kNCoef)[0];
+            const int c = tm.C[lc];
+            const float4 u4 = ceq[3 * lc];
             const float ur[3] = {u4.x, u4.y, u4.z};
             float2 g[NP], h[NP];
             ldp<NP>(g, sa + lc * KC + col);
@@ -630,9 +713,9 @@ __global__ void __launch_bounds__(NW * 32, 1) k_sweep_cell32(FusedArgs<float> A)
     __syncthreads();
     // ---- finalize cells of T (FP64)
     for (int lc = threadIdx.x; lc < hd.nT; lc += NW * 32) {
-        const int c = A.cells[hd.cellStart + lc];
-        const float* blk = A.cc + (size_t)c * kNCoef;
-        const double ur[3] = {blk[0], blk[1], blk[2]};
+        const int c = tm.C[lc];
+        const float4 u4 = ceq[3 * lc];
+        const double ur[3] = {u4.x, u4.y, u4.z};
         double M[NS], Rm[NS];
         for (int s = 0; s < NS; ++s) M[s] = mom[lc * NS + s].value();
         ref_moments_about<D, H>(A.refMom, ur, Rm);

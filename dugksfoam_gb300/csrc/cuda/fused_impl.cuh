@@ -86,6 +86,10 @@ struct FusedArgs {
     float hrefFac;              // R T0 (K+3-D)
     const double* refMom;       // [NS] raw moments of Mref (scaled)
     const double* wallRefOut;   // [nW][NS] Mref moments over outgoing DVs about U_w (+ flux)
+    // FP32: per-tile metadata blocks staged into shared memory (int4 units;
+    // layout in tile_meta32_layout), tile t at meta + metaOff[t]
+    const int4* meta;
+    const int* metaOff;
     // macros of the next step
     double *rhoN, *UN, *TN, *qN, *tauN;
     double gscale, invGscale;

@@ -11,11 +11,9 @@ struct SmemLayout {
     static constexpr int NS = Slots<D, H>::NS;
     __host__ __device__ static size_t rows(int n) { return (size_t)n * KC * sizeof(S) * (H ? 2 : 1); }
     __host__ __device__ static size_t align(size_t x) { return (x + 15) & ~size_t(15); }
-    __host__ __device__ static size_t face(int nT2, int nFA) {
-        return align(rows(nT2)) + (size_t)nFA * NS * sizeof(Acc<S>);
-    }
-    __host__ __device__ static size_t cell(int nT2, int nT) {
-        return align(rows(nT2)) + align(rows(nT)) + (size_t)nT * NS * sizeof(Acc<S>);
+    static size_t face(const TileDims& d) { return align(rows(d.nT2)) + (size_t)d.nFA * NS * sizeof(Acc<S>); }
+    static size_t cell(const TileDims& d) {
+        return align(rows(d.nT2)) + align(rows(d.nT)) + (size_t)d.nT * NS * sizeof(Acc<S>);
     }
 };
 

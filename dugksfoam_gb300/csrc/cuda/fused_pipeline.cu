@@ -13,6 +13,12 @@ int fused_npl(int precision) {
     return (npl == 2 || npl == 4) ? npl : 4;  // packed pairs: an even count per lane
 }
 
+int fused_ctas_per_sm() {
+    const char* e = std::getenv("DUGKS_CTAS");
+    const int c = e ? std::atoi(e) : 1;
+    return c == 2 ? 2 : 1;
+}
+
 int fused_dv_granule(int precision) { return 32 * fused_npl(precision); }
 
 std::unique_ptr<FusedPipeline> make_fused_pipeline(Solver& s, const StepArgs& a, int precision, std::string& err) {

@@ -30,25 +30,28 @@ public:
         H_ = a.hasH != 0;
         if (D_ != 2 && D_ != 3) { err = "fused pipeline supports 2D and 3D meshes"; return false; }
         npl_ = fused_npl(sizeof(S) == 4 ? DUGKS_FP32_FP64MOM : DUGKS_FP64);
+        ctas_ = sizeof(S) == 4 ? fused_ctas_per_sm() : 1;
         const int KC = 32 * npl_;
         if (a.Vp % KC != 0) { err = "padded DV count is not a multiple of the DV chunk"; return false; }
         pick();
         // ---- tile plan, sized to the shared-memory budget
         int dev = 0;
         cudaGetDevice(&dev);
-        int maxSmem = 0;
+        int maxSmem = 0, smemSM = 0;
         cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        const size_t budget = (size_t)maxSmem - 2048;
+        cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+        // ctas_ resident tiles per SM share its shared memory (1 KB per block is reserved)
+        const size_t budget = std::min((size_t)maxSmem, (size_t)smemSM / ctas_ - 1024) - 1024;
         const char* envT = std::getenv("DUGKS_TILE_CELLS");
         const int maxCells = envT ? std::max(1, std::atoi(envT)) : 4096;
-        const SmemFn fn = [this](int nT, int nT2, int nFA) {
-            return std::max(smemFace(nT2, nFA), smemCell(nT2, nT));
-        };
+        const SmemFn fn = [this](const TileDims& d) { return std::max(smemFace(d), smemCell(d)); };
         if (!build_tile_plan(m, maxCells, fn, budget, plan_, err)) return false;
         smemA_ = smemB_ = 0;
         for (const TileHdr& h : plan_.hdr) {
-            smemA_ = std::max(smemA_, smemFace(h.nT2, h.nFA));
-            smemB_ = std::max(smemB_, smemCell(h.nT2, h.nT));
+            TileDims d;
+            d.nT = h.nT; d.nT1 = h.nT1; d.nT2 = h.nT2; d.nFA = h.nFA; d.nFB = h.nFB; d.nEnt = h.nEnt;
+            smemA_ = std::max(smemA_, smemFace(d));
+            smemB_ = std::max(smemB_, smemCell(d));
         }
         cudaFuncSetAttribute(kFace_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemA_);
         cudaFuncSetAttribute(kCell_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
@@ -87,6 +90,41 @@ public:
                 fg4[3 * k + 2] = make_float4((float)dN[0], (float)dN[1], (float)dN[2], 0.0f);
             }
             args_.fg4 = upload(fg4);
+            // per-tile blocks: face records (stencil ranges relative to the
+            // tile's first entry) + geometry, entries, cells, colour order
+            std::vector<int4> meta;
+            std::vector<int> metaOff;
+            auto ints = [&](const int32_t* v, int n) {
+                for (int i = 0; i < n; i += 4)
+                    meta.push_back(make_int4(v[i], i + 1 < n ? v[i + 1] : 0, i + 2 < n ? v[i + 2] : 0,
+                                             i + 3 < n ? v[i + 3] : 0));
+            };
+            auto f4i = [](float4 f) {
+                int4 r;
+                std::memcpy(&r, &f, 16);
+                return r;
+            };
+            for (const TileHdr& h : plan_.hdr) {
+                metaOff.push_back((int)meta.size());
+                const int base = plan_.stOff[h.stStart];
+                for (int k = 0; k < h.nFB; ++k) {
+                    const size_t rec = (size_t)h.faceStart + k;
+                    const TileFace& r = plan_.faces[rec];
+                    meta.push_back(make_int4(r.ownL, r.neiL, r.a, r.w));
+                    meta.push_back(make_int4(r.stO0 - base, r.stO1 - base, r.neiL >= 0 ? r.stN0 - base : 0,
+                                             r.neiL >= 0 ? r.stN1 - base : 0));
+                    for (int q = 0; q < 3; ++q) meta.push_back(f4i(fg4[3 * rec + q]));
+                }
+                for (int e = 0; e < h.nEnt; ++e) meta.push_back(f4i(st4[(size_t)base + e]));
+                ints(&plan_.cells[h.cellStart], h.nT2);
+                ints(&plan_.colorPerm[h.permStart], h.nFB);
+                ints(&plan_.colorOff[h.colStart], h.nColors + 1);
+                const int n16 = (int)meta.size() - metaOff.back();
+                if (n16 > tile_meta32_bound(h.nFB, h.nEnt, h.nT2)) { err = "tile metadata exceeds its bound"; return false; }
+            }
+            metaOff.push_back((int)meta.size());
+            args_.meta = upload(meta);
+            args_.metaOff = upload(metaOff);
             std::vector<float4> w4(std::max(a.nW, 1), make_float4(0, 0, 0, 0));
             std::vector<double> Tw(a.nW);
             if (a.nW) cudaMemcpy(Tw.data(), a.Tw, a.nW * 8, cudaMemcpyDeviceToHost);
@@ -193,8 +231,9 @@ public:
         A.Gbgn = Gg_[1 - cur_]; A.Gbhn = Gh_[1 - cur_];
         A.cc = cc_[cur_]; A.ccn = cc_[1 - cur_];
         A.rhoN = rhoN_; A.UN = UN_; A.TN = TN_; A.qN = qN_; A.tauN = tauN_;
-        if (k == 0) kFace_<<<plan_.nTiles, kNW * 32, smemA_, s>>>(A);
-        else kCell_<<<plan_.nTiles, kNW * 32, smemB_, s>>>(A);
+        const int threads = kWarpsPerSM / ctas_ * 32;
+        if (k == 0) kFace_<<<plan_.nTiles, threads, smemA_, s>>>(A);
+        else kCell_<<<plan_.nTiles, threads, smemB_, s>>>(A);
     }
 
     void endStep(StepArgs& base) override {
@@ -233,14 +272,14 @@ public:
     size_t bytes() const override { return bytes_; }
     std::string describe() const override {
         char buf[256];
-        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d smemA=%zu smemB=%zu",
+        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d ctas=%d smemA=%zu smemB=%zu",
                  plan_.nTiles, plan_.maxT, (double)plan_.sumT / std::max(1, plan_.nTiles),
-                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, smemA_, smemB_);
+                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, ctas_, smemA_, smemB_);
         return buf;
     }
 
 private:
-    static constexpr int kNW = 16;
+    static constexpr int kWarpsPerSM = 16;  // split over ctas_ resident tiles
 
     template <typename T>
     T* alloc(size_t n) {
@@ -262,16 +301,26 @@ private:
     template <int D, bool H, int NPL>
     void set() {
         if constexpr (sizeof(S) == 4) {
-            kFace_ = k_sweep_face32<D, H, NPL, kNW>;
-            kCell_ = k_sweep_cell32<D, H, NPL, kNW>;
+            if (ctas_ == 2) {
+                kFace_ = k_sweep_face32<D, H, NPL, kWarpsPerSM / 2>;
+                kCell_ = k_sweep_cell32<D, H, NPL, kWarpsPerSM / 2>;
+            } else {
+                kFace_ = k_sweep_face32<D, H, NPL, kWarpsPerSM>;
+                kCell_ = k_sweep_cell32<D, H, NPL, kWarpsPerSM>;
+            }
             kRef_ = k_ref_tables<D, H>;
         } else {
-            kFace_ = k_sweep_face<S, D, H, NPL, kNW>;
-            kCell_ = k_sweep_cell<S, D, H, NPL, kNW>;
+            kFace_ = k_sweep_face<S, D, H, NPL, kWarpsPerSM>;
+            kCell_ = k_sweep_cell<S, D, H, NPL, kWarpsPerSM>;
         }
         kTables_ = k_wall_tables<S, D, H>;
-        smemFaceFn_ = &SmemLayout<S, D, H, NPL>::face;
-        smemCellFn_ = &SmemLayout<S, D, H, NPL>::cell;
+        if constexpr (sizeof(S) == 4) {
+            smemFaceFn_ = &SmemLayout32<D, H, NPL>::face;
+            smemCellFn_ = &SmemLayout32<D, H, NPL>::cell;
+        } else {
+            smemFaceFn_ = &SmemLayout<S, D, H, NPL>::face;
+            smemCellFn_ = &SmemLayout<S, D, H, NPL>::cell;
+        }
     }
     template <int D, bool H>
     void setD() {
@@ -286,10 +335,10 @@ private:
         if (D_ == 2) { H_ ? setD<2, true>() : setD<2, false>(); }
         else { H_ ? setD<3, true>() : setD<3, false>(); }
     }
-    size_t smemFace(int nT2, int nFA) const { return smemFaceFn_(nT2, nFA); }
-    size_t smemCell(int nT2, int nT) const { return smemCellFn_(nT2, nT); }
+    size_t smemFace(const TileDims& d) const { return smemFaceFn_(d); }
+    size_t smemCell(const TileDims& d) const { return smemCellFn_(d); }
 
-    int D_ = 2, npl_ = 1;
+    int D_ = 2, npl_ = 1, ctas_ = 1;
     bool H_ = true;
     TilePlan plan_;
     FusedArgs<S> args_{};
@@ -300,8 +349,8 @@ private:
     double* refMom_ = nullptr;
     double* wallRefOut_ = nullptr;
     double T0_ = 273.0, hrefFac_ = 0.0;
-    size_t (*smemFaceFn_)(int, int) = nullptr;
-    size_t (*smemCellFn_)(int, int) = nullptr;
+    size_t (*smemFaceFn_)(const TileDims&) = nullptr;
+    size_t (*smemCellFn_)(const TileDims&) = nullptr;
     size_t smemA_ = 0, smemB_ = 0;
     S* gT_[2] = {nullptr, nullptr};
     S* hT_[2] = {nullptr, nullptr};

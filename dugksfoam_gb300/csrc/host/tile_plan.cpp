@@ -25,7 +25,8 @@ inline int other(const Mesh& m, int j) {  // neighbour across cell-face entry j 
 struct Sets {
     std::vector<int> mark;  // stamp*3 + {0,1,2}
     int stamp = 0;
-    int nT = 0, nT1 = 0, nT2 = 0, nFA = 0;
+    TileDims d;
+    int &nT = d.nT, &nT1 = d.nT1, &nT2 = d.nT2, &nFA = d.nFA, &nFB = d.nFB, &nEnt = d.nEnt;
     std::vector<int> lc;
     explicit Sets(int nC) : mark(nC, -1) {}
     bool in(int c) const { return mark[c] >= stamp * 3 && mark[c] <= stamp * 3 + 2; }
@@ -51,12 +52,16 @@ struct Sets {
         nT1 = (int)lc.size();
         ring(nT, nT1, 2);
         nT2 = (int)lc.size();
-        nFA = 0;
+        nFA = nFB = nEnt = 0;
         for (int i = 0; i < nT; ++i) {
             const int c = lc[i];
-            for (int j = m.cellOff[c]; j < m.cellOff[c + 1]; ++j)
-                if (m.cellFace[j] >= m.nI || m.cellSide[j] == 0) ++nFA;
+            for (int j = m.cellOff[c]; j < m.cellOff[c + 1]; ++j) {
+                const int f = m.cellFace[j];
+                if (f >= m.nI || m.cellSide[j] == 0) ++nFA, ++nFB;
+                else if (!inT(m.owner[f])) ++nFB;
+            }
         }
+        for (int i = 0; i < nT1; ++i) nEnt += m.cellOff[lc[i] + 1] - m.cellOff[lc[i]];
     }
 };
 
@@ -107,7 +112,7 @@ bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t
         partition(N);
         for (auto& pr : parts) {
             S.build(m, cells.data() + pr.first, pr.second - pr.first);
-            if (smem(S.nT, S.nT2, S.nFA) > budget) return false;
+            if (smem(S.d) > budget) return false;
         }
         return true;
     };
@@ -156,6 +161,7 @@ bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t
             }
         }
         p.stOff.push_back((int)p.stEnt.size());
+        h.nEnt = (int)p.stEnt.size() - p.stOff[h.stStart];
         // faces: owned first (internal with owner in T, then walls of T), then
         // internal faces with neighbour in T and owner outside T.
         std::vector<std::pair<int, int>> owned, extra;  // (global face order key, active face)

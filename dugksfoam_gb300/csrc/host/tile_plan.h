@@ -24,7 +24,7 @@ struct TileHdr {
     int32_t colStart;    // into colorPerm / colorOff
     int32_t nColors;
     int32_t permStart;   // into colorPerm (nFB entries, grouped by colour)
-    int32_t pad1;
+    int32_t nEnt;        // stencil entries of T u H1 (from stOff[stStart])
 };
 
 // Face record (device-visible POD).
@@ -50,8 +50,14 @@ struct TilePlan {
     std::vector<int32_t> colorPerm; // per tile nFB local face ids grouped by colour
 };
 
-// Shared-memory bytes a tile needs, from |T|, |T u H1 u H2| and its owned faces.
-using SmemFn = std::function<size_t(int nT, int nT2, int nFA)>;
+// Sizes of one tile: |T|, |T u H1|, |T u H1 u H2|, owned faces (sweep A),
+// faces of T's cells (sweep B) and stencil entries of T u H1.
+struct TileDims {
+    int nT = 0, nT1 = 0, nT2 = 0, nFA = 0, nFB = 0, nEnt = 0;
+};
+
+// Shared-memory bytes a tile needs.
+using SmemFn = std::function<size_t(const TileDims&)>;
 
 // Build the plan: compact BFS tiles of at most maxTileCells cells, each the
 // largest that fits `budget` bytes of shared memory.
