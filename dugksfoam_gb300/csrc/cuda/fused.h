@@ -37,6 +37,9 @@ public:
 int fused_npl(int precision);
 // Resident tiles per SM for the FP32 sweeps (DUGKS_CTAS = 1 or 2).
 int fused_ctas_per_sm();
+// FP32 sweep B in gather form (one warp per cell over stored face values;
+// DUGKS_CELL_SWEEP=tiled selects the tiled scatter form).
+bool fused_cell_gather();
 // DV chunk granularity the fused kernels need (the padded DV count must be a multiple).
 int fused_dv_granule(int precision);
 

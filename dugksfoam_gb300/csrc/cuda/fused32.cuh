@@ -524,6 +524,11 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<flo
                 recon32<D, H, NPL, false>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
                 mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
             }
+            if (A.gF) {
+                const size_t fi = (size_t)F.r.a * Vp + v0 + lane * NPL;
+                stp<NP>(A.gF + fi, gf);
+                if (H) stp<NP>(A.hF + fi, hf);
+            }
             const float tot = reduce_scatter<NS, float>(m, lane);
             if (writer && myslot <= SL::FLUX) mom[lf * NS + myslot].add(tot);
         }
@@ -558,6 +563,7 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<flo
         b.tauF[a] = tau;
         for (int k = 0; k < 3; ++k) { b.UF[3 * a + k] = U[k]; b.qF[3 * a + k] = q[k]; }
         write_coef<D>(A.fc + (size_t)a * kNCoef, rho, U, T, q, tau, b, A.gscale);
+        if (A.feqT) eq_table(A.feqT + 3 * (size_t)a, A.fc + (size_t)a * kNCoef, face_weight(A.dt, A.fc + (size_t)a * kNCoef));
         if (r.w < 0) A.uref4[a] = make_float4((float)U[0], (float)U[1], (float)U[2], 0.0f);
         if (r.w >= 0) {
             const int w = r.w;
@@ -737,6 +743,198 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_cell32(FusedArgs<flo
 // Reference Maxwellian per DV (scaled: exp(-|xi|^2/(2 R T0))), its raw moments
 // (scaled, about the origin) and, per wall face, the reference moments over
 // the outgoing velocities about U_w plus the reference outgoing flux.
+// ---------------------------------------------------------------- sweep B, gather form
+// Asynchronous global -> shared copies (each lane copies, and later reads,
+// only its own NPL floats of a row, so a lane's wait_group is all the
+// ordering it needs).
+__device__ __forceinline__ void cp_async_row(float* dst, const float* src, int npl) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    if (npl == 4) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Shared memory of the gather sweep: per warp two stages of (1 + MF) rows of
+// g (and h): the cell's g~ row and its first MF faces' stored values.
+__host__ __device__ inline size_t gather_smem(int nw, int mf, int kc, bool h) {
+    return (size_t)nw * 2 * (1 + mf) * (h ? 2 : 1) * kc * sizeof(float);
+}
+
+// Cell macros (FP64) from the deviation moment totals M (slots as Slots<D,H>).
+template <int D, bool H>
+__device__ __forceinline__ void finalize_cell32(const FusedArgs<float>& A, int c, const double* tot) {
+    using SL = Slots<D, H>;
+    constexpr int NS = SL::NS;
+    const StepArgs& b = A.b;
+    const float4 u4 = reinterpret_cast<const float4*>(A.cc + (size_t)c * kNCoef)[0];
+    const double ur[3] = {u4.x, u4.y, u4.z};
+    double M[NS], Rm[NS];
+    ref_moments_about<D, H>(A.refMom, ur, Rm);
+    for (int s = 0; s < SL::NM; ++s) M[s] = (tot[s] + Rm[s]) * A.invGscale;
+    double rho, U[3], T, tau, qr[3];
+    macros_from_moments<D, H>(M, ur, b, rho, U, T, tau, qr);
+    const double fac = 2.0 * tau / (2.0 * tau + b.dt * b.Pr);
+    double q[3] = {fac * qr[0], fac * qr[1], fac * qr[2]};
+    A.rhoN[c] = rho;
+    A.TN[c] = T;
+    A.tauN[c] = tau;
+    for (int k = 0; k < 3; ++k) { A.UN[3 * c + k] = U[k]; A.qN[3 * c + k] = q[k]; }
+    write_coef<D>(A.ccn + (size_t)c * kNCoef, rho, U, T, q, tau, b, A.gscale);
+    if (!(rho > 0.0) || !(T > 0.0) || !isfinite(U[0] + U[1] + U[2] + q[0] + q[1] + q[2])) atomicExch(b.status, 5);
+}
+
+// Cells per warp batch of the gather sweep's FP64 macro step (one lane per cell).
+constexpr int kGatherBatch = 8;
+
+// Warps stride over the cells (persistent grid); per cell, all DV chunks:
+//   g~new = g+ + (g+ - g~)/3 - dt/V sum_f (xi.S_f) g^f_f,
+// with g+ the cell relaxation of g~ (P1), g^f_f the face value stored by
+// sweep A relaxed toward the face equilibrium (P7; incoming wall DVs take
+// rho_w Mw unrelaxed) and the sum over the cell's faces in face order (P8),
+// then the cell moments (P9).  Faces are relaxed once from each side; no
+// tiles or block barriers.  The rows of chunk k+1 are copied into the warp's
+// other stage while chunk k is computed; the FP64 macros of a batch of cells
+// are finished together, one lane per cell.
+template <int D, bool H, int NPL, int NW>
+__global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A, int MF) {
+    using SL = Slots<D, H>;
+    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2, NR = H ? 2 : 1;
+    __shared__ double sM[NW][kGatherBatch][NS];
+    __shared__ int sC[NW][kGatherBatch];
+    extern __shared__ __align__(16) float gsm[];
+    const StepArgs& b = A.b;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int Vp = b.Vp, col = lane * NPL;
+    const int stageRows = (1 + MF) * NR;
+    float* wb = gsm + (size_t)warp * 2 * stageRows * KC + col;
+    const int myslot = slot_of<NS>(lane);
+    const bool writer = NS == 16 ? (lane & 1) == 0 : true;
+    const int TW = gridDim.x * NW;
+    int nb = 0;
+    for (int c = blockIdx.x * NW + warp; c < b.nC; c += TW) {
+        const int e0 = A.cfOff[c], e1 = A.cfOff[c + 1];
+        const int nfs = min(e1 - e0, MF);  // faces staged through shared memory
+        auto issue = [&](int stage, int v0) {
+            float* st = wb + (size_t)stage * stageRows * KC;
+            const size_t gi = (size_t)c * Vp + v0 + col;
+            cp_async_row(st, A.gT + gi, NPL);
+            if (H) cp_async_row(st + KC, A.hT + gi, NPL);
+            for (int f = 0; f < nfs; ++f) {
+                const int a = __float_as_int(A.cfEnt[e0 + f].w);
+                const size_t fi = (size_t)a * Vp + v0 + col;
+                cp_async_row(st + (1 + f) * NR * KC, A.gF + fi, NPL);
+                if (H) cp_async_row(st + ((1 + f) * NR + 1) * KC, A.hF + fi, NPL);
+            }
+            cp_async_commit();
+        };
+        const float* cblk = A.cc + (size_t)c * kNCoef;
+        Eq32<D, H> ec;
+        {
+            float4 q[3];
+            eq_table(q, cblk, cell_weight(A.dt, cblk));
+            ec.load(q, b.K, A.hrefFac);
+        }
+        const float4 u4 = reinterpret_cast<const float4*>(cblk)[0];
+        const float ur[3] = {u4.x, u4.y, u4.z};
+        const float kv = -A.dt * A.invVf[c];
+        Acc<float> acc;
+        acc.zero();
+        const int nChunks = Vp / KC;
+        issue(0, 0);
+        for (int ch = 0; ch < nChunks; ++ch) {
+            const int v0 = ch * KC;
+            if (ch + 1 < nChunks) {
+                issue((ch + 1) & 1, v0 + KC);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            const float* st = wb + (size_t)(ch & 1) * stageRows * KC;
+            Lane32<D, NPL> L;
+            L.load(A, v0, lane);
+            float2 g0[NP], h0[NP], t[NP], th[NP];
+            ldp<NP>(g0, st);
+            if (H) ldp<NP>(h0, st + KC);
+    #pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                float2 g = g0[p], h = H ? h0[p] : f2(0.f);
+                ec.relax(L, p, g, h);
+                t[p] = fma2(sub2(g, g0[p]), f2(1.0f / 3.0f), g);  // exact when g+ == g~
+                th[p] = H ? fma2(sub2(h, h0[p]), f2(1.0f / 3.0f), h) : f2(0.f);
+            }
+            for (int e = e0; e < e1; ++e) {
+                const int f = e - e0;
+                const float4 ent = A.cfEnt[e];
+                const int a = __float_as_int(ent.w);
+                float2 gf[NP], hf[NP];
+                if (f < nfs) {
+                    ldp<NP>(gf, st + (1 + f) * NR * KC);
+                    if (H) ldp<NP>(hf, st + ((1 + f) * NR + 1) * KC);
+                } else {
+                    const size_t fi = (size_t)a * Vp + v0 + col;
+                    ldp<NP>(gf, A.gF + fi);
+                    if (H) ldp<NP>(hf, A.hF + fi);
+                }
+                if (!H)
+    #pragma unroll
+                    for (int p = 0; p < NP; ++p) hf[p] = f2(0.f);
+                Eq32<D, H> eq;
+                eq.load(A.feqT + 3 * (size_t)a, b.K, A.hrefFac);
+                float2 xs[NP];
+    #pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    xs[p] = fma2(L.y[p], f2(ent.y), mul2(L.x[p], f2(ent.x)));
+                    if (D == 3) xs[p] = fma2(L.z[p], f2(ent.z), xs[p]);
+                }
+                if (a >= b.nI) {  // wall: the cell is the owner; outgoing where xi.S > 0
+                    const int w = a - b.nI;
+                    const float rws = A.rhoWs[w], hwf = A.wall4[w].x;
+                    float2 mw[NP];
+                    ldp<NP>(mw, A.Mw + (size_t)w * Vp + v0 + col);
+    #pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        float2 go = gf[p], ho = hf[p];
+                        eq.relax(L, p, go, ho);
+                        const float2 gw = mul2(f2(rws), mw[p]);
+                        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
+                        gf[p] = sel2(o0, o1, go, sub2(gw, L.mr[p]));
+                        if (H) hf[p] = sel2(o0, o1, ho, sub2(mul2(gw, f2(hwf)), mul2(L.mr[p], f2(A.hrefFac))));
+                    }
+                } else {
+    #pragma unroll
+                    for (int p = 0; p < NP; ++p) eq.relax(L, p, gf[p], hf[p]);
+                }
+    #pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    const float2 kx = mul2(xs[p], f2(kv));
+                    t[p] = fma2(kx, gf[p], t[p]);
+                    if (H) th[p] = fma2(kx, hf[p], th[p]);
+                }
+            }
+            const size_t gi = (size_t)c * Vp + v0 + col;
+            stp_cs<NP>(A.gTn + gi, t);
+            if (H) stp_cs<NP>(A.hTn + gi, th);
+            float m[NS];
+    #pragma unroll
+            for (int s2 = 0; s2 < NS; ++s2) m[s2] = 0.0f;
+            mom32<D, H, NPL, NS>(m, L, ur, t, th, nullptr);
+            acc.add(reduce_scatter<NS, float>(m, lane));
+        }
+        // ---- slot totals of this cell into the batch; finish a full batch
+        if (writer) sM[warp][nb][myslot] = acc.value();
+        if (lane == 0) sC[warp][nb] = c;
+        ++nb;
+        if (nb == kGatherBatch || c + TW >= b.nC) {
+            __syncwarp();
+            if (lane < nb) finalize_cell32<D, H>(A, sC[warp][lane], sM[warp][lane]);
+            __syncwarp();
+            nb = 0;
+        }
+    }
+}
+
 template <int D, bool H>
 __global__ void k_ref_tables(StepArgs b, double T0, double hrefFac, float* mref, double* refMom, double* wallRefOut) {
     using SL = Slots<D, H>;

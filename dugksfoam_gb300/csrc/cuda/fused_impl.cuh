@@ -90,6 +90,15 @@ struct FusedArgs {
     // layout in tile_meta32_layout), tile t at meta + metaOff[t]
     const int4* meta;
     const int* metaOff;
+    // FP32: face values gbar_f (deviation form) of every active face, written
+    // by sweep A, and the face equilibrium tables {U, kexp} {1/RT, q'} {a, aA, RT, 0}
+    float* gF;                  // [nA][Vp]
+    float* hF;
+    float4* feqT;               // [nA][3]
+    // FP32: faces of each cell, {S oriented out of the cell, active face index}
+    const int* cfOff;           // [nC+1]
+    const float4* cfEnt;
+    const float* invVf;         // [nC] 1/V
     // macros of the next step
     double *rhoN, *UN, *TN, *qN, *tauN;
     double gscale, invGscale;

@@ -1,5 +1,6 @@
 // Fused pipeline factory: dispatch on the storage precision.
 #include <cstdlib>
+#include <string>
 
 #include "dugks/dugks.h"
 #include "fused.h"
@@ -17,6 +18,11 @@ int fused_ctas_per_sm() {
     const char* e = std::getenv("DUGKS_CTAS");
     const int c = e ? std::atoi(e) : 1;
     return c == 2 ? 2 : 1;
+}
+
+bool fused_cell_gather() {
+    const char* e = std::getenv("DUGKS_CELL_SWEEP");
+    return !(e && std::string(e) == "tiled");
 }
 
 int fused_dv_granule(int precision) { return 32 * fused_npl(precision); }

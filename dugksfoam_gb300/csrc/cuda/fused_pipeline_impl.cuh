@@ -31,6 +31,7 @@ public:
         if (D_ != 2 && D_ != 3) { err = "fused pipeline supports 2D and 3D meshes"; return false; }
         npl_ = fused_npl(sizeof(S) == 4 ? DUGKS_FP32_FP64MOM : DUGKS_FP64);
         ctas_ = sizeof(S) == 4 ? fused_ctas_per_sm() : 1;
+        gather_ = sizeof(S) == 4 && fused_cell_gather();
         const int KC = 32 * npl_;
         if (a.Vp % KC != 0) { err = "padded DV count is not a multiple of the DV chunk"; return false; }
         pick();
@@ -44,7 +45,9 @@ public:
         const size_t budget = std::min((size_t)maxSmem, (size_t)smemSM / ctas_ - 1024) - 1024;
         const char* envT = std::getenv("DUGKS_TILE_CELLS");
         const int maxCells = envT ? std::max(1, std::atoi(envT)) : 4096;
-        const SmemFn fn = [this](const TileDims& d) { return std::max(smemFace(d), smemCell(d)); };
+        const SmemFn fn = [this](const TileDims& d) {
+            return gather_ ? smemFace(d) : std::max(smemFace(d), smemCell(d));  // gather form: no tiles in sweep B
+        };
         if (!build_tile_plan(m, maxCells, fn, budget, plan_, err)) return false;
         smemA_ = smemB_ = 0;
         for (const TileHdr& h : plan_.hdr) {
@@ -54,7 +57,8 @@ public:
             smemB_ = std::max(smemB_, smemCell(d));
         }
         cudaFuncSetAttribute(kFace_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemA_);
-        cudaFuncSetAttribute(kCell_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
+        if (!gather_) cudaFuncSetAttribute(kCell_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
+        else smemB_ = 0;
 
         // ---- upload plan
         args_.hdr = upload(plan_.hdr);
@@ -125,6 +129,40 @@ public:
             metaOff.push_back((int)meta.size());
             args_.meta = upload(meta);
             args_.metaOff = upload(metaOff);
+            if (gather_) {
+                // faces of each cell in global face order, S oriented out of the cell
+                std::vector<int> cfOff(m.nC + 1);
+                std::vector<float4> cfEnt;
+                for (int c = 0; c < m.nC; ++c) {
+                    cfOff[c] = (int)cfEnt.size();
+                    for (int j = m.cellOff[c]; j < m.cellOff[c + 1]; ++j) {
+                        const int af = m.cellFace[j];
+                        const int gf = af < m.nI ? af : m.wallFace[af - m.nI];
+                        const double sg = m.cellSide[j] == 0 ? 1.0 : -1.0;
+                        float code;
+                        std::memcpy(&code, &af, 4);
+                        cfEnt.push_back(make_float4((float)(sg * m.Sf[3 * (size_t)gf]), (float)(sg * m.Sf[3 * (size_t)gf + 1]),
+                                                    (float)(sg * m.Sf[3 * (size_t)gf + 2]), code));
+                    }
+                }
+                cfOff[m.nC] = (int)cfEnt.size();
+                for (int c = 0; c < m.nC; ++c) gatherMF_ = std::max(gatherMF_, cfOff[c + 1] - cfOff[c]);
+                gatherMF_ = std::min(gatherMF_, 8);  // further faces of a cell are read directly
+                smemB_ = gather_smem(kGatherWarps, gatherMF_, KC, H_);
+                cudaFuncSetAttribute(kGather_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
+                int per = 0, nsm = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kGather_, kGatherWarps * 32, smemB_);
+                cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+                gatherBlocks_ = std::max(1, per) * std::max(1, nsm);  // persistent: one wave
+                args_.cfOff = upload(cfOff);
+                args_.cfEnt = upload(cfEnt);
+                std::vector<float> iv(m.nC);
+                for (int c = 0; c < m.nC; ++c) iv[c] = (float)(1.0 / m.V[c]);
+                args_.invVf = upload(iv);
+                args_.gF = alloc<float>((size_t)a.nA * a.Vp);
+                args_.hF = H_ ? alloc<float>((size_t)a.nA * a.Vp) : nullptr;
+                args_.feqT = alloc<float4>(3 * (size_t)a.nA);
+            }
             std::vector<float4> w4(std::max(a.nW, 1), make_float4(0, 0, 0, 0));
             std::vector<double> Tw(a.nW);
             if (a.nW) cudaMemcpy(Tw.data(), a.Tw, a.nW * 8, cudaMemcpyDeviceToHost);
@@ -218,7 +256,9 @@ public:
     }
 
     int nKernels() const override { return 2; }
-    const char* kernelName(int k) const override { return k == 0 ? "k_sweep_face" : "k_sweep_cell"; }
+    const char* kernelName(int k) const override {
+        return k == 0 ? "k_sweep_face" : (gather_ ? "k_cell_gather" : "k_sweep_cell");
+    }
 
     void launch(int k, const StepArgs& a, int sms, cudaStream_t s) override {
         (void)sms;
@@ -233,6 +273,7 @@ public:
         A.rhoN = rhoN_; A.UN = UN_; A.TN = TN_; A.qN = qN_; A.tauN = tauN_;
         const int threads = kWarpsPerSM / ctas_ * 32;
         if (k == 0) kFace_<<<plan_.nTiles, threads, smemA_, s>>>(A);
+        else if (gather_) kGather_<<<std::min((a.nC + kGatherWarps - 1) / kGatherWarps, gatherBlocks_), kGatherWarps * 32, smemB_, s>>>(A, gatherMF_);
         else kCell_<<<plan_.nTiles, threads, smemB_, s>>>(A);
     }
 
@@ -272,14 +313,15 @@ public:
     size_t bytes() const override { return bytes_; }
     std::string describe() const override {
         char buf[256];
-        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d ctas=%d smemA=%zu smemB=%zu",
+        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d ctas=%d gather=%d smemA=%zu smemB=%zu",
                  plan_.nTiles, plan_.maxT, (double)plan_.sumT / std::max(1, plan_.nTiles),
-                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, ctas_, smemA_, smemB_);
+                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, ctas_, (int)gather_, smemA_, smemB_);
         return buf;
     }
 
 private:
     static constexpr int kWarpsPerSM = 16;  // split over ctas_ resident tiles
+    static constexpr int kGatherWarps = 8;  // warps (cells) per block of the gather sweep
 
     template <typename T>
     T* alloc(size_t n) {
@@ -308,6 +350,7 @@ private:
                 kFace_ = k_sweep_face32<D, H, NPL, kWarpsPerSM>;
                 kCell_ = k_sweep_cell32<D, H, NPL, kWarpsPerSM>;
             }
+            if (gather_) kGather_ = k_cell_gather32<D, H, NPL, kGatherWarps>;
             kRef_ = k_ref_tables<D, H>;
         } else {
             kFace_ = k_sweep_face<S, D, H, NPL, kWarpsPerSM>;
@@ -339,6 +382,9 @@ private:
     size_t smemCell(const TileDims& d) const { return smemCellFn_(d); }
 
     int D_ = 2, npl_ = 1, ctas_ = 1;
+    bool gather_ = false;
+    int gatherMF_ = 0, gatherBlocks_ = 1;
+    void (*kGather_)(FusedArgs<S>, int) = nullptr;
     bool H_ = true;
     TilePlan plan_;
     FusedArgs<S> args_{};
