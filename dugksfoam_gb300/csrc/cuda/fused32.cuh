@@ -83,13 +83,16 @@ __host__ __device__ constexpr int tile_meta32_bound(int nFB, int nEnt, int nT2) 
 }
 
 // Shared memory of the FP32 sweeps (all offsets multiples of 16 bytes):
-//   sweep A: rows(T u H1 u H2) | face moments | metadata | face Uref | cell equilibria
+//   sweep A: NB x rows(T u H1 u H2) | face moments | metadata | face Uref | cell equilibria
 //   sweep B: rows(T u H1 u H2) | rows(T) | cell moments | metadata | face equilibria | cell equilibria
-template <int D, bool H, int NPL>
+// (NB = 2: the next chunk's rows stream into the second buffer.)
+template <int D, bool H, int NPL, int NB = 1>
 struct SmemLayout32 {
     static constexpr int KC = 32 * NPL, NS = Slots<D, H>::NS;
     __host__ __device__ static size_t rows(int n) { return (size_t)n * KC * sizeof(float) * (H ? 2 : 1); }
-    __host__ __device__ static size_t metaA(int nT2, int nFA) { return rows(nT2) + (size_t)nFA * NS * sizeof(Acc<float>); }
+    __host__ __device__ static size_t metaA(int nT2, int nFA) {
+        return NB * rows(nT2) + (size_t)nFA * NS * sizeof(Acc<float>);
+    }
     __host__ __device__ static size_t metaB(int nT2, int nT) {
         return rows(nT2) + rows(nT) + (size_t)nT * NS * sizeof(Acc<float>);
     }
@@ -99,6 +102,11 @@ struct SmemLayout32 {
     }
     static size_t cell(const TileDims& d) {
         return metaB(d.nT2, d.nT) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 48 * (size_t)d.nFB +
+               48 * (size_t)d.nT2;
+    }
+    // one-ring face-sides sweep: every face of T carries moments and a Uref
+    static size_t sides(const TileDims& d) {
+        return metaA(d.nT2, d.nFB) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 16 * (size_t)d.nFB +
                48 * (size_t)d.nT2;
     }
 };
@@ -202,6 +210,55 @@ struct Eq32 {
     }
 };
 
+
+// Asynchronous global -> shared copies (each lane copies, and later reads,
+// only its own NPL floats of a row, so a lane's wait_group is all the
+// ordering it needs).
+__device__ __forceinline__ void cp_async_row(float* dst, const float* src, int npl) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+    if (npl == 4) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
+    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Raw g~ (and h~) rows of T u H1 u H2 for the DV chunk at v0 into shared
+// memory, 16-byte asynchronous copies spread over the block (one commit group).
+template <int NPL, bool H, int NT>
+__device__ __forceinline__ void issue_rows32(const FusedArgs<float>& A, const TileHdr& hd, const int* C, float* sg,
+                                             float* sh, int v0) {
+    constexpr int KC = 32 * NPL, SEG = KC / 4;
+    const int n = hd.nT2 * SEG;
+    for (int i = threadIdx.x; i < n; i += NT) {
+        const int r = i / SEG, sgm = i - r * SEG;
+        const size_t gi = (size_t)C[r] * A.b.Vp + v0 + sgm * 4;
+        cp_async_row(sg + r * KC + sgm * 4, A.gT + gi, 4);
+        if (H) cp_async_row(sh + r * KC + sgm * 4, A.hT + gi, 4);
+    }
+    cp_async_commit();
+}
+
+// gbar+ = relaxation of the raw rows in place (shared memory only).
+template <int D, bool H, int NPL, int NW>
+__device__ __forceinline__ void relax_rows32(const FusedArgs<float>& A, const TileHdr& hd, const float4* ceq,
+                                             const Lane32<D, NPL>& L, int lane, int warp, float* sg, float* sh) {
+    constexpr int KC = 32 * NPL, NP = NPL / 2;
+    for (int r = warp; r < hd.nT2; r += NW) {
+        float2 g[NP], h[NP];
+        ldp<NP>(g, sg + r * KC + lane * NPL);
+        if (H) ldp<NP>(h, sh + r * KC + lane * NPL);
+        Eq32<D, H> e;
+        e.load(ceq + 3 * r, A.b.K, A.hrefFac);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            if (!H) h[p] = f2(0.f);
+            e.relax(L, p, g[p], h[p]);
+        }
+        stp<NP>(sg + r * KC + lane * NPL, g);
+        if (H) stp<NP>(sh + r * KC + lane * NPL, h);
+    }
+}
 
 // gbar+ rows of T u H1 u H2 (and for sweep B the g~new partial of T's rows).
 // Two rows per warp iteration keep two row loads in flight.
@@ -359,9 +416,9 @@ __device__ __forceinline__ void recon32(const FusedArgs<float>& A, const float4*
 #pragma unroll
         for (int k = 0; k < D; ++k) { gw[k][p] = f2(0.f); hw[k][p] = f2(0.f); }
     }
-    for (int e = F.r.stO0; e < F.r.stO1; ++e)
-        side_entry<D, H, NP, WALL>(A, E, e, F.dOx, F.dOy, F.dOz, cO, hO, sg, sh, col, v0, L.x, L.y, L.z, aO, ahO, gw, hw);
     if (WALL) {
+        for (int e = F.r.stO0; e < F.r.stO1; ++e)
+            side_entry<D, H, NP, true>(A, E, e, F.dOx, F.dOy, F.dOz, cO, hO, sg, sh, col, v0, L.x, L.y, L.z, aO, ahO, gw, hw);
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
             gf[p] = add2(cO[p], aO[p]);
@@ -372,8 +429,16 @@ __device__ __forceinline__ void recon32(const FusedArgs<float>& A, const float4*
     ldp<NP>(cN, sg + F.r.neiL * KC + col);
     if (H) ldp<NP>(hN, sh + F.r.neiL * KC + col);
     float2 dw[D][NP], dhw[D][NP];
-    for (int e = F.r.stN0; e < F.r.stN1; ++e)
-        side_entry<D, H, NP, false>(A, E, e, F.dNx, F.dNy, F.dNz, cN, hN, sg, sh, col, v0, L.x, L.y, L.z, aN, ahN, dw, dhw);
+    // owner and neighbour entries interleaved: two independent accumulation chains
+    const int nO = F.r.stO1 - F.r.stO0, nN = F.r.stN1 - F.r.stN0;
+    for (int k = 0; k < max(nO, nN); ++k) {
+        if (k < nO)
+            side_entry<D, H, NP, false>(A, E, F.r.stO0 + k, F.dOx, F.dOy, F.dOz, cO, hO, sg, sh, col, v0, L.x, L.y, L.z, aO,
+                                        ahO, gw, hw);
+        if (k < nN)
+            side_entry<D, H, NP, false>(A, E, F.r.stN0 + k, F.dNx, F.dNy, F.dNz, cN, hN, sg, sh, col, v0, L.x, L.y, L.z, aN,
+                                        ahN, dw, dhw);
+    }
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
         const float2 go = add2(cO[p], aO[p]), gn = add2(cN[p], aN[p]);
@@ -452,8 +517,65 @@ __device__ __forceinline__ void ref_moments_about(const double* R, const double*
     }
 }
 
+// Face macros (FP64) from the deviation moment totals M of face a (wall w or
+// -1) about its reference velocity u4: P4 Maxwell-wall density, P5 incoming
+// wall moments, P6 face macros, wall heat flux and stress; then the face
+// equilibrium table and the next reference velocity.
+template <int D, bool H>
+__device__ __forceinline__ void finalize_face32(const FusedArgs<float>& A, int a, int w, float4 u4, double* M) {
+    using SL = Slots<D, H>;
+    constexpr int NS = SL::NS;
+    const StepArgs& b = A.b;
+    const double ur[3] = {u4.x, u4.y, u4.z};
+    double rw = 0.0;
+    if (w >= 0) {  // outgoing: deviation + reference parts; incoming: rho_w * Mw
+        const double* RO = A.wallRefOut + (size_t)w * NS;
+        for (int s = 0; s <= SL::FLUX; ++s) M[s] += RO[s];
+        rw = M[SL::FLUX] / b.incAbs[w];
+        for (int s = 0; s < SL::NM; ++s) M[s] += rw * A.Min[(size_t)w * NS + s];
+    } else {
+        double Rm[NS];
+        ref_moments_about<D, H>(A.refMom, ur, Rm);
+        for (int s = 0; s < SL::NM; ++s) M[s] += Rm[s];
+    }
+    for (int s = 0; s < SL::NM; ++s) M[s] *= A.invGscale;
+    double rho, U[3], T, tau, qr[3];
+    macros_from_moments<D, H>(M, ur, b, rho, U, T, tau, qr);
+    const double fac = 2.0 * tau / (2.0 * tau + 0.5 * b.dt * b.Pr);
+    double q[3] = {fac * qr[0], fac * qr[1], fac * qr[2]};
+    b.rhoF[a] = rho;
+    b.TF[a] = T;
+    b.tauF[a] = tau;
+    for (int k = 0; k < 3; ++k) { b.UF[3 * a + k] = U[k]; b.qF[3 * a + k] = q[k]; }
+    float* blk = A.fc + (size_t)a * kNCoef;
+    write_coef<D>(blk, rho, U, T, q, tau, b, A.gscale);
+    if (A.feqT) eq_table(A.feqT + 3 * (size_t)a, blk, face_weight(A.dt, blk));
+    if (w < 0) {
+        A.uref4[a] = make_float4((float)U[0], (float)U[1], (float)U[2], 0.0f);
+        return;
+    }
+    b.rhoW[w] = rw * A.invGscale;
+    A.rhoWs[w] = (float)rw;
+    const double fq = 2.0 * tau / (2.0 * tau + 0.5 * b.dt * b.Pr);
+    const double fs = 2.0 * tau / (2.0 * tau + 0.5 * b.dt);
+    for (int k = 0; k < 3; ++k) {
+        double v = 0.0;
+        if (k < D) v = 0.5 * M[SL::M3 + k] + (H ? 0.5 * M[SL::H1 + k] : 0.0);
+        b.qWall[3 * w + k] = fq * v;
+    }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double sv = 0.0;
+            if (i < D && j < D) {
+                const double m2 = M[SL::M2 + (i <= j ? sym<D>(i, j) : sym<D>(j, i))];
+                sv = m2 + ur[i] * M[SL::M1 + j] + ur[j] * M[SL::M1 + i] + ur[i] * ur[j] * M[0];
+            }
+            b.stressWall[9 * w + 3 * i + j] = fs * sv;
+        }
+}
+
 // ---------------------------------------------------------------- sweep A
-template <int D, bool H, int NPL, int NW>
+template <int D, bool H, int NPL, int NW, bool PIPE>
 __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<float> A) {
     using SL = Slots<D, H>;
     constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
@@ -462,10 +584,11 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<flo
     const StepArgs& b = A.b;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Vp = b.Vp;
-    using LY = SmemLayout32<D, H, NPL>;
+    using LY = SmemLayout32<D, H, NPL, PIPE ? 2 : 1>;
     float* sg = reinterpret_cast<float*>(smem);
     float* sh = sg + (size_t)hd.nT2 * KC;
-    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + LY::rows(hd.nT2));
+    const size_t bufStride = LY::rows(hd.nT2) / sizeof(float);  // second row buffer (PIPE)
+    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + (PIPE ? 2 : 1) * LY::rows(hd.nT2));
     for (int i = threadIdx.x; i < hd.nFA * NS; i += NW * 32) mom[i].zero();
     const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::metaA(hd.nT2, hd.nFA));
     float4* sU = tm.dyn;             // [nFA] face Uref
@@ -480,12 +603,31 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<flo
     const int myslot = slot_of<NS>(lane);
     const bool writer = NS == 16 ? (lane & 1) == 0 : true;
 
+    if (PIPE) {
+        __syncthreads();  // cell ids staged
+        issue_rows32<NPL, H, NW * 32>(A, hd, tm.C, sg, sh, 0);
+    }
     for (int ch = 0; ch < nChunks; ++ch) {
         const int v0 = ch * KC;
         Lane32<D, NPL> L;
         L.load(A, v0, lane);
-        __syncthreads();
-        rows32<D, H, NPL, NW, false>(A, hd, tm, ceq, L, v0, lane, warp, sg, sh, nullptr, nullptr);
+        float* cg = sg;
+        float* chh = sh;
+        if (PIPE) {
+            // chunk ch's raw rows landed in buffer ch&1; the other buffer's
+            // faces (chunk ch-1) are done, so chunk ch+1 streams into it
+            cp_async_wait<0>();
+            __syncthreads();
+            cg = sg + (ch & 1) * bufStride;
+            chh = sh + (ch & 1) * bufStride;
+            if (ch + 1 < nChunks)
+                issue_rows32<NPL, H, NW * 32>(A, hd, tm.C, sg + ((ch + 1) & 1) * bufStride,
+                                              sh + ((ch + 1) & 1) * bufStride, v0 + KC);
+            relax_rows32<D, H, NPL, NW>(A, hd, ceq, L, lane, warp, cg, chh);
+        } else {
+            __syncthreads();
+            rows32<D, H, NPL, NW, false>(A, hd, tm, ceq, L, v0, lane, warp, sg, sh, nullptr, nullptr);
+        }
         __syncthreads();
         for (int lf = warp; lf < hd.nFA; lf += NW) {
             Face32 F;
@@ -500,7 +642,7 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<flo
 #pragma unroll
             for (int s = 0; s < NS; ++s) m[s] = 0.0f;
             if (F.r.w >= 0) {
-                recon32<D, H, NPL, true>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
+                recon32<D, H, NPL, true>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
                 float2 gn[NP], hn[NP], use[NP];
                 float fl = 0.0f;
 #pragma unroll
@@ -521,7 +663,7 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<flo
                 if (H) stp<NP>(A.Gbhn + wi, hn);
                 mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
             } else {
-                recon32<D, H, NPL, false>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
+                recon32<D, H, NPL, false>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
                 mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
             }
             if (A.gF) {
@@ -537,55 +679,187 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<flo
     // ---- finalize owned faces (FP64)
     for (int lf = threadIdx.x; lf < hd.nFA; lf += NW * 32) {
         const int4 rr = tm.F[5 * lf];
-        struct { int a, w; } r = {rr.z, rr.w};
         const float4 u4 = sU[lf];
-        const double ur[3] = {u4.x, u4.y, u4.z};
-        double M[NS], Rm[NS];
+        double M[NS];
         for (int s = 0; s < NS; ++s) M[s] = mom[lf * NS + s].value();
-        double rw = 0.0;
-        if (r.w >= 0) {  // outgoing: deviation + reference parts; incoming: rho_w * Mw
-            const double* RO = A.wallRefOut + (size_t)r.w * NS;
-            for (int s = 0; s <= SL::FLUX; ++s) M[s] += RO[s];
-            rw = M[SL::FLUX] / b.incAbs[r.w];
-            for (int s = 0; s < SL::NM; ++s) M[s] += rw * A.Min[(size_t)r.w * NS + s];
-        } else {
-            ref_moments_about<D, H>(A.refMom, ur, Rm);
-            for (int s = 0; s < SL::NM; ++s) M[s] += Rm[s];
-        }
-        for (int s = 0; s < SL::NM; ++s) M[s] *= A.invGscale;
-        double rho, U[3], T, tau, qr[3];
-        macros_from_moments<D, H>(M, ur, b, rho, U, T, tau, qr);
-        const double fac = 2.0 * tau / (2.0 * tau + 0.5 * b.dt * b.Pr);
-        double q[3] = {fac * qr[0], fac * qr[1], fac * qr[2]};
-        const int a = r.a;
-        b.rhoF[a] = rho;
-        b.TF[a] = T;
-        b.tauF[a] = tau;
-        for (int k = 0; k < 3; ++k) { b.UF[3 * a + k] = U[k]; b.qF[3 * a + k] = q[k]; }
-        write_coef<D>(A.fc + (size_t)a * kNCoef, rho, U, T, q, tau, b, A.gscale);
-        if (A.feqT) eq_table(A.feqT + 3 * (size_t)a, A.fc + (size_t)a * kNCoef, face_weight(A.dt, A.fc + (size_t)a * kNCoef));
-        if (r.w < 0) A.uref4[a] = make_float4((float)U[0], (float)U[1], (float)U[2], 0.0f);
-        if (r.w >= 0) {
-            const int w = r.w;
-            b.rhoW[w] = rw * A.invGscale;
-            A.rhoWs[w] = (float)rw;
-            const double fq = 2.0 * tau / (2.0 * tau + 0.5 * b.dt * b.Pr);
-            const double fs = 2.0 * tau / (2.0 * tau + 0.5 * b.dt);
-            for (int k = 0; k < 3; ++k) {
-                double v = 0.0;
-                if (k < D) v = 0.5 * M[SL::M3 + k] + (H ? 0.5 * M[SL::H1 + k] : 0.0);
-                b.qWall[3 * w + k] = fq * v;
-            }
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) {
-                    double s = 0.0;
-                    if (i < D && j < D) {
-                        const double m2 = M[SL::M2 + (i <= j ? sym<D>(i, j) : sym<D>(j, i))];
-                        s = m2 + ur[i] * M[SL::M1 + j] + ur[j] * M[SL::M1 + i] + ur[i] * ur[j] * M[0];
+        finalize_face32<D, H>(A, rr.z, rr.w, u4, M);
+    }
+}
+
+// ---------------------------------------------------------------- sweep A, face sides
+// One-sided upwind reconstruction from cell u (local row lu, stencil entries
+// [e0,e1) of u, d = Cf - C_u): val = gbar+_u + sum_e L_e.(d - xi dt/2) (gbar+_e - gbar+_u).
+template <int D, bool H, int NPL>
+__device__ __forceinline__ void recon_one32(const FusedArgs<float>& A, const float4* E, int e0, int e1, int lu,
+                                            float dx, float dy, float dz, const Lane32<D, NPL>& L, const float* sg,
+                                            const float* sh, int lane, int v0, float2 (&gv)[NPL / 2],
+                                            float2 (&hv)[NPL / 2]) {
+    constexpr int KC = 32 * NPL, NP = NPL / 2;
+    const int col = lane * NPL;
+    float2 c[NP], hc[NP], ac[NP], ah[NP], gw[D][NP], hw[D][NP];
+    ldp<NP>(c, sg + lu * KC + col);
+    if (H) ldp<NP>(hc, sh + lu * KC + col);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        ac[p] = f2(0.f);
+        ah[p] = f2(0.f);
+        if (!H) hc[p] = f2(0.f);
+    }
+    for (int e = e0; e < e1; ++e)
+        side_entry<D, H, NP, false>(A, E, e, dx, dy, dz, c, hc, sg, sh, col, v0, L.x, L.y, L.z, ac, ah, gw, hw);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        gv[p] = add2(c[p], ac[p]);
+        hv[p] = H ? add2(hc[p], ah[p]) : f2(0.f);
+    }
+}
+
+// Sweep A on tiles with a one-ring halo (rows of T u H1).  Every face touching
+// T is visited.  A face with both cells in T, and every wall face of T, is
+// complete here; for a face across the tile boundary only the side whose cell
+// is in T is reconstructed (its gradient needs T u H1 only): the velocities
+// for which that cell is upwind, plus half of the ties (xi.S == 0) in the
+// moments.  The tile on the other side adds the rest, so every face side is
+// reconstructed exactly once.  Per-side moment totals go to faceMom[a][side]
+// (side 0: owner or complete, side 1: neighbour) and k_face_macros32 forms the
+// face macros.  Face values are stored for the velocities this side owns
+// (tie values are never read: their flux is zero).  Raw rows of the next DV
+// chunk stream into the second row buffer while this chunk's faces run.
+template <int D, bool H, int NPL, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) k_face_sides32(FusedArgs<float> A) {
+    using SL = Slots<D, H>;
+    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
+    extern __shared__ __align__(16) unsigned char smem[];
+    const TileHdr hd = A.hdr[blockIdx.x];
+    const StepArgs& b = A.b;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int Vp = b.Vp, col = lane * NPL;
+    using LY = SmemLayout32<D, H, NPL, 2>;
+    float* sg = reinterpret_cast<float*>(smem);
+    float* sh = sg + (size_t)hd.nT2 * KC;
+    const size_t bufStride = LY::rows(hd.nT2) / sizeof(float);
+    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + 2 * LY::rows(hd.nT2));
+    for (int i = threadIdx.x; i < hd.nFB * NS; i += NW * 32) mom[i].zero();
+    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::metaA(hd.nT2, hd.nFB));
+    float4* sU = tm.dyn;            // [nFB] face Uref
+    float4* ceq = tm.dyn + hd.nFB;  // [nT2][3] cell equilibria
+    __syncthreads();
+    for (int i = threadIdx.x; i < hd.nFB; i += NW * 32) sU[i] = A.uref4[tm.F[5 * i].z];
+    for (int i = threadIdx.x; i < hd.nT2; i += NW * 32) {
+        const float* blk = A.cc + (size_t)tm.C[i] * kNCoef;
+        eq_table(ceq + 3 * i, blk, cell_weight(A.dt, blk));
+    }
+    issue_rows32<NPL, H, NW * 32>(A, hd, tm.C, sg, sh, 0);
+    const int nChunks = Vp / KC;
+    const int myslot = slot_of<NS>(lane);
+    const bool writer = NS == 16 ? (lane & 1) == 0 : true;
+
+    for (int ch = 0; ch < nChunks; ++ch) {
+        const int v0 = ch * KC;
+        Lane32<D, NPL> L;
+        L.load(A, v0, lane);
+        cp_async_wait<0>();
+        __syncthreads();
+        float* cg = sg + (ch & 1) * bufStride;
+        float* chh = sh + (ch & 1) * bufStride;
+        if (ch + 1 < nChunks)
+            issue_rows32<NPL, H, NW * 32>(A, hd, tm.C, sg + ((ch + 1) & 1) * bufStride, sh + ((ch + 1) & 1) * bufStride,
+                                          v0 + KC);
+        relax_rows32<D, H, NPL, NW>(A, hd, ceq, L, lane, warp, cg, chh);
+        __syncthreads();
+        for (int lf = warp; lf < hd.nFB; lf += NW) {
+            Face32 F;
+            F.load(tm.F + 5 * lf);
+            const float4 u4 = sU[lf];
+            const float ur[3] = {u4.x, u4.y, u4.z};
+            float2 xs[NP];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) xs[p] = F.xs<D, NPL>(L, p);
+            float2 gf[NP], hf[NP], gw[D][NP], hw[D][NP];
+            float m[NS];
+#pragma unroll
+            for (int s = 0; s < NS; ++s) m[s] = 0.0f;
+            const size_t fi = (size_t)F.r.a * Vp + v0 + col;
+            if (F.r.w >= 0) {
+                recon32<D, H, NPL, true>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
+                float2 gn[NP], hn[NP], use[NP];
+                float fl = 0.0f;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    gn[p] = fma2(gw[1][p], f2(F.dNy), mul2(gw[0][p], f2(F.dNx)));
+                    if (D == 3) gn[p] = fma2(gw[2][p], f2(F.dNz), gn[p]);
+                    if (H) {
+                        hn[p] = fma2(hw[1][p], f2(F.dNy), mul2(hw[0][p], f2(F.dNx)));
+                        if (D == 3) hn[p] = fma2(hw[2][p], f2(F.dNz), hn[p]);
                     }
-                    b.stressWall[9 * w + 3 * i + j] = fs * s;
+                    use[p] = make_float2(xs[p].x > 0.f ? 1.f : 0.f, xs[p].y > 0.f ? 1.f : 0.f);
+                    const float2 fx = mul2(mul2(mul2(L.w[p], xs[p]), gf[p]), use[p]);
+                    fl += fx.x + fx.y;
                 }
+                m[SL::FLUX] = fl;
+                const size_t wi = (size_t)F.r.w * Vp + v0 + col;
+                stp<NP>(A.Gbgn + wi, gn);
+                if (H) stp<NP>(A.Gbhn + wi, hn);
+                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
+                stp<NP>(A.gF + fi, gf);
+                if (H) stp<NP>(A.hF + fi, hf);
+            } else if (F.r.ownL < hd.nT && F.r.neiL < hd.nT) {  // both sides in T: complete
+                recon32<D, H, NPL, false>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
+                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
+                stp<NP>(A.gF + fi, gf);
+                if (H) stp<NP>(A.hF + fi, hf);
+            } else {  // one side in T
+                const bool own = F.r.ownL < hd.nT;
+                if (own)
+                    recon_one32<D, H, NPL>(A, tm.E, F.r.stO0, F.r.stO1, F.r.ownL, F.dOx, F.dOy, F.dOz, L, cg, chh, lane,
+                                           v0, gf, hf);
+                else
+                    recon_one32<D, H, NPL>(A, tm.E, F.r.stN0, F.r.stN1, F.r.neiL, F.dNx, F.dNy, F.dNz, L, cg, chh, lane,
+                                           v0, gf, hf);
+                float2 wt[NP];
+                float* dg = A.gF + fi;
+                float* dh = H ? A.hF + fi : nullptr;
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    const bool u0 = own ? xs[p].x > 0.f : xs[p].x < 0.f, u1 = own ? xs[p].y > 0.f : xs[p].y < 0.f;
+                    wt[p] = make_float2(u0 ? 1.f : (xs[p].x == 0.f ? 0.5f : 0.f), u1 ? 1.f : (xs[p].y == 0.f ? 0.5f : 0.f));
+                    if (u0) {
+                        dg[2 * p] = gf[p].x;
+                        if (H) dh[2 * p] = hf[p].x;
+                    }
+                    if (u1) {
+                        dg[2 * p + 1] = gf[p].y;
+                        if (H) dh[2 * p + 1] = hf[p].y;
+                    }
+                }
+                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, wt);
+            }
+            const float tot = reduce_scatter<NS, float>(m, lane);
+            if (writer && myslot <= SL::FLUX) mom[lf * NS + myslot].add(tot);
         }
+    }
+    __syncthreads();
+    // ---- per-side totals (FP64) to faceMom[a][side]
+    for (int lf = threadIdx.x; lf < hd.nFB; lf += NW * 32) {
+        const int4 rr = tm.F[5 * lf];  // {ownL, neiL, a, w}
+        const bool own = rr.x < hd.nT, complete = rr.w >= 0 || (own && rr.y < hd.nT);
+        double* dst = A.faceMom + (size_t)rr.z * 2 * NS;
+        double* mine = dst + (own ? 0 : NS);
+        for (int s = 0; s < NS; ++s) mine[s] = mom[lf * NS + s].value();
+        if (complete)
+            for (int s = 0; s < NS; ++s) dst[NS + s] = 0.0;
+    }
+}
+
+// Face macros of every active face from the two per-side moment totals.
+template <int D, bool H>
+__global__ void k_face_macros32(FusedArgs<float> A) {
+    constexpr int NS = Slots<D, H>::NS;
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.b.nA; a += gridDim.x * blockDim.x) {
+        const double* src = A.faceMom + (size_t)a * 2 * NS;
+        double M[NS];
+        for (int s = 0; s < NS; ++s) M[s] = src[s] + src[NS + s];
+        finalize_face32<D, H>(A, a, a >= A.b.nI ? a - A.b.nI : -1, A.uref4[a], M);
     }
 }
 
@@ -744,18 +1018,6 @@ __global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_cell32(FusedArgs<flo
 // (scaled, about the origin) and, per wall face, the reference moments over
 // the outgoing velocities about U_w plus the reference outgoing flux.
 // ---------------------------------------------------------------- sweep B, gather form
-// Asynchronous global -> shared copies (each lane copies, and later reads,
-// only its own NPL floats of a row, so a lane's wait_group is all the
-// ordering it needs).
-__device__ __forceinline__ void cp_async_row(float* dst, const float* src, int npl) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
-    if (npl == 4) asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(src) : "memory");
-    else asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-
 // Shared memory of the gather sweep: per warp two stages of (1 + MF) rows of
 // g (and h): the cell's g~ row and its first MF faces' stored values.
 __host__ __device__ inline size_t gather_smem(int nw, int mf, int kc, bool h) {
@@ -786,7 +1048,7 @@ __device__ __forceinline__ void finalize_cell32(const FusedArgs<float>& A, int c
 }
 
 // Cells per warp batch of the gather sweep's FP64 macro step (one lane per cell).
-constexpr int kGatherBatch = 8;
+constexpr int kGatherBatch = 32;
 
 // Warps stride over the cells (persistent grid); per cell, all DV chunks:
 //   g~new = g+ + (g+ - g~)/3 - dt/V sum_f (xi.S_f) g^f_f,

@@ -95,6 +95,7 @@ struct FusedArgs {
     float* gF;                  // [nA][Vp]
     float* hF;
     float4* feqT;               // [nA][3]
+    double* faceMom;            // [nA][2][NS] per-side face moment totals (one-ring tiles)
     // FP32: faces of each cell, {S oriented out of the cell, active face index}
     const int* cfOff;           // [nC+1]
     const float4* cfEnt;
@@ -410,8 +411,9 @@ __device__ __forceinline__ void macros_from_moments(const double* M, const doubl
                                                     double& rho, double* U, double& T, double& tau, double* qraw) {
     using SL = Slots<D, H>;
     rho = M[0];
+    const double irho = 1.0 / rho;
     double d[3] = {0, 0, 0};
-    for (int i = 0; i < D; ++i) d[i] = M[SL::M1 + i] / rho;
+    for (int i = 0; i < D; ++i) d[i] = M[SL::M1 + i] * irho;
     for (int i = 0; i < 3; ++i) U[i] = Uref[i] + d[i];
     double tr = 0, m1d = 0, dd = 0;
     for (int i = 0; i < D; ++i) {
@@ -433,17 +435,21 @@ __device__ __forceinline__ void macros_from_moments(const double* M, const doubl
     }
 }
 
-// FP32 equilibrium coefficient block from FP64 macros (density scaled by gs).
+// FP32 equilibrium coefficient block from FP64 macros (density scaled by gs),
+// each entry rounded once; two FP64 divisions (GB300 issues FP64 at 1/64 of
+// the FP32 rate).
 template <int D>
 __device__ __forceinline__ void write_coef(float* blk, double rho, const double* U, double T, const double* q,
                                            double tau, const StepArgs& b, double gs) {
     const double RT = b.R * T;
-    const double pw = D == 2 ? 2.0 * kPi * RT : (D == 3 ? pow(2.0 * kPi * RT, 1.5) : sqrt(2.0 * kPi * RT));
-    const double qs = (1.0 - b.Pr) / (5.0 * rho * RT * RT);
+    const double iRT = 1.0 / RT, irho = 1.0 / rho;
+    const double t = iRT * (0.5 / kPi);  // 1/(2 pi RT)
+    const double ipw = D == 2 ? t : (D == 3 ? t * sqrt(t) : sqrt(t));
+    const double qs = (1.0 - b.Pr) * 0.2 * irho * iRT * iRT;
     float4* o = reinterpret_cast<float4*>(blk);
-    o[0] = make_float4((float)U[0], (float)U[1], (float)U[2], (float)(-1.4426950408889634 / (2.0 * RT)));
-    o[1] = make_float4((float)(1.0 / RT), (float)(q[0] * qs), (float)(q[1] * qs), (float)(q[2] * qs));
-    o[2] = make_float4((float)(rho * gs / pw), (float)RT, (float)tau, 0.0f);
+    o[0] = make_float4((float)U[0], (float)U[1], (float)U[2], (float)(-0.72134752044448170 * iRT));  // -log2(e)/(2RT)
+    o[1] = make_float4((float)iRT, (float)(q[0] * qs), (float)(q[1] * qs), (float)(q[2] * qs));
+    o[2] = make_float4((float)(rho * gs * ipw), (float)RT, (float)tau, 0.0f);
 }
 
 }  // namespace dugks

@@ -25,6 +25,16 @@ bool fused_cell_gather() {
     return !(e && std::string(e) == "tiled");
 }
 
+bool fused_face_pipe() {
+    const char* e = std::getenv("DUGKS_SWEEPA_PIPE");
+    return !(e && std::string(e) == "0");
+}
+
+bool fused_face_sides() {
+    const char* e = std::getenv("DUGKS_SWEEPA");
+    return !(e && std::string(e) == "owned");
+}
+
 int fused_dv_granule(int precision) { return 32 * fused_npl(precision); }
 
 std::unique_ptr<FusedPipeline> make_fused_pipeline(Solver& s, const StepArgs& a, int precision, std::string& err) {

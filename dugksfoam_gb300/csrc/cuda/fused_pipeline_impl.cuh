@@ -32,6 +32,8 @@ public:
         npl_ = fused_npl(sizeof(S) == 4 ? DUGKS_FP32_FP64MOM : DUGKS_FP64);
         ctas_ = sizeof(S) == 4 ? fused_ctas_per_sm() : 1;
         gather_ = sizeof(S) == 4 && fused_cell_gather();
+        pipeA_ = sizeof(S) == 4 && fused_face_pipe();
+        sides_ = gather_ && fused_face_sides();
         const int KC = 32 * npl_;
         if (a.Vp % KC != 0) { err = "padded DV count is not a multiple of the DV chunk"; return false; }
         pick();
@@ -48,7 +50,7 @@ public:
         const SmemFn fn = [this](const TileDims& d) {
             return gather_ ? smemFace(d) : std::max(smemFace(d), smemCell(d));  // gather form: no tiles in sweep B
         };
-        if (!build_tile_plan(m, maxCells, fn, budget, plan_, err)) return false;
+        if (!build_tile_plan(m, maxCells, fn, budget, plan_, err, sides_ ? 1 : 2)) return false;
         smemA_ = smemB_ = 0;
         for (const TileHdr& h : plan_.hdr) {
             TileDims d;
@@ -115,8 +117,9 @@ public:
                     const size_t rec = (size_t)h.faceStart + k;
                     const TileFace& r = plan_.faces[rec];
                     meta.push_back(make_int4(r.ownL, r.neiL, r.a, r.w));
-                    meta.push_back(make_int4(r.stO0 - base, r.stO1 - base, r.neiL >= 0 ? r.stN0 - base : 0,
-                                             r.neiL >= 0 ? r.stN1 - base : 0));
+                    const bool so = r.stO1 > r.stO0, sn = r.neiL >= 0 && r.stN1 > r.stN0;  // non-empty stencils
+                    meta.push_back(make_int4(so ? r.stO0 - base : 0, so ? r.stO1 - base : 0, sn ? r.stN0 - base : 0,
+                                             sn ? r.stN1 - base : 0));
                     for (int q = 0; q < 3; ++q) meta.push_back(f4i(fg4[3 * rec + q]));
                 }
                 for (int e = 0; e < h.nEnt; ++e) meta.push_back(f4i(st4[(size_t)base + e]));
@@ -162,6 +165,7 @@ public:
                 args_.gF = alloc<float>((size_t)a.nA * a.Vp);
                 args_.hF = H_ ? alloc<float>((size_t)a.nA * a.Vp) : nullptr;
                 args_.feqT = alloc<float4>(3 * (size_t)a.nA);
+                if (sides_) args_.faceMom = alloc<double>((size_t)a.nA * 2 * 32);
             }
             std::vector<float4> w4(std::max(a.nW, 1), make_float4(0, 0, 0, 0));
             std::vector<double> Tw(a.nW);
@@ -255,8 +259,9 @@ public:
         if (sizeof(S) == 4) k_face_uref<<<sms * 2, 256, 0, s>>>(a, args_.uref4);
     }
 
-    int nKernels() const override { return 2; }
+    int nKernels() const override { return sides_ ? 3 : 2; }
     const char* kernelName(int k) const override {
+        if (sides_) return k == 0 ? "k_face_sides" : (k == 1 ? "k_face_macros" : "k_cell_gather");
         return k == 0 ? "k_sweep_face" : (gather_ ? "k_cell_gather" : "k_sweep_cell");
     }
 
@@ -272,6 +277,11 @@ public:
         A.cc = cc_[cur_]; A.ccn = cc_[1 - cur_];
         A.rhoN = rhoN_; A.UN = UN_; A.TN = TN_; A.qN = qN_; A.tauN = tauN_;
         const int threads = kWarpsPerSM / ctas_ * 32;
+        if (sides_ && k == 1) {
+            kMacros_<<<sms * 4, 128, 0, s>>>(A);
+            return;
+        }
+        if (sides_ && k == 2) k = 1;
         if (k == 0) kFace_<<<plan_.nTiles, threads, smemA_, s>>>(A);
         else if (gather_) kGather_<<<std::min((a.nC + kGatherWarps - 1) / kGatherWarps, gatherBlocks_), kGatherWarps * 32, smemB_, s>>>(A, gatherMF_);
         else kCell_<<<plan_.nTiles, threads, smemB_, s>>>(A);
@@ -313,9 +323,9 @@ public:
     size_t bytes() const override { return bytes_; }
     std::string describe() const override {
         char buf[256];
-        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d ctas=%d gather=%d smemA=%zu smemB=%zu",
+        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d ctas=%d gather=%d pipeA=%d sides=%d smemA=%zu smemB=%zu",
                  plan_.nTiles, plan_.maxT, (double)plan_.sumT / std::max(1, plan_.nTiles),
-                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, ctas_, (int)gather_, smemA_, smemB_);
+                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, ctas_, (int)gather_, (int)pipeA_, (int)sides_, smemA_, smemB_);
         return buf;
     }
 
@@ -344,13 +354,19 @@ private:
     void set() {
         if constexpr (sizeof(S) == 4) {
             if (ctas_ == 2) {
-                kFace_ = k_sweep_face32<D, H, NPL, kWarpsPerSM / 2>;
+                kFace_ = pipeA_ ? k_sweep_face32<D, H, NPL, kWarpsPerSM / 2, true>
+                                : k_sweep_face32<D, H, NPL, kWarpsPerSM / 2, false>;
                 kCell_ = k_sweep_cell32<D, H, NPL, kWarpsPerSM / 2>;
             } else {
-                kFace_ = k_sweep_face32<D, H, NPL, kWarpsPerSM>;
+                kFace_ = pipeA_ ? k_sweep_face32<D, H, NPL, kWarpsPerSM, true>
+                                : k_sweep_face32<D, H, NPL, kWarpsPerSM, false>;
                 kCell_ = k_sweep_cell32<D, H, NPL, kWarpsPerSM>;
             }
             if (gather_) kGather_ = k_cell_gather32<D, H, NPL, kGatherWarps>;
+            if (sides_) {
+                kFace_ = k_face_sides32<D, H, NPL, kWarpsPerSM>;
+                kMacros_ = k_face_macros32<D, H>;
+            }
             kRef_ = k_ref_tables<D, H>;
         } else {
             kFace_ = k_sweep_face<S, D, H, NPL, kWarpsPerSM>;
@@ -358,7 +374,8 @@ private:
         }
         kTables_ = k_wall_tables<S, D, H>;
         if constexpr (sizeof(S) == 4) {
-            smemFaceFn_ = &SmemLayout32<D, H, NPL>::face;
+            smemFaceFn_ = sides_ ? &SmemLayout32<D, H, NPL, 2>::sides
+                                 : (pipeA_ ? &SmemLayout32<D, H, NPL, 2>::face : &SmemLayout32<D, H, NPL, 1>::face);
             smemCellFn_ = &SmemLayout32<D, H, NPL>::cell;
         } else {
             smemFaceFn_ = &SmemLayout<S, D, H, NPL>::face;
@@ -382,7 +399,8 @@ private:
     size_t smemCell(const TileDims& d) const { return smemCellFn_(d); }
 
     int D_ = 2, npl_ = 1, ctas_ = 1;
-    bool gather_ = false;
+    bool gather_ = false, pipeA_ = false, sides_ = false;
+    KernelFn kMacros_ = nullptr;
     int gatherMF_ = 0, gatherBlocks_ = 1;
     void (*kGather_)(FusedArgs<S>, int) = nullptr;
     bool H_ = true;

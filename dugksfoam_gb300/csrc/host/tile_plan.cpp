@@ -31,7 +31,7 @@ struct Sets {
     explicit Sets(int nC) : mark(nC, -1) {}
     bool in(int c) const { return mark[c] >= stamp * 3 && mark[c] <= stamp * 3 + 2; }
     bool inT(int c) const { return mark[c] == stamp * 3; }
-    void build(const Mesh& m, const int* cells, int n) {
+    void build(const Mesh& m, const int* cells, int n, int rings) {
         ++stamp;
         lc.assign(cells, cells + n);
         for (int i = 0; i < n; ++i) mark[cells[i]] = stamp * 3;
@@ -50,7 +50,7 @@ struct Sets {
         };
         ring(0, nT, 1);
         nT1 = (int)lc.size();
-        ring(nT, nT1, 2);
+        if (rings == 2) ring(nT, nT1, 2);
         nT2 = (int)lc.size();
         nFA = nFB = nEnt = 0;
         for (int i = 0; i < nT; ++i) {
@@ -61,7 +61,8 @@ struct Sets {
                 else if (!inT(m.owner[f])) ++nFB;
             }
         }
-        for (int i = 0; i < nT1; ++i) nEnt += m.cellOff[lc[i] + 1] - m.cellOff[lc[i]];
+        const int nSt = rings == 2 ? nT1 : nT;  // cells with a stencil
+        for (int i = 0; i < nSt; ++i) nEnt += m.cellOff[lc[i] + 1] - m.cellOff[lc[i]];
     }
 };
 
@@ -96,7 +97,8 @@ void rcb(const Mesh& m, std::vector<int>& cells, int b, int e, int N, std::vecto
 }  // namespace
 
 bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t budget, TilePlan& p,
-                     std::string& err) {
+                     std::string& err, int rings) {
+    if (rings != 1 && rings != 2) { err = "tile plan: rings must be 1 or 2"; return false; }
     const int nC = m.nC, nI = m.nI;
     if (maxTileCells < 1) { err = "tile size must be positive"; return false; }
     p = TilePlan();
@@ -111,7 +113,7 @@ bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t
     auto fits = [&](int N) {
         partition(N);
         for (auto& pr : parts) {
-            S.build(m, cells.data() + pr.first, pr.second - pr.first);
+            S.build(m, cells.data() + pr.first, pr.second - pr.first, rings);
             if (smem(S.d) > budget) return false;
         }
         return true;
@@ -128,7 +130,7 @@ bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t
     std::vector<int> loc(nC, -1);
     int t = 0;
     for (auto& pr : parts) {
-        S.build(m, cells.data() + pr.first, pr.second - pr.first);
+        S.build(m, cells.data() + pr.first, pr.second - pr.first, rings);
         // ---- emit the tile
         TileHdr h{};
         const std::vector<int>& lc = S.lc;
@@ -140,9 +142,10 @@ bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t
             loc[lc[i]] = i;
             p.cells.push_back(lc[i]);
         }
-        // stencils of T u H1, entries in global face order
+        // stencils of T u H1 (rings = 2) or T (rings = 1), entries in global face order
+        const int nSt = rings == 2 ? h.nT1 : h.nT;
         h.stStart = (int)p.stOff.size();
-        for (int i = 0; i < h.nT1; ++i) {
+        for (int i = 0; i < nSt; ++i) {
             const int c = lc[i];
             p.stOff.push_back((int)p.stEnt.size());
             for (int j = m.cellOff[c]; j < m.cellOff[c + 1]; ++j) {
@@ -201,10 +204,11 @@ bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t
                 err = "tile plan: face cell outside T u H1";
                 return false;
             }
-            r.stO0 = p.stOff[h.stStart + r.ownL];
-            r.stO1 = p.stOff[h.stStart + r.ownL + 1];
-            r.stN0 = r.neiL >= 0 ? p.stOff[h.stStart + r.neiL] : 0;
-            r.stN1 = r.neiL >= 0 ? p.stOff[h.stStart + r.neiL + 1] : 0;
+            const bool stO = r.ownL < nSt, stN = r.neiL >= 0 && r.neiL < nSt;
+            r.stO0 = stO ? p.stOff[h.stStart + r.ownL] : 0;
+            r.stO1 = stO ? p.stOff[h.stStart + r.ownL + 1] : 0;
+            r.stN0 = stN ? p.stOff[h.stStart + r.neiL] : 0;
+            r.stN1 = stN ? p.stOff[h.stStart + r.neiL + 1] : 0;
             p.faces.push_back(r);
         }
         // greedy colouring: faces of one colour touch distinct cells of T

@@ -61,7 +61,12 @@ using SmemFn = std::function<size_t(const TileDims&)>;
 
 // Build the plan: compact BFS tiles of at most maxTileCells cells, each the
 // largest that fits `budget` bytes of shared memory.
+//
+// rings = 2: rows of T u H1 u H2, stencils of T u H1 (a face's two upwind
+// candidates both have their gradients in the tile).  rings = 1: rows of
+// T u H1, stencils of T only (nT2 == nT1); a face's stencil range is set for
+// the sides whose cell is in T and empty otherwise.
 bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t budget, TilePlan& p,
-                     std::string& err);
+                     std::string& err, int rings = 2);
 
 }  // namespace dugks
