@@ -13,7 +13,11 @@ FP32-bulk / FP64-moment fused pipeline.  A "step" is one fvDVM::evolution()
              the engine: per step dugks_get_conum (D2H), dugks_set_dt (H2D),
              dugks_step, dugks_get_macros into pinned host buffers (D2H)
   fp64_plain the plain FP64 pipeline on the same workload (fewer steps)
-  roofline   the dominant kernel (k_sweep_cell) against measured HBM bandwidth
+  roofline   the dominant kernel against measured HBM bandwidth: its
+             algorithmic bytes (each array it reads or writes touched once)
+             per launch over its CUDA-event launch time; step_frac is the
+             whole step against the compulsory state traffic (read and write
+             g~,h~ once: 16 B per cell*DV in FP32 with h, 8 B without)
   cpu_baseline the FP64 CPU oracle (a restatement of the reference step) on a
              bounded sample of the same workload, all host threads
 
@@ -38,7 +42,18 @@ sys.path.insert(0, ROOT)
 
 METRIC = "cell*DV updates/s FP32+FP64-moment vs plain FP64, same GB300, <=1e-5 rel err"
 UNIT = "cell*DV updates/s"
-ALG_BYTES = {"k_sweep_cell": 16, "k_sweep_face": 8}  # FP32 g,h per cell*DV: read (+write)
+
+
+def alg_bytes(info):
+    """Algorithmic bytes per launch of each FP32 kernel (each array read or
+    written once): k_face_sides reads g~,h~ of every cell and writes the face
+    values of every active face; k_cell_gather reads g~,h~ and the face values
+    and writes g~new,h~new; k_face_macros moves O(faces) side data."""
+    nd = 2 if info["has_h"] else 1
+    V = info["n_dv"]
+    nC, nA = info["n_cells"], info["n_internal_faces"] + info["n_wall_faces"]
+    return {"k_face_sides": 4 * nd * V * (nC + nA), "k_cell_gather": 4 * nd * V * (2 * nC + nA),
+            "k_face_macros": nA * (2 * 16 * 8 + 160)}
 
 
 def _peaks():
@@ -51,7 +66,10 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 10 ms by one
+    nvidia-smi process that runs across the timed region; mark() brackets the
+    region and summary() keeps the samples inside it (or the nearest one on
+    each side when the region is shorter than the sampling period)."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -59,39 +77,68 @@ class ClockSampler:
 
     def __init__(self, index=0):
         self.index = index
-        self.samples = []
-        self._stop = threading.Event()
+        self.samples = []  # (time, fields)
+        self.t0 = self.t1 = None
+        self._p = None
         self._t = None
 
     def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if out.returncode == 0 and out.stdout.strip():
-                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        for line in self._p.stdout:
+            f = [x.strip() for x in line.strip().split(",")]
+            if len(f) == 7:
+                self.samples.append((time.perf_counter(), f))
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                        "--format=csv,noheader,nounits", "-lms", "10"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._run, daemon=True)
+            self._t.start()
+            deadline = time.perf_counter() + 5.0
+            while not self.samples and time.perf_counter() < deadline:
+                time.sleep(0.01)
+        except Exception:
+            self._p = None
         return self
 
+    def mark(self, start):
+        if start:
+            self.t0 = time.perf_counter()
+        else:
+            self.t1 = time.perf_counter()
+            time.sleep(0.05)  # let the sample after the region arrive
+
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self._p is not None:
+            self._p.terminate()
+            try:
+                self._p.wait(timeout=5)
+            except Exception:
+                self._p.kill()
+        if self._t is not None:
+            self._t.join(timeout=5)
 
     def summary(self):
-        if not self.samples:
+        smp = self.samples
+        if self.t0 is not None and self.t1 is not None and smp:
+            inside = [s for t, s in smp if self.t0 <= t <= self.t1]
+            if not inside:
+                before = [s for t, s in smp if t < self.t0][-1:]
+                after = [s for t, s in smp if t > self.t1][:1]
+                inside = before + after
+            smp = inside
+        else:
+            smp = [s for _, s in smp]
+        if not smp:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        num = lambda x: x.replace(".", "", 1).isdigit()
+        sm = [float(s[0]) for s in smp if num(s[0])]
+        mx = [float(s[1]) for s in smp if num(s[1])]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower().startswith("active")})
+        reasons = sorted({names[i] for s in smp for i in range(4) if s[3 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "reasons": reasons, "samples": len(smp)}
 
 
 def _dist():
@@ -209,10 +256,12 @@ def run_engine(args):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk, torch.cuda.stream(stream):
+        clk.mark(True)
         e0.record(stream)
         s.evolution(args.steps)
         e1.record(stream)
         e1.synchronize()
+        clk.mark(False)
     torch.cuda.synchronize()
     _barrier(world)
     ms = e0.elapsed_time(e1)
@@ -260,13 +309,14 @@ def run_engine(args):
         return
     peak, peak_kind = _peaks()
     dom = max(prof, key=prof.get)
-    alg = ALG_BYTES.get(dom, 16) * n_upd
-    achieved = alg / (prof[dom] / 1e3) / 1e9
+    alg = alg_bytes(info)
+    achieved = alg[dom] / (prof[dom] / 1e3) / 1e9
+    step_bytes = 4 * (2 if info["has_h"] else 1) * 2  # read + write g~(,h~) once, FP32
     traffic = None
     tfile = os.path.join(ROOT, "profiles", "traffic_per_cell_dv.json")
-    if os.path.exists(tfile):
+    if os.path.exists(tfile):  # ncu DRAM bytes per cell*DV of each kernel (small-case capture)
         try:
-            tb = json.load(open(tfile)).get(dom)
+            tb = json.load(open(tfile)).get(args.workload, {}).get(dom)
             traffic = tb * n_upd if tb else None
         except Exception:
             traffic = None
@@ -280,8 +330,9 @@ def run_engine(args):
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
-                     "alg_bytes_per_cell_dv": ALG_BYTES.get(dom, 16),
-                     "step_frac": sum(ALG_BYTES.values()) * value / world / 1e9 / peak},
+                     "alg_bytes": alg[dom],
+                     "step_bytes_per_cell_dv": step_bytes,
+                     "step_frac": step_bytes * value / world / 1e9 / peak},
         "kernels_ms": prof,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 8, "d2h_bytes_per_step": d2h},
         "gpu_launches": s.launches_per_step() * args.steps,

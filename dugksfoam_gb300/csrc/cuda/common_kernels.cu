@@ -50,13 +50,39 @@ __global__ void k_import(StepArgs a, const double* src, S* dst, double scale) {
     }
 }
 
-__global__ void k_conum(StepArgs a, const double* dcI, double xi_max, double* out) {
+// Deterministic two-stage reductions over all SMs: kRedBlocks fixed blocks
+// write partials, one block adds them in a fixed order.
+constexpr int kRedBlocks = 128, kRedThreads = 256;
+
+template <int N>
+__global__ void k_reduce_partials(const double* part, int nmax, double* out) {
+    __shared__ double red[32 * N];
+    double s[N];
+    double mx = 0.0;
+    for (int i = 0; i < N; ++i) s[i] = threadIdx.x < kRedBlocks ? part[threadIdx.x * (N + 1) + i] : 0.0;
+    if (threadIdx.x < kRedBlocks && nmax) mx = part[threadIdx.x * (N + 1) + N];
+    block_sum<N>(s, red);
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ double redm[32];
+    if ((threadIdx.x & 31) == 0) redm[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = fmax(m, redm[i]);
+        if (nmax) out[0] = m;
+        for (int i = 0; i < N; ++i) out[nmax + i] = s[i];
+    }
+}
+
+// fvDVM::getCoNum (fvDVM.C:1111-1119): per internal face deltaCoeff * (|U_f| + sqrt(D) xi_max);
+// partial {sum, max} per block.
+__global__ void k_conum(StepArgs a, const double* dcI, double xi_max, double* part) {
     __shared__ double red[32];
     __shared__ double redm[32];
     double s[1] = {0.0};
     double mx = 0.0;
     const double sq = sqrt((double)a.D) * xi_max;
-    for (int f = threadIdx.x; f < a.nI; f += blockDim.x) {
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.nI; f += gridDim.x * blockDim.x) {
         double ux = a.UF[3 * f], uy = a.UF[3 * f + 1], uz = a.UF[3 * f + 2];
         double u = dcI[f] * (sqrt(ux * ux + uy * uy + uz * uz) + sq);
         s[0] += u;
@@ -69,16 +95,17 @@ __global__ void k_conum(StepArgs a, const double* dcI, double xi_max, double* ou
     if (threadIdx.x == 0) {
         double m = 0.0;
         for (int i = 0; i < (int)(blockDim.x >> 5); ++i) m = fmax(m, redm[i]);
-        out[0] = m;
-        out[1] = s[0];
+        part[blockIdx.x * 2] = s[0];
+        part[blockIdx.x * 2 + 1] = m;
     }
 }
 
 // dugksFoam.C:88-107 residuals; then the "old" fields take the current ones.
-__global__ void k_residual(StepArgs a, double* Uo, double* To, double* ro, double* out) {
+// Partial sums per block.
+__global__ void k_residual(StepArgs a, double* Uo, double* To, double* ro, double* part) {
     __shared__ double red[32 * 6];
     double s[6] = {0, 0, 0, 0, 0, 0};
-    for (int c = threadIdx.x; c < a.nC; c += blockDim.x) {
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.nC; c += gridDim.x * blockDim.x) {
         double dx = a.U[3 * c] - Uo[3 * c], dy = a.U[3 * c + 1] - Uo[3 * c + 1], dz = a.U[3 * c + 2] - Uo[3 * c + 2];
         s[0] += sqrt(dx * dx + dy * dy + dz * dz);
         s[1] += sqrt(a.U[3 * c] * a.U[3 * c] + a.U[3 * c + 1] * a.U[3 * c + 1] + a.U[3 * c + 2] * a.U[3 * c + 2]);
@@ -86,16 +113,13 @@ __global__ void k_residual(StepArgs a, double* Uo, double* To, double* ro, doubl
         s[3] += a.T[c];
         s[4] += fabs(a.rho[c] - ro[c]);
         s[5] += a.rho[c];
-    }
-    block_sum<6>(s, red);
-    __syncthreads();
-    for (int c = threadIdx.x; c < a.nC; c += blockDim.x) {
         Uo[3 * c] = a.U[3 * c]; Uo[3 * c + 1] = a.U[3 * c + 1]; Uo[3 * c + 2] = a.U[3 * c + 2];
         To[c] = a.T[c];
         ro[c] = a.rho[c];
     }
+    block_sum<6>(s, red);
     if (threadIdx.x == 0)
-        for (int i = 0; i < 6; ++i) out[i] = s[i];
+        for (int i = 0; i < 6; ++i) part[blockIdx.x * 7 + i] = s[i];
 }
 
 }  // namespace
@@ -112,11 +136,17 @@ template <typename S>
 void launch_import_dist(const StepArgs& a, const double* src, S* dst, double scale, int sms, cudaStream_t s) {
     k_import<S><<<grid_for((long long)a.nC * a.nV, 256, sms), 256, 0, s>>>(a, src, dst, scale);
 }
+// out: {max, sum}; scratch: kRedBlocks * 2 doubles past out + 8
 void launch_conum(const StepArgs& a, const double* dcI, double xi_max, double* out, cudaStream_t s) {
-    k_conum<<<1, 1024, 0, s>>>(a, dcI, xi_max, out);
+    double* part = out + 8;
+    k_conum<<<kRedBlocks, kRedThreads, 0, s>>>(a, dcI, xi_max, part);
+    k_reduce_partials<1><<<1, kRedBlocks, 0, s>>>(part, 1, out);
 }
+// out: 6 sums; scratch: kRedBlocks * 7 doubles past out + 8
 void launch_residual(const StepArgs& a, double* Uo, double* To, double* ro, double* out, cudaStream_t s) {
-    k_residual<<<1, 1024, 0, s>>>(a, Uo, To, ro, out);
+    double* part = out + 8;
+    k_residual<<<kRedBlocks, kRedThreads, 0, s>>>(a, Uo, To, ro, part);
+    k_reduce_partials<6><<<1, kRedBlocks, 0, s>>>(part, 0, out);
 }
 
 template void launch_init_state<double>(const StepArgs&, double*, double*, double, int, cudaStream_t);

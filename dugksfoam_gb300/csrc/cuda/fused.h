@@ -35,17 +35,6 @@ public:
 
 // DVs per lane of the fused kernels for a precision (FP32: DUGKS_NPL, default 4).
 int fused_npl(int precision);
-// Resident tiles per SM for the FP32 sweeps (DUGKS_CTAS = 1 or 2).
-int fused_ctas_per_sm();
-// FP32 sweep B in gather form (one warp per cell over stored face values;
-// DUGKS_CELL_SWEEP=tiled selects the tiled scatter form).
-bool fused_cell_gather();
-// FP32 sweep A streams the next DV chunk's rows into a second shared buffer
-// (DUGKS_SWEEPA_PIPE=0 selects the single-buffer form).
-bool fused_face_pipe();
-// FP32 sweep A on one-ring tiles, each face side reconstructed by the tile of
-// its cell (DUGKS_SWEEPA=owned selects two-ring tiles with owned faces).
-bool fused_face_sides();
 // DV chunk granularity the fused kernels need (the padded DV count must be a multiple).
 int fused_dv_granule(int precision);
 

@@ -1,14 +1,21 @@
-// FP32 fused sweeps (fast path).  Same two-sweep algorithm as fused_kernels.cuh
-// (see fused_impl.cuh for the pass-by-pass mapping to the reference), with
-// three changes that matter on GB300:
+// FP32 step (fast path): three launches per step.
 //
-//  * each lane owns NPL consecutive discrete velocities (vector loads and
-//    stores of g~ rows; one warp task covers KC = 32*NPL velocities), so the
-//    per-face and per-row fixed costs -- metadata loads, the warp
-//    reduce-scatter of the moments -- are paid once per KC velocities;
-//  * the upwind side is chosen per velocity inside a single stencil loop (both
-//    sides' rows are read, one gradient is formed), so warps never run the
-//    owner- and neighbour-side reconstructions as divergent paths;
+//  k_face_sides32  (tiles of cells T with a one-ring halo H1, DV chunks of
+//                   KC = 32*NPL velocities): gbar+ rows of T u H1 (P1), the
+//                   least-squares gradient of each T cell (P2) and the upwind
+//                   reconstruction of every face side whose cell is in T (P3),
+//                   lagged wall gradients, stored face values and per-side
+//                   face moments;
+//  k_face_macros32 (one thread per face): Maxwell-wall density (P4), incoming
+//                   wall moments (P5), face macros and equilibrium tables (P6);
+//  k_cell_gather32 (one warp per cell): face relaxation (P7), flux sum and
+//                   g~ update (P8), cell moments and macros (P9).
+//
+// Layout and arithmetic choices:
+//  * each lane owns NPL consecutive discrete velocities held as NPL/2 packed
+//    float2 pairs (f32x2 FMA/ADD/MUL), so every per-velocity operation is one
+//    packed instruction per pair and the per-face fixed costs (metadata, the
+//    warp reduce-scatter of the moments) are paid once per KC velocities;
 //  * the distributions are stored as deviations from a fixed rest Maxwellian:
 //      G = gscale * g - Mref(xi),   Mref = exp(-|xi|^2 / (2 R T0)),
 //    gscale = (2 pi R T0)^(D/2) / rho0 (h likewise with Href = Mref R T0 (K+3-D)).
@@ -19,6 +26,9 @@
 //    O(1) distribution cuts the FP32 storage rounding by the same factor.
 //    (The Mref part of the face flux, Mref xi.sum_f(+-S_f), vanishes for a
 //    closed cell and is not formed.)
+//  * no FP64 instruction runs inside the DV chunk loops (GB300 issues FP64 at
+//    1/64 of the FP32 rate): per-chunk warp totals go into FP32 Kahan pairs
+//    and are finished in FP64, batched so that whole warps do the FP64 work.
 #pragma once
 
 #include "fused_impl.cuh"
@@ -53,18 +63,7 @@ __device__ __forceinline__ void stp(float* p, const float2 (&d)[NP]) {
     if constexpr (NP == 2) *reinterpret_cast<float4*>(p) = make_float4(d[0].x, d[0].y, d[1].x, d[1].y);
     else *reinterpret_cast<float2*>(p) = d[0];
 }
-// Streaming (evict-first) access for the g~ rows: they are touched once per
-// sweep, so they should not push the tile's metadata out of L1.
-template <int NP>
-__device__ __forceinline__ void ldp_cs(float2 (&d)[NP], const float* p) {
-    if constexpr (NP == 2) {
-        const float4 t = __ldcs(reinterpret_cast<const float4*>(p));
-        d[0] = make_float2(t.x, t.y);
-        d[1] = make_float2(t.z, t.w);
-    } else {
-        d[0] = __ldcs(reinterpret_cast<const float2*>(p));
-    }
-}
+// Streaming (evict-first) store of the g~new rows: written once, read next step.
 template <int NP>
 __device__ __forceinline__ void stp_cs(float* p, const float2 (&d)[NP]) {
     if constexpr (NP == 2) __stcs(reinterpret_cast<float4*>(p), make_float4(d[0].x, d[0].y, d[1].x, d[1].y));
@@ -82,31 +81,18 @@ __host__ __device__ constexpr int tile_meta32_bound(int nFB, int nEnt, int nT2) 
     return 5 * nFB + nEnt + (nT2 + 3) / 4 + (nFB + 3) / 4 + 17;
 }
 
-// Shared memory of the FP32 sweeps (all offsets multiples of 16 bytes):
-//   sweep A: NB x rows(T u H1 u H2) | face moments | metadata | face Uref | cell equilibria
-//   sweep B: rows(T u H1 u H2) | rows(T) | cell moments | metadata | face equilibria | cell equilibria
-// (NB = 2: the next chunk's rows stream into the second buffer.)
-template <int D, bool H, int NPL, int NB = 1>
+// Shared memory of the face-sides sweep (all offsets multiples of 16 bytes):
+//   2 x rows(T u H1) | face moments | metadata | face Uref | cell equilibria
+// (the next DV chunk's raw rows stream into the second row buffer).
+template <int D, bool H, int NPL>
 struct SmemLayout32 {
     static constexpr int KC = 32 * NPL, NS = Slots<D, H>::NS;
     __host__ __device__ static size_t rows(int n) { return (size_t)n * KC * sizeof(float) * (H ? 2 : 1); }
-    __host__ __device__ static size_t metaA(int nT2, int nFA) {
-        return NB * rows(nT2) + (size_t)nFA * NS * sizeof(Acc<float>);
+    __host__ __device__ static size_t meta(int nRows, int nF) {
+        return 2 * rows(nRows) + (size_t)nF * NS * sizeof(Acc<float>);
     }
-    __host__ __device__ static size_t metaB(int nT2, int nT) {
-        return rows(nT2) + rows(nT) + (size_t)nT * NS * sizeof(Acc<float>);
-    }
-    static size_t face(const TileDims& d) {
-        return metaA(d.nT2, d.nFA) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 16 * (size_t)d.nFA +
-               48 * (size_t)d.nT2;
-    }
-    static size_t cell(const TileDims& d) {
-        return metaB(d.nT2, d.nT) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 48 * (size_t)d.nFB +
-               48 * (size_t)d.nT2;
-    }
-    // one-ring face-sides sweep: every face of T carries moments and a Uref
     static size_t sides(const TileDims& d) {
-        return metaA(d.nT2, d.nFB) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 16 * (size_t)d.nFB +
+        return meta(d.nT2, d.nFB) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 16 * (size_t)d.nFB +
                48 * (size_t)d.nT2;
     }
 };
@@ -257,61 +243,6 @@ __device__ __forceinline__ void relax_rows32(const FusedArgs<float>& A, const Ti
         }
         stp<NP>(sg + r * KC + lane * NPL, g);
         if (H) stp<NP>(sh + r * KC + lane * NPL, h);
-    }
-}
-
-// gbar+ rows of T u H1 u H2 (and for sweep B the g~new partial of T's rows).
-// Two rows per warp iteration keep two row loads in flight.
-template <int D, bool H, int NPL, bool PART>
-__device__ __forceinline__ void row32(const TileHdr& hd, const Lane32<D, NPL>& L, int lc, const float2* g0,
-                                      const float2* h0, const Eq32<D, H>& eq, int lane, float* sg, float* sh,
-                                      float* sa, float* sah) {
-    constexpr int KC = 32 * NPL, NP = NPL / 2;
-    float2 g[NP], h[NP];
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-        g[p] = g0[p];
-        h[p] = H ? h0[p] : f2(0.0f);
-        eq.relax(L, p, g[p], h[p]);
-    }
-    stp<NP>(sg + lc * KC + lane * NPL, g);
-    if (H) stp<NP>(sh + lc * KC + lane * NPL, h);
-    if (PART && lc < hd.nT) {  // g+ + (g+ - g~)/3: exact when g+ == g~ (no FP32 mass bias)
-        float2 pa[NP], ph[NP];
-#pragma unroll
-        for (int p = 0; p < NP; ++p) {
-            pa[p] = fma2(sub2(g[p], g0[p]), f2(1.0f / 3.0f), g[p]);
-            if (H) ph[p] = fma2(sub2(h[p], h0[p]), f2(1.0f / 3.0f), h[p]);
-        }
-        stp<NP>(sa + lc * KC + lane * NPL, pa);
-        if (H) stp<NP>(sah + lc * KC + lane * NPL, ph);
-    }
-}
-
-template <int D, bool H, int NPL, int NW, bool PART>
-__device__ __forceinline__ void rows32(const FusedArgs<float>& A, const TileHdr& hd, const TileMeta32& tm,
-                                       const float4* ceq, const Lane32<D, NPL>& L, int v0, int lane, int warp,
-                                       float* sg, float* sh, float* sa, float* sah) {
-    constexpr int NP = NPL / 2;
-    const int Vp = A.b.Vp;
-    for (int l0 = warp; l0 < hd.nT2; l0 += 2 * NW) {
-        const int l1 = l0 + NW;
-        const bool two = l1 < hd.nT2;
-        const int c0 = tm.C[l0];
-        const int c1 = two ? tm.C[l1] : c0;
-        const size_t i0 = (size_t)c0 * Vp + v0 + lane * NPL, i1 = (size_t)c1 * Vp + v0 + lane * NPL;
-        float2 ga[NP], ha[NP], gb[NP], hb[NP];
-        ldp_cs<NP>(ga, A.gT + i0);
-        ldp_cs<NP>(gb, A.gT + i1);
-        if (H) {
-            ldp_cs<NP>(ha, A.hT + i0);
-            ldp_cs<NP>(hb, A.hT + i1);
-        }
-        Eq32<D, H> e0, e1;
-        e0.load(ceq + 3 * l0, A.b.K, A.hrefFac);
-        e1.load(ceq + 3 * (two ? l1 : l0), A.b.K, A.hrefFac);
-        row32<D, H, NPL, PART>(hd, L, l0, ga, ha, e0, lane, sg, sh, sa, sah);
-        if (two) row32<D, H, NPL, PART>(hd, L, l1, gb, hb, e1, lane, sg, sh, sa, sah);
     }
 }
 
@@ -574,118 +505,6 @@ __device__ __forceinline__ void finalize_face32(const FusedArgs<float>& A, int a
         }
 }
 
-// ---------------------------------------------------------------- sweep A
-template <int D, bool H, int NPL, int NW, bool PIPE>
-__global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_face32(FusedArgs<float> A) {
-    using SL = Slots<D, H>;
-    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
-    extern __shared__ __align__(16) unsigned char smem[];
-    const TileHdr hd = A.hdr[blockIdx.x];
-    const StepArgs& b = A.b;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int Vp = b.Vp;
-    using LY = SmemLayout32<D, H, NPL, PIPE ? 2 : 1>;
-    float* sg = reinterpret_cast<float*>(smem);
-    float* sh = sg + (size_t)hd.nT2 * KC;
-    const size_t bufStride = LY::rows(hd.nT2) / sizeof(float);  // second row buffer (PIPE)
-    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + (PIPE ? 2 : 1) * LY::rows(hd.nT2));
-    for (int i = threadIdx.x; i < hd.nFA * NS; i += NW * 32) mom[i].zero();
-    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::metaA(hd.nT2, hd.nFA));
-    float4* sU = tm.dyn;             // [nFA] face Uref
-    float4* ceq = tm.dyn + hd.nFA;   // [nT2][3] cell equilibria
-    __syncthreads();
-    for (int i = threadIdx.x; i < hd.nFA; i += NW * 32) sU[i] = A.uref4[tm.F[5 * i].z];
-    for (int i = threadIdx.x; i < hd.nT2; i += NW * 32) {
-        const float* blk = A.cc + (size_t)tm.C[i] * kNCoef;
-        eq_table(ceq + 3 * i, blk, cell_weight(A.dt, blk));
-    }
-    const int nChunks = Vp / KC;
-    const int myslot = slot_of<NS>(lane);
-    const bool writer = NS == 16 ? (lane & 1) == 0 : true;
-
-    if (PIPE) {
-        __syncthreads();  // cell ids staged
-        issue_rows32<NPL, H, NW * 32>(A, hd, tm.C, sg, sh, 0);
-    }
-    for (int ch = 0; ch < nChunks; ++ch) {
-        const int v0 = ch * KC;
-        Lane32<D, NPL> L;
-        L.load(A, v0, lane);
-        float* cg = sg;
-        float* chh = sh;
-        if (PIPE) {
-            // chunk ch's raw rows landed in buffer ch&1; the other buffer's
-            // faces (chunk ch-1) are done, so chunk ch+1 streams into it
-            cp_async_wait<0>();
-            __syncthreads();
-            cg = sg + (ch & 1) * bufStride;
-            chh = sh + (ch & 1) * bufStride;
-            if (ch + 1 < nChunks)
-                issue_rows32<NPL, H, NW * 32>(A, hd, tm.C, sg + ((ch + 1) & 1) * bufStride,
-                                              sh + ((ch + 1) & 1) * bufStride, v0 + KC);
-            relax_rows32<D, H, NPL, NW>(A, hd, ceq, L, lane, warp, cg, chh);
-        } else {
-            __syncthreads();
-            rows32<D, H, NPL, NW, false>(A, hd, tm, ceq, L, v0, lane, warp, sg, sh, nullptr, nullptr);
-        }
-        __syncthreads();
-        for (int lf = warp; lf < hd.nFA; lf += NW) {
-            Face32 F;
-            F.load(tm.F + 5 * lf);
-            const float4 u4 = sU[lf];
-            const float ur[3] = {u4.x, u4.y, u4.z};
-            float2 xs[NP];
-#pragma unroll
-            for (int p = 0; p < NP; ++p) xs[p] = F.xs<D, NPL>(L, p);
-            float2 gf[NP], hf[NP], gw[D][NP], hw[D][NP];
-            float m[NS];
-#pragma unroll
-            for (int s = 0; s < NS; ++s) m[s] = 0.0f;
-            if (F.r.w >= 0) {
-                recon32<D, H, NPL, true>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
-                float2 gn[NP], hn[NP], use[NP];
-                float fl = 0.0f;
-#pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    gn[p] = fma2(gw[1][p], f2(F.dNy), mul2(gw[0][p], f2(F.dNx)));
-                    if (D == 3) gn[p] = fma2(gw[2][p], f2(F.dNz), gn[p]);
-                    if (H) {
-                        hn[p] = fma2(hw[1][p], f2(F.dNy), mul2(hw[0][p], f2(F.dNx)));
-                        if (D == 3) hn[p] = fma2(hw[2][p], f2(F.dNz), hn[p]);
-                    }
-                    use[p] = make_float2(xs[p].x > 0.f ? 1.f : 0.f, xs[p].y > 0.f ? 1.f : 0.f);
-                    const float2 fx = mul2(mul2(mul2(L.w[p], xs[p]), gf[p]), use[p]);
-                    fl += fx.x + fx.y;
-                }
-                m[SL::FLUX] = fl;
-                const size_t wi = (size_t)F.r.w * Vp + v0 + lane * NPL;
-                stp<NP>(A.Gbgn + wi, gn);
-                if (H) stp<NP>(A.Gbhn + wi, hn);
-                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
-            } else {
-                recon32<D, H, NPL, false>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
-                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
-            }
-            if (A.gF) {
-                const size_t fi = (size_t)F.r.a * Vp + v0 + lane * NPL;
-                stp<NP>(A.gF + fi, gf);
-                if (H) stp<NP>(A.hF + fi, hf);
-            }
-            const float tot = reduce_scatter<NS, float>(m, lane);
-            if (writer && myslot <= SL::FLUX) mom[lf * NS + myslot].add(tot);
-        }
-    }
-    __syncthreads();
-    // ---- finalize owned faces (FP64)
-    for (int lf = threadIdx.x; lf < hd.nFA; lf += NW * 32) {
-        const int4 rr = tm.F[5 * lf];
-        const float4 u4 = sU[lf];
-        double M[NS];
-        for (int s = 0; s < NS; ++s) M[s] = mom[lf * NS + s].value();
-        finalize_face32<D, H>(A, rr.z, rr.w, u4, M);
-    }
-}
-
 // ---------------------------------------------------------------- sweep A, face sides
 // One-sided upwind reconstruction from cell u (local row lu, stencil entries
 // [e0,e1) of u, d = Cf - C_u): val = gbar+_u + sum_e L_e.(d - xi dt/2) (gbar+_e - gbar+_u).
@@ -734,13 +553,13 @@ __global__ void __launch_bounds__(NW * 32, 1) k_face_sides32(FusedArgs<float> A)
     const StepArgs& b = A.b;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Vp = b.Vp, col = lane * NPL;
-    using LY = SmemLayout32<D, H, NPL, 2>;
+    using LY = SmemLayout32<D, H, NPL>;
     float* sg = reinterpret_cast<float*>(smem);
     float* sh = sg + (size_t)hd.nT2 * KC;
     const size_t bufStride = LY::rows(hd.nT2) / sizeof(float);
     Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + 2 * LY::rows(hd.nT2));
     for (int i = threadIdx.x; i < hd.nFB * NS; i += NW * 32) mom[i].zero();
-    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::metaA(hd.nT2, hd.nFB));
+    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::meta(hd.nT2, hd.nFB));
     float4* sU = tm.dyn;            // [nFB] face Uref
     float4* ceq = tm.dyn + hd.nFB;  // [nT2][3] cell equilibria
     __syncthreads();
@@ -863,160 +682,6 @@ __global__ void k_face_macros32(FusedArgs<float> A) {
     }
 }
 
-// ---------------------------------------------------------------- sweep B
-template <int D, bool H, int NPL, int NW>
-__global__ void __launch_bounds__(NW * 32, 16 / NW) k_sweep_cell32(FusedArgs<float> A) {
-    using SL = Slots<D, H>;
-    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
-    extern __shared__ __align__(16) unsigned char smem[];
-    const TileHdr hd = A.hdr[blockIdx.x];
-    const StepArgs& b = A.b;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int Vp = b.Vp;
-    using LY = SmemLayout32<D, H, NPL>;
-    float* sg = reinterpret_cast<float*>(smem);
-    float* sh = sg + (size_t)hd.nT2 * KC;
-    float* sa = reinterpret_cast<float*>(smem + LY::rows(hd.nT2));
-    float* sah = sa + (size_t)hd.nT * KC;
-    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + LY::rows(hd.nT2) + LY::rows(hd.nT));
-    for (int i = threadIdx.x; i < hd.nT * NS; i += NW * 32) mom[i].zero();
-    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::metaB(hd.nT2, hd.nT));
-    float4* feq = tm.dyn;                // [nFB][3] face equilibria
-    float4* ceq = tm.dyn + 3 * hd.nFB;   // [nT2][3] cell equilibria
-    __syncthreads();
-    for (int i = threadIdx.x; i < hd.nFB; i += NW * 32) {
-        const float* blk = A.fc + (size_t)tm.F[5 * i].z * kNCoef;
-        eq_table(feq + 3 * i, blk, face_weight(A.dt, blk));
-    }
-    for (int i = threadIdx.x; i < hd.nT2; i += NW * 32) {
-        const float* blk = A.cc + (size_t)tm.C[i] * kNCoef;
-        eq_table(ceq + 3 * i, blk, cell_weight(A.dt, blk));
-    }
-    const int nChunks = Vp / KC;
-    const int myslot = slot_of<NS>(lane);
-    const bool writer = NS == 16 ? (lane & 1) == 0 : true;
-    const int col = lane * NPL;
-
-    for (int ch = 0; ch < nChunks; ++ch) {
-        const int v0 = ch * KC;
-        Lane32<D, NPL> L;
-        L.load(A, v0, lane);
-        __syncthreads();
-        rows32<D, H, NPL, NW, true>(A, hd, tm, ceq, L, v0, lane, warp, sg, sh, sa, sah);
-        __syncthreads();
-        for (int ci = 0; ci < hd.nColors; ++ci) {
-            const int k0 = tm.O[ci], k1 = tm.O[ci + 1];
-            for (int k = k0 + warp; k < k1; k += NW) {
-                const int lf = tm.P[k];
-                Face32 F;
-                F.load(tm.F + 5 * lf);
-                Eq32<D, H> eq;
-                eq.load(feq + 3 * lf, A.b.K, A.hrefFac);
-                float2 xs[NP];
-#pragma unroll
-                for (int p = 0; p < NP; ++p) xs[p] = F.xs<D, NPL>(L, p);
-                float2 gf[NP], hf[NP], gw[D][NP], hw[D][NP];
-                if (F.r.w >= 0) {
-                    recon32<D, H, NPL, true>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
-                    const float rws = A.rhoWs[F.r.w], hwf = A.wall4[F.r.w].x;
-                    float2 mw[NP];
-                    ldp<NP>(mw, A.Mw + (size_t)F.r.w * Vp + v0 + col);
-#pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        float2 go = gf[p], ho = H ? hf[p] : f2(0.f);
-                        eq.relax(L, p, go, ho);                       // outgoing: relaxed
-                        const float2 gi = mul2(f2(rws), mw[p]);       // incoming: rho_w Mw, not relaxed
-                        const float2 gin = sub2(gi, L.mr[p]);
-                        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
-                        gf[p] = sel2(o0, o1, go, gin);
-                        if (H) hf[p] = sel2(o0, o1, ho, sub2(mul2(gi, f2(hwf)), mul2(L.mr[p], f2(A.hrefFac))));
-                    }
-                } else {
-                    recon32<D, H, NPL, false>(A, tm.E, F, L, sg, sh, lane, v0, xs, gf, hf, gw, hw);
-#pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        if (!H) hf[p] = f2(0.f);
-                        eq.relax(L, p, gf[p], hf[p]);
-                    }
-                }
-                const bool ownIn = F.r.ownL < hd.nT, neiIn = F.r.neiL >= 0 && F.r.neiL < hd.nT;
-                if (ownIn) {
-                    float2 t[NP], th[NP];
-                    ldp<NP>(t, sa + F.r.ownL * KC + col);
-                    if (H) ldp<NP>(th, sah + F.r.ownL * KC + col);
-#pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        const float2 kx = mul2(xs[p], f2(-A.dt * F.iVo));
-                        t[p] = fma2(kx, gf[p], t[p]);
-                        if (H) th[p] = fma2(kx, hf[p], th[p]);
-                    }
-                    stp<NP>(sa + F.r.ownL * KC + col, t);
-                    if (H) stp<NP>(sah + F.r.ownL * KC + col, th);
-                }
-                if (neiIn) {
-                    float2 t[NP], th[NP];
-                    ldp<NP>(t, sa + F.r.neiL * KC + col);
-                    if (H) ldp<NP>(th, sah + F.r.neiL * KC + col);
-#pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        const float2 kx = mul2(xs[p], f2(A.dt * F.iVn));
-                        t[p] = fma2(kx, gf[p], t[p]);
-                        if (H) th[p] = fma2(kx, hf[p], th[p]);
-                    }
-                    stp<NP>(sa + F.r.neiL * KC + col, t);
-                    if (H) stp<NP>(sah + F.r.neiL * KC + col, th);
-                }
-            }
-            __syncthreads();
-        }
-        for (int lc = warp; lc < hd.nT; lc += NW) {
-            const int c = tm.C[lc];
-            const float4 u4 = ceq[3 * lc];
-            const float ur[3] = {u4.x, u4.y, u4.z};
-            float2 g[NP], h[NP];
-            ldp<NP>(g, sa + lc * KC + col);
-            if (H) ldp<NP>(h, sah + lc * KC + col);
-            else
-#pragma unroll
-                for (int p = 0; p < NP; ++p) h[p] = f2(0.f);
-            const size_t gi = (size_t)c * Vp + v0 + col;
-            stp_cs<NP>(A.gTn + gi, g);
-            if (H) stp_cs<NP>(A.hTn + gi, h);
-            float m[NS];
-#pragma unroll
-            for (int s = 0; s < NS; ++s) m[s] = 0.0f;
-            mom32<D, H, NPL, NS>(m, L, ur, g, h, nullptr);
-            const float tot = reduce_scatter<NS, float>(m, lane);
-            if (writer && myslot < SL::NM) mom[lc * NS + myslot].add(tot);
-        }
-    }
-    __syncthreads();
-    // ---- finalize cells of T (FP64)
-    for (int lc = threadIdx.x; lc < hd.nT; lc += NW * 32) {
-        const int c = tm.C[lc];
-        const float4 u4 = ceq[3 * lc];
-        const double ur[3] = {u4.x, u4.y, u4.z};
-        double M[NS], Rm[NS];
-        for (int s = 0; s < NS; ++s) M[s] = mom[lc * NS + s].value();
-        ref_moments_about<D, H>(A.refMom, ur, Rm);
-        for (int s = 0; s < SL::NM; ++s) M[s] = (M[s] + Rm[s]) * A.invGscale;
-        double rho, U[3], T, tau, qr[3];
-        macros_from_moments<D, H>(M, ur, b, rho, U, T, tau, qr);
-        const double fac = 2.0 * tau / (2.0 * tau + b.dt * b.Pr);
-        double q[3] = {fac * qr[0], fac * qr[1], fac * qr[2]};
-        A.rhoN[c] = rho;
-        A.TN[c] = T;
-        A.tauN[c] = tau;
-        for (int k = 0; k < 3; ++k) { A.UN[3 * c + k] = U[k]; A.qN[3 * c + k] = q[k]; }
-        write_coef<D>(A.ccn + (size_t)c * kNCoef, rho, U, T, q, tau, b, A.gscale);
-        if (!(rho > 0.0) || !(T > 0.0) || !isfinite(U[0] + U[1] + U[2] + q[0] + q[1] + q[2])) atomicExch(b.status, 5);
-    }
-}
-
-// ------------------------------------------------------------ set-up kernels
-// Reference Maxwellian per DV (scaled: exp(-|xi|^2/(2 R T0))), its raw moments
-// (scaled, about the origin) and, per wall face, the reference moments over
-// the outgoing velocities about U_w plus the reference outgoing flux.
 // ---------------------------------------------------------------- sweep B, gather form
 // Shared memory of the gather sweep: per warp two stages of (1 + MF) rows of
 // g (and h): the cell's g~ row and its first MF faces' stored values.
@@ -1197,6 +862,10 @@ __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A
     }
 }
 
+// ------------------------------------------------------------ set-up kernels
+// Reference Maxwellian per DV (scaled: exp(-|xi|^2/(2 R T0))), its raw moments
+// (scaled, about the origin) and, per wall face, the reference moments over
+// the outgoing velocities about U_w plus the reference outgoing flux.
 template <int D, bool H>
 __global__ void k_ref_tables(StepArgs b, double T0, double hrefFac, float* mref, double* refMom, double* wallRefOut) {
     using SL = Slots<D, H>;

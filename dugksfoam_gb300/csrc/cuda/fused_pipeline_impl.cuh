@@ -1,5 +1,7 @@
 // FusedPipelineT<S>: owns the tile plan and the double-buffered state of the
-// fused sweeps; included once per storage type (fused_fp32.cu, fused_fp64.cu).
+// fused step; included once per storage type (fused_fp32.cu, fused_fp64.cu).
+// FP64: two tiled sweeps (fused_kernels.cuh).  FP32: face sides on one-ring
+// tiles, face macros, cell gather (fused32.cuh).
 #pragma once
 
 #include <cmath>
@@ -30,37 +32,30 @@ public:
         H_ = a.hasH != 0;
         if (D_ != 2 && D_ != 3) { err = "fused pipeline supports 2D and 3D meshes"; return false; }
         npl_ = fused_npl(sizeof(S) == 4 ? DUGKS_FP32_FP64MOM : DUGKS_FP64);
-        ctas_ = sizeof(S) == 4 ? fused_ctas_per_sm() : 1;
-        gather_ = sizeof(S) == 4 && fused_cell_gather();
-        pipeA_ = sizeof(S) == 4 && fused_face_pipe();
-        sides_ = gather_ && fused_face_sides();
+        fp32_ = sizeof(S) == 4;
         const int KC = 32 * npl_;
         if (a.Vp % KC != 0) { err = "padded DV count is not a multiple of the DV chunk"; return false; }
         pick();
         // ---- tile plan, sized to the shared-memory budget
         int dev = 0;
         cudaGetDevice(&dev);
-        int maxSmem = 0, smemSM = 0;
+        int maxSmem = 0;
         cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-        cudaDeviceGetAttribute(&smemSM, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-        // ctas_ resident tiles per SM share its shared memory (1 KB per block is reserved)
-        const size_t budget = std::min((size_t)maxSmem, (size_t)smemSM / ctas_ - 1024) - 1024;
+        const size_t budget = (size_t)maxSmem - 2048;
         const char* envT = std::getenv("DUGKS_TILE_CELLS");
         const int maxCells = envT ? std::max(1, std::atoi(envT)) : 4096;
-        const SmemFn fn = [this](const TileDims& d) {
-            return gather_ ? smemFace(d) : std::max(smemFace(d), smemCell(d));  // gather form: no tiles in sweep B
-        };
-        if (!build_tile_plan(m, maxCells, fn, budget, plan_, err, sides_ ? 1 : 2)) return false;
+        // FP32: sweep A alone is tiled (one-ring halo); FP64: both sweeps (two-ring halo)
+        const SmemFn fn = [this](const TileDims& d) { return fp32_ ? smemFace(d) : std::max(smemFace(d), smemCell(d)); };
+        if (!build_tile_plan(m, maxCells, fn, budget, plan_, err, fp32_ ? 1 : 2)) return false;
         smemA_ = smemB_ = 0;
         for (const TileHdr& h : plan_.hdr) {
             TileDims d;
             d.nT = h.nT; d.nT1 = h.nT1; d.nT2 = h.nT2; d.nFA = h.nFA; d.nFB = h.nFB; d.nEnt = h.nEnt;
             smemA_ = std::max(smemA_, smemFace(d));
-            smemB_ = std::max(smemB_, smemCell(d));
+            if (!fp32_) smemB_ = std::max(smemB_, smemCell(d));
         }
         cudaFuncSetAttribute(kFace_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemA_);
-        if (!gather_) cudaFuncSetAttribute(kCell_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
-        else smemB_ = 0;
+        if (!fp32_) cudaFuncSetAttribute(kCell_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
 
         // ---- upload plan
         args_.hdr = upload(plan_.hdr);
@@ -132,7 +127,7 @@ public:
             metaOff.push_back((int)meta.size());
             args_.meta = upload(meta);
             args_.metaOff = upload(metaOff);
-            if (gather_) {
+            {
                 // faces of each cell in global face order, S oriented out of the cell
                 std::vector<int> cfOff(m.nC + 1);
                 std::vector<float4> cfEnt;
@@ -151,10 +146,10 @@ public:
                 cfOff[m.nC] = (int)cfEnt.size();
                 for (int c = 0; c < m.nC; ++c) gatherMF_ = std::max(gatherMF_, cfOff[c + 1] - cfOff[c]);
                 gatherMF_ = std::min(gatherMF_, 8);  // further faces of a cell are read directly
-                smemB_ = gather_smem(kGatherWarps, gatherMF_, KC, H_);
-                cudaFuncSetAttribute(kGather_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
+                gatherSmem_ = gather_smem(kGatherWarps, gatherMF_, KC, H_);
+                cudaFuncSetAttribute(kGather_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gatherSmem_);
                 int per = 0, nsm = 0;
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kGather_, kGatherWarps * 32, smemB_);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kGather_, kGatherWarps * 32, gatherSmem_);
                 cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
                 gatherBlocks_ = std::max(1, per) * std::max(1, nsm);  // persistent: one wave
                 args_.cfOff = upload(cfOff);
@@ -165,7 +160,7 @@ public:
                 args_.gF = alloc<float>((size_t)a.nA * a.Vp);
                 args_.hF = H_ ? alloc<float>((size_t)a.nA * a.Vp) : nullptr;
                 args_.feqT = alloc<float4>(3 * (size_t)a.nA);
-                if (sides_) args_.faceMom = alloc<double>((size_t)a.nA * 2 * 32);
+                args_.faceMom = alloc<double>((size_t)a.nA * 2 * 32);
             }
             std::vector<float4> w4(std::max(a.nW, 1), make_float4(0, 0, 0, 0));
             std::vector<double> Tw(a.nW);
@@ -259,10 +254,10 @@ public:
         if (sizeof(S) == 4) k_face_uref<<<sms * 2, 256, 0, s>>>(a, args_.uref4);
     }
 
-    int nKernels() const override { return sides_ ? 3 : 2; }
+    int nKernels() const override { return fp32_ ? 3 : 2; }
     const char* kernelName(int k) const override {
-        if (sides_) return k == 0 ? "k_face_sides" : (k == 1 ? "k_face_macros" : "k_cell_gather");
-        return k == 0 ? "k_sweep_face" : (gather_ ? "k_cell_gather" : "k_sweep_cell");
+        if (fp32_) return k == 0 ? "k_face_sides" : (k == 1 ? "k_face_macros" : "k_cell_gather");
+        return k == 0 ? "k_sweep_face" : "k_sweep_cell";
     }
 
     void launch(int k, const StepArgs& a, int sms, cudaStream_t s) override {
@@ -276,15 +271,12 @@ public:
         A.Gbgn = Gg_[1 - cur_]; A.Gbhn = Gh_[1 - cur_];
         A.cc = cc_[cur_]; A.ccn = cc_[1 - cur_];
         A.rhoN = rhoN_; A.UN = UN_; A.TN = TN_; A.qN = qN_; A.tauN = tauN_;
-        const int threads = kWarpsPerSM / ctas_ * 32;
-        if (sides_ && k == 1) {
-            kMacros_<<<sms * 4, 128, 0, s>>>(A);
-            return;
-        }
-        if (sides_ && k == 2) k = 1;
-        if (k == 0) kFace_<<<plan_.nTiles, threads, smemA_, s>>>(A);
-        else if (gather_) kGather_<<<std::min((a.nC + kGatherWarps - 1) / kGatherWarps, gatherBlocks_), kGatherWarps * 32, smemB_, s>>>(A, gatherMF_);
-        else kCell_<<<plan_.nTiles, threads, smemB_, s>>>(A);
+        if (k == 0) kFace_<<<plan_.nTiles, kWarps * 32, smemA_, s>>>(A);
+        else if (!fp32_) kCell_<<<plan_.nTiles, kWarps * 32, smemB_, s>>>(A);
+        else if (k == 1) kMacros_<<<sms * 4, 128, 0, s>>>(A);
+        else
+            kGather_<<<std::min((a.nC + kGatherWarps - 1) / kGatherWarps, gatherBlocks_), kGatherWarps * 32, gatherSmem_,
+                       s>>>(A, gatherMF_);
     }
 
     void endStep(StepArgs& base) override {
@@ -323,14 +315,14 @@ public:
     size_t bytes() const override { return bytes_; }
     std::string describe() const override {
         char buf[256];
-        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d ctas=%d gather=%d pipeA=%d sides=%d smemA=%zu smemB=%zu",
+        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d smemA=%zu smemB=%zu gatherMF=%d",
                  plan_.nTiles, plan_.maxT, (double)plan_.sumT / std::max(1, plan_.nTiles),
-                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, ctas_, (int)gather_, (int)pipeA_, (int)sides_, smemA_, smemB_);
+                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, smemA_, smemB_, gatherMF_);
         return buf;
     }
 
 private:
-    static constexpr int kWarpsPerSM = 16;  // split over ctas_ resident tiles
+    static constexpr int kWarps = 16;       // warps per tile block (one tile per SM)
     static constexpr int kGatherWarps = 8;  // warps (cells) per block of the gather sweep
 
     template <typename T>
@@ -353,30 +345,18 @@ private:
     template <int D, bool H, int NPL>
     void set() {
         if constexpr (sizeof(S) == 4) {
-            if (ctas_ == 2) {
-                kFace_ = pipeA_ ? k_sweep_face32<D, H, NPL, kWarpsPerSM / 2, true>
-                                : k_sweep_face32<D, H, NPL, kWarpsPerSM / 2, false>;
-                kCell_ = k_sweep_cell32<D, H, NPL, kWarpsPerSM / 2>;
-            } else {
-                kFace_ = pipeA_ ? k_sweep_face32<D, H, NPL, kWarpsPerSM, true>
-                                : k_sweep_face32<D, H, NPL, kWarpsPerSM, false>;
-                kCell_ = k_sweep_cell32<D, H, NPL, kWarpsPerSM>;
-            }
-            if (gather_) kGather_ = k_cell_gather32<D, H, NPL, kGatherWarps>;
-            if (sides_) {
-                kFace_ = k_face_sides32<D, H, NPL, kWarpsPerSM>;
-                kMacros_ = k_face_macros32<D, H>;
-            }
+            kFace_ = k_face_sides32<D, H, NPL, kWarps>;
+            kMacros_ = k_face_macros32<D, H>;
+            kGather_ = k_cell_gather32<D, H, NPL, kGatherWarps>;
             kRef_ = k_ref_tables<D, H>;
         } else {
-            kFace_ = k_sweep_face<S, D, H, NPL, kWarpsPerSM>;
-            kCell_ = k_sweep_cell<S, D, H, NPL, kWarpsPerSM>;
+            kFace_ = k_sweep_face<S, D, H, NPL, kWarps>;
+            kCell_ = k_sweep_cell<S, D, H, NPL, kWarps>;
         }
         kTables_ = k_wall_tables<S, D, H>;
         if constexpr (sizeof(S) == 4) {
-            smemFaceFn_ = sides_ ? &SmemLayout32<D, H, NPL, 2>::sides
-                                 : (pipeA_ ? &SmemLayout32<D, H, NPL, 2>::face : &SmemLayout32<D, H, NPL, 1>::face);
-            smemCellFn_ = &SmemLayout32<D, H, NPL>::cell;
+            smemFaceFn_ = &SmemLayout32<D, H, NPL>::sides;
+            smemCellFn_ = nullptr;
         } else {
             smemFaceFn_ = &SmemLayout<S, D, H, NPL>::face;
             smemCellFn_ = &SmemLayout<S, D, H, NPL>::cell;
@@ -398,10 +378,11 @@ private:
     size_t smemFace(const TileDims& d) const { return smemFaceFn_(d); }
     size_t smemCell(const TileDims& d) const { return smemCellFn_(d); }
 
-    int D_ = 2, npl_ = 1, ctas_ = 1;
-    bool gather_ = false, pipeA_ = false, sides_ = false;
+    int D_ = 2, npl_ = 1;
+    bool fp32_ = false;
     KernelFn kMacros_ = nullptr;
     int gatherMF_ = 0, gatherBlocks_ = 1;
+    size_t gatherSmem_ = 0;
     void (*kGather_)(FusedArgs<S>, int) = nullptr;
     bool H_ = true;
     TilePlan plan_;

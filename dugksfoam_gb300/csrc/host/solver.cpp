@@ -209,7 +209,7 @@ int Solver::init(const dugks_case_desc& d) {
     a.rhoF = dalloc<double>(nA); a.UF = dalloc<double>(3 * (size_t)nA); a.TF = dalloc<double>(nA);
     a.qF = dalloc<double>(3 * (size_t)nA); a.tauF = dalloc<double>(nA);
     a.status = dalloc<int>(1);
-    Uo_ = dalloc<double>(3 * (size_t)nC); To_ = dalloc<double>(nC); ro_ = dalloc<double>(nC); red_ = dalloc<double>(8);
+    Uo_ = dalloc<double>(3 * (size_t)nC); To_ = dalloc<double>(nC); ro_ = dalloc<double>(nC); red_ = dalloc<double>(8 + 128 * 8);  // results + per-block partials
     if (oom_) return fail(DUGKS_ERR_OOM, "device allocation failed");
     cudaError_t ce = cudaSuccess;
     auto chk = [&](cudaError_t e) { if (ce == cudaSuccess) ce = e; };
