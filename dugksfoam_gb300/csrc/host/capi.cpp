@@ -1,8 +1,10 @@
 // extern "C" entry points of libdugks (include/dugks/dugks.h).
 #include <cstring>
 #include <exception>
+#include <filesystem>
 #include <memory>
 #include <string>
+#include <vector>
 
 #include "../cuda/noalloc.h"
 #include "dugks/dugks.h"
@@ -12,6 +14,10 @@
 struct dugks_handle {
     std::unique_ptr<dugks::Solver> solver;
     std::string err;
+    // case description kept on the host for dugks_write_time
+    std::vector<std::string> patchNames;
+    std::vector<int32_t> patchStart, patchSize, patchKind;
+    std::vector<double> wallU, wallT;  // per boundary face
 };
 
 namespace {
@@ -47,7 +53,17 @@ int dugks_create(const dugks_case_desc* desc, dugks_handle** out) {
         int code = DUGKS_OK;
         auto s = dugks::Solver::create(*desc, err, code);
         if (!s) { g_err = err; return code; }
-        *out = new dugks_handle{std::move(s), std::string()};
+        auto* h = new dugks_handle{std::move(s), std::string(), {}, {}, {}, {}, {}, {}};
+        const int nB = desc->n_faces - desc->n_internal_faces;
+        for (int p = 0; p < desc->n_patches; ++p) {
+            h->patchNames.push_back("patch" + std::to_string(p));
+            h->patchStart.push_back(desc->patch_start[p]);
+            h->patchSize.push_back(desc->patch_size[p]);
+            h->patchKind.push_back(desc->patch_kind[p]);
+        }
+        if (desc->wall_U) h->wallU.assign(desc->wall_U, desc->wall_U + 3 * (size_t)nB);
+        if (desc->wall_T) h->wallT.assign(desc->wall_T, desc->wall_T + nB);
+        *out = h;
         return DUGKS_OK;
     } catch (const std::exception& e) {
         g_err = e.what();
@@ -80,8 +96,88 @@ int dugks_create_from_case_dir(const char* dir, int32_t precision, dugks_handle*
     d.pipeline = DUGKS_PIPE_AUTO;
     d.device = 0;
     int rc = dugks_create(&d, out);
+    if (rc == DUGKS_OK) (*out)->patchNames = c.patchNames;
     if (rc == DUGKS_OK && c.deltaT > 0) (*out)->solver->setDt(c.deltaT);
     return rc;
+}
+
+int dugks_inspect_case_dir(const char* dir, dugks_case_summary* out) {
+    if (!dir || !out) { g_err = "null argument"; return DUGKS_ERR_ARG; }
+    dugks::FoamCase c;
+    std::string err;
+    if (!dugks::read_foam_case(dir, c, err)) {
+        g_err = err;
+        return err.find("unsupported") != std::string::npos ? DUGKS_ERR_UNSUPPORTED : DUGKS_ERR_IO;
+    }
+    dugks_case_summary r{};
+    r.n_points = (int32_t)(c.points.size() / 3);
+    r.n_cells = c.nCells; r.n_faces = c.nFaces; r.n_internal_faces = c.nInternal;
+    r.n_patches = (int32_t)c.patchNames.size();
+    for (size_t p = 0; p < c.patchNames.size(); ++p)
+        (c.patchKind[p] == DUGKS_PATCH_MAXWELL ? r.n_wall_faces : r.n_empty_faces) += c.patchSize[p];
+    r.n_xi_per_dim = c.nDV; r.KInner = c.KInner;
+    r.xi_max = c.xiMax; r.R = c.R; r.omega = c.omega; r.Tref = c.Tref; r.muRef = c.muRef; r.Pr = c.Pr;
+    r.delta_t = c.deltaT;
+    for (double v : c.rho0) r.rho_sum += v;
+    for (double v : c.T0) r.T_sum += v;
+    *out = r;
+    return DUGKS_OK;
+}
+
+int dugks_write_time(dugks_handle* h, const char* case_dir, const char* time_name) {
+    if (!h || !h->solver || !case_dir || !time_name) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int {
+        const dugks::Mesh& m = s.mesh();
+        const int nC = m.nC, nI = m.nI, nP = (int)h->patchNames.size();
+        std::vector<double> rho(nC), U(3 * (size_t)nC), T(nC), q(3 * (size_t)nC);
+        if (int e = s.macros(rho.data(), U.data(), T.data(), q.data(), nullptr)) return e;
+        std::vector<double> qF(3 * (size_t)(m.nI + m.nW));
+        if (int e = s.faceMacros(nullptr, nullptr, nullptr, qF.data(), nullptr)) return e;
+        // per patch outputs, in patch face order
+        std::vector<dugks::PatchOut> pr(nP), pu(nP), pt(nP), pq(nP), pqs(nP), pst(nP);
+        for (int p = 0; p < nP; ++p) {
+            const bool wall = h->patchKind[p] == DUGKS_PATCH_MAXWELL;
+            pr[p] = {h->patchNames[p], wall ? "calculatedMaxwell" : "empty", {}};
+            pu[p] = {h->patchNames[p], wall ? "fixedValue" : "empty", {}};
+            pt[p] = pu[p];
+            pq[p] = {h->patchNames[p], wall ? "calculated" : "empty", {}};
+            pqs[p] = pq[p];
+            pst[p] = pq[p];
+            if (!wall) continue;
+            const int n = h->patchSize[p];
+            std::vector<double> rw(n), qw(3 * (size_t)n), sw(9 * (size_t)n);
+            if (int e = s.wall(p, rw.data(), qw.data(), sw.data())) return e;
+            pr[p].values = rw;
+            pqs[p].values = qw;
+            pst[p].values = sw;
+            const int b0 = h->patchStart[p] - nI;  // boundary-face offset of the patch
+            for (int i = 0; i < n; ++i) {
+                for (int k = 0; k < 3; ++k) pu[p].values.push_back(h->wallU.empty() ? 0.0 : h->wallU[3 * (size_t)(b0 + i) + k]);
+                pt[p].values.push_back(h->wallT.empty() ? 0.0 : h->wallT[b0 + i]);
+            }
+        }
+        // face heat flux of the wall faces, by wall index -> patch position
+        for (int p = 0; p < nP; ++p)
+            if (h->patchKind[p] == DUGKS_PATCH_MAXWELL) pq[p].values.assign(3 * (size_t)h->patchSize[p], 0.0);
+        for (int w = 0; w < m.nW; ++w) {
+            const int p = m.wallPatch[w], i = m.wallFace[w] - h->patchStart[p];
+            for (int k = 0; k < 3; ++k) pq[p].values[3 * (size_t)i + k] = qF[3 * (size_t)(nI + w) + k];
+        }
+        const std::string dir = std::string(case_dir) + "/" + time_name;
+        std::error_code ec;
+        std::filesystem::create_directories(dir, ec);
+        if (ec) return s.fail(DUGKS_ERR_IO, "cannot create " + dir + ": " + ec.message());
+        std::string err;
+        const bool ok =
+            dugks::write_vol_field(dir + "/rho", "rho", "[1 -3 0 0 0 0 0]", 1, rho.data(), nC, pr, err) &&
+            dugks::write_vol_field(dir + "/U", "U", "[0 1 -1 0 0 0 0]", 3, U.data(), nC, pu, err) &&
+            dugks::write_vol_field(dir + "/T", "T", "[0 0 0 1 0 0 0]", 1, T.data(), nC, pt, err) &&
+            dugks::write_vol_field(dir + "/q", "q", "[1 0 -3 0 0 0 0]", 3, q.data(), nC, pq, err) &&
+            dugks::write_vol_field(dir + "/qSurf", "qSurf", "[1 0 -3 0 0 0 0]", 3, nullptr, nC, pqs, err) &&
+            dugks::write_vol_field(dir + "/stressSurf", "stressSurf", "[1 -1 -2 0 0 0 0]", 9, nullptr, nC, pst, err);
+        if (!ok) return s.fail(DUGKS_ERR_IO, err);
+        return DUGKS_OK;
+    });
 }
 
 int dugks_destroy(dugks_handle* h) {

@@ -350,8 +350,14 @@ bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err) {
     for (int p = 0; p < nP; ++p) {
         const Dict* pr = brho->sub(c.patchNames[p]);
         const Entry* ty = pr ? pr->find("type") : nullptr;
-        if (!ty || ty->toks.empty()) { err = "0/rho: no boundary entry for patch " + c.patchNames[p]; return false; }
-        std::string type = ty->toks[0].s;
+        // an empty polyMesh patch without a field entry is empty (as OpenFOAM's
+        // boundary-field reader fills unlisted empty patches)
+        const bool emptyMesh = c.patchTypes[p] == "empty";
+        if ((!ty || ty->toks.empty()) && !emptyMesh) {
+            err = "0/rho: no boundary entry for patch " + c.patchNames[p];
+            return false;
+        }
+        std::string type = (ty && !ty->toks.empty()) ? ty->toks[0].s : std::string("empty");
         c.rhoBC.push_back(type);
         if (type == "calculatedMaxwell") {
             c.patchKind.push_back(DUGKS_PATCH_MAXWELL);
@@ -421,49 +427,39 @@ void header(std::ostream& o, const char* cls, const std::string& obj) {
 }
 }  // namespace
 
-bool write_vol_scalar(const std::string& path, const std::string& name, const std::string& dims, const double* v,
-                      int n, const FoamCase& c, const std::vector<std::vector<double>>& pv, std::string& err) {
+bool write_vol_field(const std::string& path, const std::string& name, const std::string& dims, int ncomp,
+                     const double* internal, int n, const std::vector<PatchOut>& patches, std::string& err) {
+    const char* cls = ncomp == 1 ? "volScalarField" : (ncomp == 3 ? "volVectorField" : "volTensorField");
+    const char* lst = ncomp == 1 ? "scalar" : (ncomp == 3 ? "vector" : "tensor");
+    if (ncomp != 1 && ncomp != 3 && ncomp != 9) { err = "write_vol_field: ncomp must be 1, 3 or 9"; return false; }
     std::ofstream o(path);
     if (!o) { err = "cannot write " + path; return false; }
-    o.precision(12);
-    header(o, "volScalarField", name);
-    o << "dimensions      " << dims << ";\n\ninternalField   nonuniform List<scalar>\n" << n << "\n(\n";
-    for (int i = 0; i < n; ++i) o << v[i] << "\n";
-    o << ")\n;\n\nboundaryField\n{\n";
-    for (size_t p = 0; p < c.patchNames.size(); ++p) {
-        o << "    " << c.patchNames[p] << "\n    {\n";
-        if (c.patchKind[p] == DUGKS_PATCH_EMPTY) {
-            o << "        type            empty;\n";
-        } else {
-            o << "        type            calculated;\n        value           nonuniform List<scalar> "
-              << pv[p].size() << "(";
-            for (size_t i = 0; i < pv[p].size(); ++i) o << (i ? " " : "") << pv[p][i];
-            o << ");\n";
-        }
-        o << "    }\n";
+    o.precision(17);
+    auto item = [&](const double* v) {
+        if (ncomp == 1) { o << v[0]; return; }
+        o << "(";
+        for (int k = 0; k < ncomp; ++k) o << (k ? " " : "") << v[k];
+        o << ")";
+    };
+    header(o, cls, name);
+    o << "dimensions      " << dims << ";\n\n";
+    if (internal) {
+        o << "internalField   nonuniform List<" << lst << ">\n" << n << "\n(\n";
+        for (int i = 0; i < n; ++i) { item(internal + (size_t)ncomp * i); o << "\n"; }
+        o << ")\n;\n\n";
+    } else {
+        const double zero[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        o << "internalField   uniform ";
+        item(zero);
+        o << ";\n\n";
     }
-    o << "}\n";
-    return (bool)o;
-}
-
-bool write_vol_vector(const std::string& path, const std::string& name, const std::string& dims, const double* v,
-                      int n, const FoamCase& c, const std::vector<std::vector<double>>& pv, std::string& err) {
-    std::ofstream o(path);
-    if (!o) { err = "cannot write " + path; return false; }
-    o.precision(12);
-    header(o, "volVectorField", name);
-    o << "dimensions      " << dims << ";\n\ninternalField   nonuniform List<vector>\n" << n << "\n(\n";
-    for (int i = 0; i < n; ++i) o << "(" << v[3 * i] << " " << v[3 * i + 1] << " " << v[3 * i + 2] << ")\n";
-    o << ")\n;\n\nboundaryField\n{\n";
-    for (size_t p = 0; p < c.patchNames.size(); ++p) {
-        o << "    " << c.patchNames[p] << "\n    {\n";
-        if (c.patchKind[p] == DUGKS_PATCH_EMPTY) {
-            o << "        type            empty;\n";
-        } else {
-            o << "        type            calculated;\n        value           nonuniform List<vector> "
-              << pv[p].size() / 3 << "(";
-            for (size_t i = 0; i < pv[p].size() / 3; ++i)
-                o << (i ? " " : "") << "(" << pv[p][3 * i] << " " << pv[p][3 * i + 1] << " " << pv[p][3 * i + 2] << ")";
+    o << "boundaryField\n{\n";
+    for (const PatchOut& p : patches) {
+        o << "    " << p.name << "\n    {\n        type            " << p.type << ";\n";
+        if (p.type != "empty") {
+            const size_t m = p.values.size() / ncomp;
+            o << "        value           nonuniform List<" << lst << "> " << m << "(";
+            for (size_t i = 0; i < m; ++i) { o << (i ? " " : ""); item(p.values.data() + ncomp * i); }
             o << ");\n";
         }
         o << "    }\n";

@@ -40,13 +40,16 @@ struct FoamCase {
 
 bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err);
 
-// Write a volScalarField / volVectorField file (uniform boundary values
-// given per patch as "calculated" or "fixedValue" entries).
-bool write_vol_scalar(const std::string& path, const std::string& name, const std::string& dims,
-                      const double* v, int n, const FoamCase& c, const std::vector<std::vector<double>>& patchVals,
-                      std::string& err);
-bool write_vol_vector(const std::string& path, const std::string& name, const std::string& dims,
-                      const double* v, int n, const FoamCase& c, const std::vector<std::vector<double>>& patchVals,
-                      std::string& err);
+// One patch of a written vol field: "empty" patches carry no value.
+struct PatchOut {
+    std::string name, type;
+    std::vector<double> values;  // ncomp per face
+};
+
+// Write a vol field in OpenFOAM ASCII (volScalarField / volVectorField /
+// volTensorField by ncomp = 1 / 3 / 9), full double precision (17 digits).
+// internal == nullptr writes a uniform zero internal field.
+bool write_vol_field(const std::string& path, const std::string& name, const std::string& dims, int ncomp,
+                     const double* internal, int n, const std::vector<PatchOut>& patches, std::string& err);
 
 }  // namespace dugks

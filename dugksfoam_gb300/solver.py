@@ -31,6 +31,7 @@ EXPORTS = [
     "dugks_get_conum", "dugks_get_macros", "dugks_get_face_macros", "dugks_get_wall", "dugks_get_residual",
     "dugks_get_dist", "dugks_set_dist", "dugks_checkpoint_size", "dugks_checkpoint_save",
     "dugks_checkpoint_load", "dugks_profile_step", "dugks_launches_per_step", "dugks_macros_noalloc",
+    "dugks_inspect_case_dir", "dugks_write_time",
 ]
 
 
@@ -65,6 +66,17 @@ class Info(C.Structure):
         ("n_wall_faces", C.c_int32), ("n_dv", C.c_int32), ("n_dv_padded", C.c_int32),
         ("n_solution_d", C.c_int32), ("has_h", C.c_int32), ("precision", C.c_int32), ("pipeline", C.c_int32),
         ("dt", C.c_double), ("step_count", C.c_int64), ("device_bytes", C.c_size_t),
+    ]
+
+
+class CaseSummary(C.Structure):
+    _fields_ = [
+        ("n_points", C.c_int32), ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_internal_faces", C.c_int32),
+        ("n_patches", C.c_int32), ("n_wall_faces", C.c_int32), ("n_empty_faces", C.c_int32),
+        ("n_xi_per_dim", C.c_int32), ("KInner", C.c_int32),
+        ("xi_max", C.c_double), ("R", C.c_double), ("omega", C.c_double), ("Tref", C.c_double),
+        ("muRef", C.c_double), ("Pr", C.c_double), ("delta_t", C.c_double),
+        ("rho_sum", C.c_double), ("T_sum", C.c_double),
     ]
 
 
@@ -106,8 +118,20 @@ def load_library(path: str | None = None):
     lib.dugks_profile_step.argtypes = [vp, C.c_int32, C.c_char_p, C.c_size_t, _dp, C.c_int32, _ip]
     lib.dugks_launches_per_step.argtypes = [vp, _ip]
     lib.dugks_macros_noalloc.argtypes = [vp] + [vp] * 6
+    lib.dugks_inspect_case_dir.argtypes = [C.c_char_p, C.POINTER(CaseSummary)]
+    lib.dugks_write_time.argtypes = [vp, C.c_char_p, C.c_char_p]
     _lib = lib
     return lib
+
+
+def inspect_case_dir(path):
+    """Sizes and parameters of an OpenFOAM case directory (host only, no GPU)."""
+    lib = load_library()
+    out = CaseSummary()
+    rc = lib.dugks_inspect_case_dir(str(path).encode(), C.byref(out))
+    if rc != 0:
+        raise DugksError(rc, lib.dugks_global_error().decode())
+    return {k: getattr(out, k) for k, _ in CaseSummary._fields_}
 
 
 def _d(a):
@@ -286,6 +310,10 @@ class FvDVM:
         g = np.ascontiguousarray(g, np.float64)
         h = None if h is None else np.ascontiguousarray(h, np.float64)
         self._check(self._lib.dugks_set_dist(self._h, _d(g), _d(h)))
+
+    def write(self, case_dir, time_name):
+        """runTime.write(): rho, U, T, q, qSurf, stressSurf into case_dir/time_name (dugksFoam.C:81)."""
+        self._check(self._lib.dugks_write_time(self._h, str(case_dir).encode(), str(time_name).encode()))
 
     def checkpoint(self) -> bytes:
         n = C.c_size_t()

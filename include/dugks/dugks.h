@@ -197,6 +197,27 @@ int dugks_launches_per_step(dugks_handle* h, int32_t* n);
 int dugks_macros_noalloc(dugks_handle* h, const double* g, const double* hh, double* rho, double* U, double* T,
                          double* q);
 
+/* Sizes and parameters of an OpenFOAM case directory, read on the host only
+ * (no device, no handle): the same reader as dugks_create_from_case_dir. */
+typedef struct dugks_case_summary {
+    int32_t n_points, n_cells, n_faces, n_internal_faces, n_patches, n_wall_faces, n_empty_faces;
+    int32_t n_xi_per_dim, KInner;
+    double xi_max, R, omega, Tref, muRef, Pr, delta_t;
+    double rho_sum, T_sum;          /* sums of the 0/rho and 0/T internal fields */
+} dugks_case_summary;
+int dugks_inspect_case_dir(const char* case_dir, dugks_case_summary* out);
+
+/* runTime.write() of dugksFoam.C:81: write the current fields into
+ * <case_dir>/<time_name>/ in OpenFOAM ASCII (17 significant digits):
+ * rho, U, T (createFields.H AUTO_WRITE), q (fvDVM qVol_), qSurf and
+ * stressSurf (fvDVM qWall_/stressWall_: zero internal field, wall heat flux
+ * and stress on the wall patches).  Wall patches of rho keep the
+ * calculatedMaxwell type with the wall density as value, U and T are
+ * fixedValue with the wall velocity and temperature, so a written time
+ * directory is a valid 0/ for dugks_create_from_case_dir.  Patch names are
+ * those of the case directory, or patch<i> for handles made by dugks_create. */
+int dugks_write_time(dugks_handle* h, const char* case_dir, const char* time_name);
+
 #ifdef __cplusplus
 }
 #endif
