@@ -9,6 +9,7 @@
 #include "../cuda/noalloc.h"
 #include "dugks/dugks.h"
 #include "foam_io.h"
+#include "objective.h"
 #include "solver.h"
 
 struct dugks_handle {
@@ -304,6 +305,47 @@ int dugks_macros_noalloc(dugks_handle* h, const double* g, const double* hh, dou
 int dugks_launches_per_step(dugks_handle* h, int32_t* n) {
     if (!n) return DUGKS_ERR_ARG;
     return call(h, [&](dugks::Solver& s) -> int { *n = s.launchesPerStep(); return DUGKS_OK; });
+}
+
+}  // extern "C"
+
+namespace {
+int to_objective(dugks_handle* h, const dugks_objective* o, dugks::Objective& r) {
+    if (!o) return DUGKS_ERR_ARG;
+    r.nSteps = o->n_steps;
+    r.avgFirst = o->avg_first;
+    r.qPatch = o->q_patch;
+    r.stressPatch = o->stress_patch;
+    r.ckptEvery = o->checkpoint_every;
+    const int nP = (int)h->patchKind.size();
+    for (int p : {r.qPatch, r.stressPatch})
+        if (p < -1 || p >= nP || (p >= 0 && h->patchKind[p] != DUGKS_PATCH_MAXWELL)) return DUGKS_ERR_ARG;
+    return DUGKS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int dugks_objective_value(dugks_handle* h, const dugks_objective* o, double* J) {
+    if (!h || !h->solver || !J) return DUGKS_ERR_ARG;
+    dugks::Objective ob;
+    if (int e = to_objective(h, o, ob)) { h->err = "objective: bad patch or null descriptor"; return e; }
+    return call(h, [&](dugks::Solver& s) -> int { return dugks::objective_value(s, ob, *J); });
+}
+
+int dugks_objective_tangent(dugks_handle* h, const dugks_objective* o, const double* dTw, double ds, double* J,
+                            double* dJ) {
+    if (!h || !h->solver || !J || !dJ) return DUGKS_ERR_ARG;
+    dugks::Objective ob;
+    if (int e = to_objective(h, o, ob)) { h->err = "objective: bad patch or null descriptor"; return e; }
+    return call(h, [&](dugks::Solver& s) -> int { return dugks::objective_tangent(s, ob, dTw, ds, *J, *dJ); });
+}
+
+int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J, double* dJ_dTw, double* dJ_ds) {
+    if (!h || !h->solver || !J || !dJ_ds) return DUGKS_ERR_ARG;
+    dugks::Objective ob;
+    if (int e = to_objective(h, o, ob)) { h->err = "objective: bad patch or null descriptor"; return e; }
+    return call(h, [&](dugks::Solver& s) -> int { return dugks::objective_adjoint(s, ob, *J, dJ_dTw, *dJ_ds); });
 }
 
 }  // extern "C"

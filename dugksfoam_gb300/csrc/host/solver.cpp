@@ -237,6 +237,11 @@ int Solver::init(const dugks_case_desc& d) {
     chk(cudaMemcpy(Uo_, d.U0, 3 * (size_t)nC * sizeof(double), cudaMemcpyHostToDevice));
     chk(cudaMemcpy(To_, d.T0, nC * sizeof(double), cudaMemcpyHostToDevice));
     chk(cudaMemcpy(ro_, d.rho0, nC * sizeof(double), cudaMemcpyHostToDevice));
+    initRho_ = dalloc<double>(nC); initU_ = dalloc<double>(3 * (size_t)nC); initT_ = dalloc<double>(nC);
+    if (oom_) return fail(DUGKS_ERR_OOM, "device allocation failed");
+    chk(cudaMemcpy(initRho_, d.rho0, nC * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(initU_, d.U0, 3 * (size_t)nC * sizeof(double), cudaMemcpyHostToDevice));
+    chk(cudaMemcpy(initT_, d.T0, nC * sizeof(double), cudaMemcpyHostToDevice));
     chk(up(a.UF, UF));
     chk(up(a.rhoW, one));
     if (ce != cudaSuccess) return checkCuda(ce, "upload");

@@ -51,6 +51,11 @@ public:
     // Step arguments with the current dt (device pointers of the handle).
     StepArgs stepArgs() const { return argsNow(); }
     int device() const { return device_; }
+    int sms() const { return sms_; }
+    // initial fields rho0, U0, T0 on the device (the state dugks_create starts from)
+    const double* initRho() const { return initRho_; }
+    const double* initU() const { return initU_; }
+    const double* initT() const { return initT_; }
 
     // internal: allocation helper (recorded for release)
     template <typename T>
@@ -78,6 +83,7 @@ private:
     StepArgs base_{};
     // mesh-side device arrays not in StepArgs
     double* dcI_ = nullptr;
+    double *initRho_ = nullptr, *initU_ = nullptr, *initT_ = nullptr;
     // reference pipeline buffers (FP64)
     RefBuffers ref_{};
     // residual "old" fields and scratch

@@ -32,6 +32,7 @@ EXPORTS = [
     "dugks_get_dist", "dugks_set_dist", "dugks_checkpoint_size", "dugks_checkpoint_save",
     "dugks_checkpoint_load", "dugks_profile_step", "dugks_launches_per_step", "dugks_macros_noalloc",
     "dugks_inspect_case_dir", "dugks_write_time",
+    "dugks_objective_value", "dugks_objective_tangent", "dugks_objective_adjoint",
 ]
 
 
@@ -80,6 +81,11 @@ class CaseSummary(C.Structure):
     ]
 
 
+class ObjectiveDesc(C.Structure):
+    _fields_ = [("n_steps", C.c_int32), ("avg_first", C.c_int32), ("q_patch", C.c_int32),
+                ("stress_patch", C.c_int32), ("checkpoint_every", C.c_int32)]
+
+
 _lib = None
 
 
@@ -120,6 +126,10 @@ def load_library(path: str | None = None):
     lib.dugks_macros_noalloc.argtypes = [vp] + [vp] * 6
     lib.dugks_inspect_case_dir.argtypes = [C.c_char_p, C.POINTER(CaseSummary)]
     lib.dugks_write_time.argtypes = [vp, C.c_char_p, C.c_char_p]
+    op = C.POINTER(ObjectiveDesc)
+    lib.dugks_objective_value.argtypes = [vp, op, _dp]
+    lib.dugks_objective_tangent.argtypes = [vp, op, _dp, C.c_double, _dp, _dp]
+    lib.dugks_objective_adjoint.argtypes = [vp, op, _dp, _dp, _dp]
     _lib = lib
     return lib
 
@@ -314,6 +324,35 @@ class FvDVM:
     def write(self, case_dir, time_name):
         """runTime.write(): rho, U, T, q, qSurf, stressSurf into case_dir/time_name (dugksFoam.C:81)."""
         self._check(self._lib.dugks_write_time(self._h, str(case_dir).encode(), str(time_name).encode()))
+
+    # ------------------------------------------------------------ gradient harness
+    @staticmethod
+    def _obj(n_steps, avg_first, q_patch, stress_patch, checkpoint_every):
+        return ObjectiveDesc(int(n_steps), int(avg_first), int(q_patch), int(stress_patch), int(checkpoint_every))
+
+    def objective_value(self, n_steps, avg_first, q_patch=-1, stress_patch=-1, checkpoint_every=100):
+        """FP64 wall objective over steps [avg_first, n_steps) from the initial state."""
+        o = self._obj(n_steps, avg_first, q_patch, stress_patch, checkpoint_every)
+        J = C.c_double()
+        self._check(self._lib.dugks_objective_value(self._h, C.byref(o), C.byref(J)))
+        return J.value
+
+    def objective_tangent(self, dTw, ds, n_steps, avg_first, q_patch=-1, stress_patch=-1, checkpoint_every=100):
+        """(J, dJ) along (dTw per wall face, ds): FP64 tangent-linear step."""
+        o = self._obj(n_steps, avg_first, q_patch, stress_patch, checkpoint_every)
+        d = np.ascontiguousarray(dTw, np.float64)
+        J, dJ = C.c_double(), C.c_double()
+        self._check(self._lib.dugks_objective_tangent(self._h, C.byref(o), _d(d), float(ds), C.byref(J), C.byref(dJ)))
+        return J.value, dJ.value
+
+    def objective_adjoint(self, n_steps, avg_first, q_patch=-1, stress_patch=-1, checkpoint_every=100):
+        """(J, dJ/dTw per wall face, dJ/ds): hand-written adjoint of the FP64 step."""
+        o = self._obj(n_steps, avg_first, q_patch, stress_patch, checkpoint_every)
+        info = self.info()
+        g = np.zeros(max(info["n_wall_faces"], 1))
+        J, gs = C.c_double(), C.c_double()
+        self._check(self._lib.dugks_objective_adjoint(self._h, C.byref(o), C.byref(J), _d(g), C.byref(gs)))
+        return J.value, g[: info["n_wall_faces"]], gs.value
 
     def checkpoint(self) -> bytes:
         n = C.c_size_t()

@@ -218,6 +218,28 @@ int dugks_inspect_case_dir(const char* case_dir, dugks_case_summary* out);
  * those of the case directory, or patch<i> for handles made by dugks_create. */
 int dugks_write_time(dugks_handle* h, const char* case_dir, const char* time_name);
 
+/* ---- gradient harness (no counterpart in the reference; SURVEY config 4) ----
+ * Objective over a window of FP64 steps from the handle's initial state:
+ *   J = 1/(n_steps-avg_first) * sum_{n=avg_first}^{n_steps-1}
+ *       [ sum_{w in q_patch} S_w . qWall_w(n) + sum_{w in stress_patch} |S_w| stressWall_w,xy(n) ]
+ * (qWall, stressWall as fvDVM::updateMacroSurf, fvDVM.C:535-576).  Parameters:
+ * the wall temperature of every wall face (wall order = patch order) and the
+ * viscosity scale s (mu_ref -> s mu_ref, derivatives at s = 1).  These run the
+ * plain FP64 reference pipeline on private buffers; the handle's state, dt
+ * and stream are used but its fields are not modified. */
+typedef struct dugks_objective {
+    int32_t n_steps, avg_first;
+    int32_t q_patch, stress_patch;   /* patch indices, -1 for an absent term */
+    int32_t checkpoint_every;        /* adjoint: steps between stored states */
+} dugks_objective;
+
+int dugks_objective_value(dugks_handle* h, const dugks_objective* o, double* J);
+/* Tangent-linear (forward-mode) derivative along (dTw [n_wall_faces], ds). */
+int dugks_objective_tangent(dugks_handle* h, const dugks_objective* o, const double* dTw, double ds, double* J,
+                            double* dJ);
+/* Adjoint gradient: dJ/dTw [n_wall_faces] and dJ/ds, with J. */
+int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J, double* dJ_dTw, double* dJ_ds);
+
 #ifdef __cplusplus
 }
 #endif
