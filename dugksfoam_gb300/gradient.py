@@ -136,3 +136,51 @@ def adjoint_case(n=128, nxi=32, Kn=0.075, seed=0, sigma=5.0):
     nlid = wall_slice(base, "movingWall")[0].stop - wall_slice(base, "movingWall")[0].start
     Tw = 273.0 + sigma * np.random.default_rng(seed).standard_normal(nlid)
     return base, Tw
+
+
+def main(argv=None):
+    """Adjoint case run: J, the adjoint gradient, its agreement with the
+    tangent-linear step and (optionally) central differences, and the cost of
+    the adjoint against one FP64 forward.  One JSON line on stdout."""
+    import argparse
+    import json
+    import time
+
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--nxi", type=int, default=32)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--window", type=int, default=500)
+    ap.add_argument("--checkpoint-every", type=int, default=100)
+    ap.add_argument("--fd", type=int, default=0, help="number of lid faces checked by central differences")
+    a = ap.parse_args(argv)
+    base, Tw = adjoint_case(n=a.n, nxi=a.nxi)
+    setup = Setup(case=base, dt=cases.stable_dt(base), n_steps=a.steps, avg_first=a.steps - a.window,
+                  checkpoint_every=a.checkpoint_every)
+    t0 = time.perf_counter()
+    J0 = value(setup, Tw, 1.0)
+    t1 = time.perf_counter()
+    J, gTw, gs = adjoint(setup, Tw, 1.0)
+    t2 = time.perf_counter()
+    d = np.random.default_rng(1).standard_normal(len(Tw))
+    Jt, dJ = tangent(setup, Tw, 1.0, d, 1.0)
+    t3 = time.perf_counter()
+    out = dict(case=f"{a.n}^2 quads, {a.nxi}^2 DVs, {a.steps} steps, objective over the last {a.window}, "
+                    f"checkpoint every {a.checkpoint_every}",
+               J=J, J_forward=J0, dJ_ds=gs, dJ_dTw_norm=float(np.linalg.norm(gTw)),
+               adjoint_vs_tangent=abs(float(gTw @ d) + gs - dJ) / abs(dJ),
+               seconds=dict(forward=t1 - t0, adjoint=t2 - t1, tangent=t3 - t2),
+               adjoint_over_forward=(t2 - t1) / (t1 - t0))
+    if a.fd:
+        h, errs = 1e-3, []
+        for k in np.linspace(0, len(Tw) - 1, a.fd).astype(int):
+            e = np.zeros(len(Tw))
+            e[k] = 1.0
+            fd = (value(setup, Tw + h * e, 1.0) - value(setup, Tw - h * e, 1.0)) / (2 * h)
+            errs.append(abs(gTw[k] - fd) / abs(fd))
+        out["fd_rel_err_max"] = max(errs)
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()
