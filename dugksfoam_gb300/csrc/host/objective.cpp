@@ -4,6 +4,7 @@
 #include "objective.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -81,8 +82,8 @@ bool in_window(const Objective& o, int n) { return n >= o.avgFirst && n < o.nSte
 double window_scale(const Objective& o) { return 1.0 / std::max(1, o.nSteps - o.avgFirst); }
 
 void fwd_step(Solver& s, Fwd& f, const Objective& o, int n, const double* wq, const double* ws, double* J,
-              int lastPass = kRefKernels - 1) {
-    for (int k = 0; k <= lastPass; ++k) {
+              int lastPass = kRefKernels - 1, int firstPass = 0) {
+    for (int k = firstPass; k <= lastPass; ++k) {
         launch_ref_pass(k, f.a, f.b, s.sms(), s.stream());
         if (k == 4 && J && in_window(o, n)) launch_objective(f.a, wq, ws, window_scale(o), J, s.stream());
     }
@@ -221,6 +222,18 @@ int objective_adjoint(Solver& s, const Objective& o, double& J, double* dJdTw, d
     const int K = o.ckptEvery, N = o.nSteps, nSeg = (N + K - 1) / K;
     double* ckpt = W.alloc<double>(stateN * (size_t)nSeg);
     double* seg = W.alloc<double>(stateN * (size_t)(K + 1));
+    // Per-step forward values the reverse reads (face values before relaxation,
+    // face macros, rho_w), kept for a whole segment when device memory allows;
+    // otherwise each reverse step recomputes P1..P6 from its stored state.
+    const size_t iS = 0, iSh = nA * Vp, iF = H * nA * Vp, iW = iF + 9 * nA, interN = iW + nW;
+    double* inter = nullptr;
+    {
+        size_t freeB = 0, totalB = 0;
+        cudaMemGetInfo(&freeB, &totalB);
+        const char* rc = std::getenv("DUGKS_ADJ_RECOMPUTE");  // force the recompute form
+        if (!(rc && rc[0] == '1') && interN * (size_t)K * 8 < freeB / 2) inter = W.alloc<double>(interN * (size_t)K);
+        if (W.oom) { cudaGetLastError(); W.oom = false; inter = nullptr; }
+    }
     double* dJ = W.alloc<double>(1);
     // adjoint buffers
     AdjState A{};
@@ -258,19 +271,40 @@ int objective_adjoint(Solver& s, const Objective& o, double& J, double* dJdTw, d
         restore(ckpt + stateN * (size_t)sg);
         save(seg);
         for (int n = n0; n < n1; ++n) {
-            fwd_step(s, f, o, n, nullptr, nullptr, nullptr);
+            if (inter) {
+                fwd_step(s, f, o, n, nullptr, nullptr, nullptr, 4);  // P1..P6
+                double* it = inter + interN * (size_t)(n - n0);
+                cudaMemcpyAsync(it + iS, f.b.gS, nA * Vp * 8, cudaMemcpyDeviceToDevice, st);
+                if (a.hasH) cudaMemcpyAsync(it + iSh, f.b.hS, nA * Vp * 8, cudaMemcpyDeviceToDevice, st);
+                adj_pack_macros(a.nA, a.rhoF, a.UF, a.TF, a.qF, a.tauF, it + iF, sms, st);
+                cudaMemcpyAsync(it + iW, a.rhoW, nW * 8, cudaMemcpyDeviceToDevice, st);
+                fwd_step(s, f, o, n, nullptr, nullptr, nullptr, kRefKernels - 1, 5);  // P7..P9
+            } else {
+                fwd_step(s, f, o, n, nullptr, nullptr, nullptr);
+            }
             save(seg + stateN * (size_t)(n - n0 + 1));
         }
         for (int n = n1 - 1; n >= n0; --n) {
             const double* stN = seg + stateN * (size_t)(n - n0);
             const double* stN1 = seg + stateN * (size_t)(n - n0 + 1);
-            restore(stN);
-            fwd_step(s, f, o, n, nullptr, nullptr, nullptr, 4);  // P1..P6 of step n
-            adj_pack_macros(a.nC, a.rho, a.U, a.T, a.q, a.tau, mC, sms, st);
-            adj_pack_macros(a.nA, a.rhoF, a.UF, a.TF, a.qF, a.tauF, mF, sms, st);
             A.a = f.a;
-            A.gT = f.b.gT; A.hT = f.b.hT; A.gS = f.b.gS; A.hS = f.b.hS;
-            A.mC = mC; A.mF = mF;
+            if (inter) {
+                const double* it = inter + interN * (size_t)(n - n0);
+                const double* m = stN + oM;
+                adj_pack_macros(a.nC, m, m + nC, m + 4 * nC, m + 5 * nC, m + 8 * nC, mC, sms, st);
+                A.gT = stN + oG; A.hT = a.hasH ? stN + oH : nullptr;
+                A.gS = it + iS; A.hS = a.hasH ? it + iSh : nullptr;
+                A.mF = it + iF;
+                A.a.rhoW = const_cast<double*>(it + iW);
+            } else {
+                restore(stN);
+                fwd_step(s, f, o, n, nullptr, nullptr, nullptr, 4);  // P1..P6 of step n
+                adj_pack_macros(a.nC, a.rho, a.U, a.T, a.q, a.tau, mC, sms, st);
+                adj_pack_macros(a.nA, a.rhoF, a.UF, a.TF, a.qF, a.tauF, mF, sms, st);
+                A.gT = f.b.gT; A.hT = f.b.hT; A.gS = f.b.gS; A.hS = f.b.hS;
+                A.mF = mF;
+            }
+            A.mC = mC;
             A.lmN = lmN; A.lm = lm;
             A.haveMacroAdj = n < N - 1;
             adj_launch_step(A, stN1 + oG, a.hasH ? stN1 + oH : nullptr, in_window(o, n), wq, ws, window_scale(o), sms, st);

@@ -58,17 +58,20 @@ def test_tangent_and_adjoint_match_central_differences(built_lib):
     assert abs(gs - fd) <= 1e-4 * abs(fd), (gs, fd)
 
 
-def test_adjoint_independent_of_checkpoint_interval(built_lib):
+def test_adjoint_independent_of_checkpoint_interval(built_lib, monkeypatch):
+    """Same gradient for any checkpoint interval, with the per-step forward
+    values kept for a segment or recomputed from the stored states."""
     from dugksfoam_gb300 import gradient
 
     ref = None
-    for k in (8, 12, 40):
+    for k, recompute in ((8, "0"), (12, "0"), (40, "0"), (8, "1"), (12, "1")):
+        monkeypatch.setenv("DUGKS_ADJ_RECOMPUTE", recompute)
         setup, Tw = _setup(checkpoint_every=k)
         J, gTw, gs = gradient.adjoint(setup, Tw, 1.0)
         if ref is None:
             ref = (J, gTw, gs)
         else:
-            assert J == ref[0] and np.array_equal(gTw, ref[1]) and gs == ref[2]
+            assert J == ref[0] and np.array_equal(gTw, ref[1]) and gs == ref[2], (k, recompute)
 
 
 def test_autograd_function(built_lib):
