@@ -386,6 +386,16 @@ def cavity3d(n=48, Kn=0.1, nxi=20):
     return make_case(mesh, gas, rho0, nxi, xi_max, two_d=False)
 
 
+def batch_case(inst):
+    """Case dict of one batch instance: N x N lid-driven cavity, M x M DVs,
+    its Kn, lid speed and wall temperature (all walls at Tw; initial T = Tw)."""
+    gas, rho0 = gas_from_kn(inst["Kn"], T0=inst["Tw"])
+    xi_max = 4.0 * math.sqrt(2 * gas["R"] * inst["Tw"])
+    mesh = structured_mesh(inst["N"], inst["N"], 1, two_d=True)
+    return make_case(mesh, gas, rho0, inst["M"], xi_max, two_d=True, lid_u=inst["lid_u"], T0=inst["Tw"],
+                     Tw=inst["Tw"])
+
+
 def batch_instances(count=64, steps=2000):
     """Seeded parameter list of independent 2D cavities (one rng per instance)."""
     out = []

@@ -31,7 +31,43 @@ public:
     virtual void* gradBPtr(int which) = 0;  // current lagged boundary gradient
     virtual size_t bytes() const = 0;
     virtual std::string describe() const = 0;
+
+    // ---- batched stepping of several cases (FP32 pipeline only)
+    virtual bool batchable() const { return false; }
+    // Kernel arguments (a FusedArgs<float>) of the step that starts `parity`
+    // steps from now (0 or 1), for base arguments `a` of the current step.
+    virtual void batchArgs(const StepArgs& a, int parity, void* out) const { (void)a; (void)parity; (void)out; }
+    virtual size_t batchArgsBytes() const { return 0; }
+    virtual int batchTiles() const { return 0; }
+    virtual size_t batchSmemFace() const { return 0; }
+    virtual int batchGatherMF() const { return 0; }
+    virtual int batchNpl() const { return 0; }
 };
+
+// One launch over several cases: kernel k (0 face sides, 1 face macros,
+// 2 cell gather) of the FP32 step for every case.
+struct BatchLaunch {
+    const void* args = nullptr;  // device FusedArgs<float>[nCases] of this step
+    const int2* work = nullptr;  // [nWork] (case, tile)
+    int nWork = 0;
+    const int* faceOff = nullptr;  // [nCases+1] first global active face of each case
+    const int* cellOff = nullptr;  // [nCases+1] first global cell of each case
+    int nCases = 0;
+    size_t smemFace = 0;
+    int MF = 0;
+    size_t gatherSmem = 0;
+    int gatherBlocks = 1;
+    int D = 2, H = 1, npl = 4;
+};
+// Set function attributes and the persistent gather grid; false if the
+// (D, H, npl) combination has no kernels.
+bool fused_batch_prepare(BatchLaunch& L, int sms);
+void fused_batch_launch(int k, const BatchLaunch& L, int sms, cudaStream_t s);
+
+// Tuning override for pipelines created while it is set (0 = default):
+// DVs per lane and the tile-size cap of the face sweep.
+void fused_set_tuning(int npl, int maxTileCells);
+int fused_tile_cap();
 
 // DVs per lane of the fused kernels for a precision (FP32: DUGKS_NPL, default 4).
 int fused_npl(int precision);

@@ -108,9 +108,10 @@ struct TileMeta32 {
 
 // Copy the tile's block into shared memory (caller synchronises).
 template <int NT>
-__device__ __forceinline__ TileMeta32 stage_meta(const FusedArgs<float>& A, const TileHdr& hd, unsigned char* at) {
+__device__ __forceinline__ TileMeta32 stage_meta(const FusedArgs<float>& A, const TileHdr& hd, int tile,
+                                                 unsigned char* at) {
     int4* sm = reinterpret_cast<int4*>(at);
-    const int o0 = A.metaOff[blockIdx.x], n16 = A.metaOff[blockIdx.x + 1] - o0;
+    const int o0 = A.metaOff[tile], n16 = A.metaOff[tile + 1] - o0;
     const int4* gm = A.meta + o0;
     for (int i = threadIdx.x; i < n16; i += NT) sm[i] = __ldg(gm + i);
     TileMeta32 m;
@@ -545,11 +546,10 @@ __device__ __forceinline__ void recon_one32(const FusedArgs<float>& A, const flo
 // (tie values are never read: their flux is zero).  Raw rows of the next DV
 // chunk stream into the second row buffer while this chunk's faces run.
 template <int D, bool H, int NPL, int NW>
-__global__ void __launch_bounds__(NW * 32, 1) k_face_sides32(FusedArgs<float> A) {
+__device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int tile, unsigned char* smem) {
     using SL = Slots<D, H>;
     constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
-    extern __shared__ __align__(16) unsigned char smem[];
-    const TileHdr hd = A.hdr[blockIdx.x];
+    const TileHdr hd = A.hdr[tile];
     const StepArgs& b = A.b;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Vp = b.Vp, col = lane * NPL;
@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_face_sides32(FusedArgs<float> A)
     const size_t bufStride = LY::rows(hd.nT2) / sizeof(float);
     Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + 2 * LY::rows(hd.nT2));
     for (int i = threadIdx.x; i < hd.nFB * NS; i += NW * 32) mom[i].zero();
-    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, smem + LY::meta(hd.nT2, hd.nFB));
+    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, tile, smem + LY::meta(hd.nT2, hd.nFB));
     float4* sU = tm.dyn;            // [nFB] face Uref
     float4* ceq = tm.dyn + hd.nFB;  // [nT2][3] cell equilibria
     __syncthreads();
@@ -670,15 +670,60 @@ __global__ void __launch_bounds__(NW * 32, 1) k_face_sides32(FusedArgs<float> A)
     }
 }
 
+template <int D, bool H, int NPL, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) k_face_sides32(FusedArgs<float> A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    face_sides_body<D, H, NPL, NW>(A, blockIdx.x, smem);
+}
+
+// Several independent cases in one launch: block b runs tile work[b].y of
+// case work[b].x.  The cases' arguments are read through a read-only
+// pointer; every case shares D, H and NPL.
+template <int D, bool H, int NPL, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) k_face_sides32_batch(const FusedArgs<float>* __restrict__ AA,
+                                                                   const int2* __restrict__ work) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ FusedArgs<float> sA;
+    const int2 w = work[blockIdx.x];
+    if (threadIdx.x == 0) sA = AA[w.x];
+    __syncthreads();
+    face_sides_body<D, H, NPL, NW>(sA, w.y, smem);
+}
+
 // Face macros of every active face from the two per-side moment totals.
 template <int D, bool H>
-__global__ void k_face_macros32(FusedArgs<float> A) {
+__device__ __forceinline__ void face_macros_one(const FusedArgs<float>& A, int a) {
     constexpr int NS = Slots<D, H>::NS;
-    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.b.nA; a += gridDim.x * blockDim.x) {
-        const double* src = A.faceMom + (size_t)a * 2 * NS;
-        double M[NS];
-        for (int s = 0; s < NS; ++s) M[s] = src[s] + src[NS + s];
-        finalize_face32<D, H>(A, a, a >= A.b.nI ? a - A.b.nI : -1, A.uref4[a], M);
+    const double* src = A.faceMom + (size_t)a * 2 * NS;
+    double M[NS];
+    for (int s = 0; s < NS; ++s) M[s] = src[s] + src[NS + s];
+    finalize_face32<D, H>(A, a, a >= A.b.nI ? a - A.b.nI : -1, A.uref4[a], M);
+}
+
+template <int D, bool H>
+__global__ void k_face_macros32(FusedArgs<float> A) {
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < A.b.nA; a += gridDim.x * blockDim.x)
+        face_macros_one<D, H>(A, a);
+}
+
+// Case of a global item index: off[] holds the first item of each case (n+1 entries).
+__device__ __forceinline__ int case_of(const int* __restrict__ off, int n, int g) {
+    int lo = 0, hi = n;  // off[lo] <= g < off[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int D, bool H>
+__global__ void k_face_macros32_batch(const FusedArgs<float>* __restrict__ AA, const int* __restrict__ faceOff,
+                                      int nCases) {
+    const int total = faceOff[nCases];
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x) {
+        const int i = case_of(faceOff, nCases, g);
+        face_macros_one<D, H>(AA[i], g - faceOff[i]);
     }
 }
 
@@ -715,6 +760,127 @@ __device__ __forceinline__ void finalize_cell32(const FusedArgs<float>& A, int c
 // Cells per warp batch of the gather sweep's FP64 macro step (one lane per cell).
 constexpr int kGatherBatch = 32;
 
+// One cell of the gather sweep, all DV chunks; returns this lane's slot total
+// of the new cell moments (slot slot_of(lane)).  wb: the warp's two stages,
+// offset by the lane's column.
+template <int D, bool H, int NPL>
+__device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, int MF, float* wb, int lane) {
+    using SL = Slots<D, H>;
+    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2, NR = H ? 2 : 1;
+    const StepArgs& b = A.b;
+    const int Vp = b.Vp, col = lane * NPL;
+    const int stageRows = (1 + MF) * NR;
+    const int e0 = A.cfOff[c], e1 = A.cfOff[c + 1];
+    const int nfs = min(e1 - e0, MF);  // faces staged through shared memory
+    auto issue = [&](int stage, int v0) {
+        float* st = wb + (size_t)stage * stageRows * KC;
+        const size_t gi = (size_t)c * Vp + v0 + col;
+        cp_async_row(st, A.gT + gi, NPL);
+        if (H) cp_async_row(st + KC, A.hT + gi, NPL);
+        for (int f = 0; f < nfs; ++f) {
+            const int a = __float_as_int(A.cfEnt[e0 + f].w);
+            const size_t fi = (size_t)a * Vp + v0 + col;
+            cp_async_row(st + (1 + f) * NR * KC, A.gF + fi, NPL);
+            if (H) cp_async_row(st + ((1 + f) * NR + 1) * KC, A.hF + fi, NPL);
+        }
+        cp_async_commit();
+    };
+    const float* cblk = A.cc + (size_t)c * kNCoef;
+    Eq32<D, H> ec;
+    {
+        float4 q[3];
+        eq_table(q, cblk, cell_weight(A.dt, cblk));
+        ec.load(q, b.K, A.hrefFac);
+    }
+    const float4 u4 = reinterpret_cast<const float4*>(cblk)[0];
+    const float ur[3] = {u4.x, u4.y, u4.z};
+    const float kv = -A.dt * A.invVf[c];
+    Acc<float> acc;
+    acc.zero();
+    const int nChunks = Vp / KC;
+    issue(0, 0);
+    for (int ch = 0; ch < nChunks; ++ch) {
+        const int v0 = ch * KC;
+        if (ch + 1 < nChunks) {
+            issue((ch + 1) & 1, v0 + KC);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
+        }
+        const float* st = wb + (size_t)(ch & 1) * stageRows * KC;
+        Lane32<D, NPL> L;
+        L.load(A, v0, lane);
+        float2 g0[NP], h0[NP], t[NP], th[NP];
+        ldp<NP>(g0, st);
+        if (H) ldp<NP>(h0, st + KC);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            float2 g = g0[p], h = H ? h0[p] : f2(0.f);
+            ec.relax(L, p, g, h);
+            t[p] = fma2(sub2(g, g0[p]), f2(1.0f / 3.0f), g);  // exact when g+ == g~
+            th[p] = H ? fma2(sub2(h, h0[p]), f2(1.0f / 3.0f), h) : f2(0.f);
+        }
+        for (int e = e0; e < e1; ++e) {
+            const int f = e - e0;
+            const float4 ent = A.cfEnt[e];
+            const int a = __float_as_int(ent.w);
+            float2 gf[NP], hf[NP];
+            if (f < nfs) {
+                ldp<NP>(gf, st + (1 + f) * NR * KC);
+                if (H) ldp<NP>(hf, st + ((1 + f) * NR + 1) * KC);
+            } else {
+                const size_t fi = (size_t)a * Vp + v0 + col;
+                ldp<NP>(gf, A.gF + fi);
+                if (H) ldp<NP>(hf, A.hF + fi);
+            }
+            if (!H)
+#pragma unroll
+                for (int p = 0; p < NP; ++p) hf[p] = f2(0.f);
+            Eq32<D, H> eq;
+            eq.load(A.feqT + 3 * (size_t)a, b.K, A.hrefFac);
+            float2 xs[NP];
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                xs[p] = fma2(L.y[p], f2(ent.y), mul2(L.x[p], f2(ent.x)));
+                if (D == 3) xs[p] = fma2(L.z[p], f2(ent.z), xs[p]);
+            }
+            if (a >= b.nI) {  // wall: the cell is the owner; outgoing where xi.S > 0
+                const int w = a - b.nI;
+                const float rws = A.rhoWs[w], hwf = A.wall4[w].x;
+                float2 mw[NP];
+                ldp<NP>(mw, A.Mw + (size_t)w * Vp + v0 + col);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    float2 go = gf[p], ho = hf[p];
+                    eq.relax(L, p, go, ho);
+                    const float2 gw = mul2(f2(rws), mw[p]);
+                    const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
+                    gf[p] = sel2(o0, o1, go, sub2(gw, L.mr[p]));
+                    if (H) hf[p] = sel2(o0, o1, ho, sub2(mul2(gw, f2(hwf)), mul2(L.mr[p], f2(A.hrefFac))));
+                }
+            } else {
+#pragma unroll
+                for (int p = 0; p < NP; ++p) eq.relax(L, p, gf[p], hf[p]);
+            }
+#pragma unroll
+            for (int p = 0; p < NP; ++p) {
+                const float2 kx = mul2(xs[p], f2(kv));
+                t[p] = fma2(kx, gf[p], t[p]);
+                if (H) th[p] = fma2(kx, hf[p], th[p]);
+            }
+        }
+        const size_t gi = (size_t)c * Vp + v0 + col;
+        stp_cs<NP>(A.gTn + gi, t);
+        if (H) stp_cs<NP>(A.hTn + gi, th);
+        float m[NS];
+#pragma unroll
+        for (int s2 = 0; s2 < NS; ++s2) m[s2] = 0.0f;
+        mom32<D, H, NPL, NS>(m, L, ur, t, th, nullptr);
+        acc.add(reduce_scatter<NS, float>(m, lane));
+    }
+    return acc.value();
+}
+
 // Warps stride over the cells (persistent grid); per cell, all DV chunks:
 //   g~new = g+ + (g+ - g~)/3 - dt/V sum_f (xi.S_f) g^f_f,
 // with g+ the cell relaxation of g~ (P1), g^f_f the face value stored by
@@ -726,136 +892,54 @@ constexpr int kGatherBatch = 32;
 // are finished together, one lane per cell.
 template <int D, bool H, int NPL, int NW>
 __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A, int MF) {
-    using SL = Slots<D, H>;
-    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2, NR = H ? 2 : 1;
+    constexpr int NS = Slots<D, H>::NS, KC = 32 * NPL, NR = H ? 2 : 1;
     __shared__ double sM[NW][kGatherBatch][NS];
     __shared__ int sC[NW][kGatherBatch];
     extern __shared__ __align__(16) float gsm[];
-    const StepArgs& b = A.b;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int Vp = b.Vp, col = lane * NPL;
-    const int stageRows = (1 + MF) * NR;
-    float* wb = gsm + (size_t)warp * 2 * stageRows * KC + col;
+    float* wb = gsm + (size_t)warp * 2 * (1 + MF) * NR * KC + lane * NPL;
     const int myslot = slot_of<NS>(lane);
     const bool writer = NS == 16 ? (lane & 1) == 0 : true;
-    const int TW = gridDim.x * NW;
+    const int TW = gridDim.x * NW, nC = A.b.nC;
     int nb = 0;
-    for (int c = blockIdx.x * NW + warp; c < b.nC; c += TW) {
-        const int e0 = A.cfOff[c], e1 = A.cfOff[c + 1];
-        const int nfs = min(e1 - e0, MF);  // faces staged through shared memory
-        auto issue = [&](int stage, int v0) {
-            float* st = wb + (size_t)stage * stageRows * KC;
-            const size_t gi = (size_t)c * Vp + v0 + col;
-            cp_async_row(st, A.gT + gi, NPL);
-            if (H) cp_async_row(st + KC, A.hT + gi, NPL);
-            for (int f = 0; f < nfs; ++f) {
-                const int a = __float_as_int(A.cfEnt[e0 + f].w);
-                const size_t fi = (size_t)a * Vp + v0 + col;
-                cp_async_row(st + (1 + f) * NR * KC, A.gF + fi, NPL);
-                if (H) cp_async_row(st + ((1 + f) * NR + 1) * KC, A.hF + fi, NPL);
-            }
-            cp_async_commit();
-        };
-        const float* cblk = A.cc + (size_t)c * kNCoef;
-        Eq32<D, H> ec;
-        {
-            float4 q[3];
-            eq_table(q, cblk, cell_weight(A.dt, cblk));
-            ec.load(q, b.K, A.hrefFac);
-        }
-        const float4 u4 = reinterpret_cast<const float4*>(cblk)[0];
-        const float ur[3] = {u4.x, u4.y, u4.z};
-        const float kv = -A.dt * A.invVf[c];
-        Acc<float> acc;
-        acc.zero();
-        const int nChunks = Vp / KC;
-        issue(0, 0);
-        for (int ch = 0; ch < nChunks; ++ch) {
-            const int v0 = ch * KC;
-            if (ch + 1 < nChunks) {
-                issue((ch + 1) & 1, v0 + KC);
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
-            }
-            const float* st = wb + (size_t)(ch & 1) * stageRows * KC;
-            Lane32<D, NPL> L;
-            L.load(A, v0, lane);
-            float2 g0[NP], h0[NP], t[NP], th[NP];
-            ldp<NP>(g0, st);
-            if (H) ldp<NP>(h0, st + KC);
-    #pragma unroll
-            for (int p = 0; p < NP; ++p) {
-                float2 g = g0[p], h = H ? h0[p] : f2(0.f);
-                ec.relax(L, p, g, h);
-                t[p] = fma2(sub2(g, g0[p]), f2(1.0f / 3.0f), g);  // exact when g+ == g~
-                th[p] = H ? fma2(sub2(h, h0[p]), f2(1.0f / 3.0f), h) : f2(0.f);
-            }
-            for (int e = e0; e < e1; ++e) {
-                const int f = e - e0;
-                const float4 ent = A.cfEnt[e];
-                const int a = __float_as_int(ent.w);
-                float2 gf[NP], hf[NP];
-                if (f < nfs) {
-                    ldp<NP>(gf, st + (1 + f) * NR * KC);
-                    if (H) ldp<NP>(hf, st + ((1 + f) * NR + 1) * KC);
-                } else {
-                    const size_t fi = (size_t)a * Vp + v0 + col;
-                    ldp<NP>(gf, A.gF + fi);
-                    if (H) ldp<NP>(hf, A.hF + fi);
-                }
-                if (!H)
-    #pragma unroll
-                    for (int p = 0; p < NP; ++p) hf[p] = f2(0.f);
-                Eq32<D, H> eq;
-                eq.load(A.feqT + 3 * (size_t)a, b.K, A.hrefFac);
-                float2 xs[NP];
-    #pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    xs[p] = fma2(L.y[p], f2(ent.y), mul2(L.x[p], f2(ent.x)));
-                    if (D == 3) xs[p] = fma2(L.z[p], f2(ent.z), xs[p]);
-                }
-                if (a >= b.nI) {  // wall: the cell is the owner; outgoing where xi.S > 0
-                    const int w = a - b.nI;
-                    const float rws = A.rhoWs[w], hwf = A.wall4[w].x;
-                    float2 mw[NP];
-                    ldp<NP>(mw, A.Mw + (size_t)w * Vp + v0 + col);
-    #pragma unroll
-                    for (int p = 0; p < NP; ++p) {
-                        float2 go = gf[p], ho = hf[p];
-                        eq.relax(L, p, go, ho);
-                        const float2 gw = mul2(f2(rws), mw[p]);
-                        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
-                        gf[p] = sel2(o0, o1, go, sub2(gw, L.mr[p]));
-                        if (H) hf[p] = sel2(o0, o1, ho, sub2(mul2(gw, f2(hwf)), mul2(L.mr[p], f2(A.hrefFac))));
-                    }
-                } else {
-    #pragma unroll
-                    for (int p = 0; p < NP; ++p) eq.relax(L, p, gf[p], hf[p]);
-                }
-    #pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    const float2 kx = mul2(xs[p], f2(kv));
-                    t[p] = fma2(kx, gf[p], t[p]);
-                    if (H) th[p] = fma2(kx, hf[p], th[p]);
-                }
-            }
-            const size_t gi = (size_t)c * Vp + v0 + col;
-            stp_cs<NP>(A.gTn + gi, t);
-            if (H) stp_cs<NP>(A.hTn + gi, th);
-            float m[NS];
-    #pragma unroll
-            for (int s2 = 0; s2 < NS; ++s2) m[s2] = 0.0f;
-            mom32<D, H, NPL, NS>(m, L, ur, t, th, nullptr);
-            acc.add(reduce_scatter<NS, float>(m, lane));
-        }
-        // ---- slot totals of this cell into the batch; finish a full batch
-        if (writer) sM[warp][nb][myslot] = acc.value();
+    for (int c = blockIdx.x * NW + warp; c < nC; c += TW) {
+        const double tot = gather_cell<D, H, NPL>(A, c, MF, wb, lane);
+        if (writer) sM[warp][nb][myslot] = tot;
         if (lane == 0) sC[warp][nb] = c;
         ++nb;
-        if (nb == kGatherBatch || c + TW >= b.nC) {
+        if (nb == kGatherBatch || c + TW >= nC) {
             __syncwarp();
             if (lane < nb) finalize_cell32<D, H>(A, sC[warp][lane], sM[warp][lane]);
+            __syncwarp();
+            nb = 0;
+        }
+    }
+}
+
+// Several independent cases in one launch: warps stride over the cells of
+// all cases (cellOff: first global cell of each case, nCases+1 entries).
+template <int D, bool H, int NPL, int NW>
+__global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32_batch(const FusedArgs<float>* __restrict__ AA,
+                                                                    const int* __restrict__ cellOff, int nCases, int MF) {
+    constexpr int NS = Slots<D, H>::NS, KC = 32 * NPL, NR = H ? 2 : 1;
+    __shared__ double sM[NW][kGatherBatch][NS];
+    __shared__ int sC[NW][kGatherBatch], sI[NW][kGatherBatch];
+    extern __shared__ __align__(16) float gsm[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* wb = gsm + (size_t)warp * 2 * (1 + MF) * NR * KC + lane * NPL;
+    const int myslot = slot_of<NS>(lane);
+    const bool writer = NS == 16 ? (lane & 1) == 0 : true;
+    const int TW = gridDim.x * NW, total = cellOff[nCases];
+    int nb = 0;
+    for (int g = blockIdx.x * NW + warp; g < total; g += TW) {
+        const int i = case_of(cellOff, nCases, g), c = g - cellOff[i];
+        const double tot = gather_cell<D, H, NPL>(AA[i], c, MF, wb, lane);
+        if (writer) sM[warp][nb][myslot] = tot;
+        if (lane == 0) { sC[warp][nb] = c; sI[warp][nb] = i; }
+        ++nb;
+        if (nb == kGatherBatch || g + TW >= total) {
+            __syncwarp();
+            if (lane < nb) finalize_cell32<D, H>(AA[sI[warp][lane]], sC[warp][lane], sM[warp][lane]);
             __syncwarp();
             nb = 0;
         }

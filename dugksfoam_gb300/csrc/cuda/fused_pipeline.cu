@@ -6,8 +6,20 @@
 
 namespace dugks {
 
+namespace {
+thread_local int g_tuneNpl = 0, g_tuneTile = 0;
+}
+
+void fused_set_tuning(int npl, int maxTileCells) {
+    g_tuneNpl = npl;
+    g_tuneTile = maxTileCells;
+}
+
+int fused_tile_cap() { return g_tuneTile; }
+
 int fused_npl(int precision) {
     if (precision == DUGKS_FP64) return 1;
+    if (g_tuneNpl == 2 || g_tuneNpl == 4) return g_tuneNpl;
     const char* e = std::getenv("DUGKS_NPL");
     const int npl = e ? std::atoi(e) : 4;
     return (npl == 2 || npl == 4) ? npl : 4;  // packed pairs: an even count per lane

@@ -43,7 +43,7 @@ public:
         cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         const size_t budget = (size_t)maxSmem - 2048;
         const char* envT = std::getenv("DUGKS_TILE_CELLS");
-        const int maxCells = envT ? std::max(1, std::atoi(envT)) : 4096;
+        const int maxCells = fused_tile_cap() > 0 ? fused_tile_cap() : (envT ? std::max(1, std::atoi(envT)) : 4096);
         // FP32: sweep A alone is tiled (one-ring halo); FP64: both sweeps (two-ring halo)
         const SmemFn fn = [this](const TileDims& d) { return fp32_ ? smemFace(d) : std::max(smemFace(d), smemCell(d)); };
         if (!build_tile_plan(m, maxCells, fn, budget, plan_, err, fp32_ ? 1 : 2)) return false;
@@ -260,17 +260,39 @@ public:
         return k == 0 ? "k_sweep_face" : "k_sweep_cell";
     }
 
-    void launch(int k, const StepArgs& a, int sms, cudaStream_t s) override {
-        (void)sms;
+    // Arguments of the step `parity` steps ahead (0: this step, 1: the next).
+    FusedArgs<S> stepArgs(const StepArgs& a, int parity) const {
         FusedArgs<S> A = args_;
         A.b = a;
         A.dt = (S)a.dt;
-        A.gT = gT_[cur_]; A.hT = hT_[cur_];
-        A.gTn = gT_[1 - cur_]; A.hTn = hT_[1 - cur_];
-        A.Gbg = Gg_[cur_]; A.Gbh = Gh_[cur_];
-        A.Gbgn = Gg_[1 - cur_]; A.Gbhn = Gh_[1 - cur_];
-        A.cc = cc_[cur_]; A.ccn = cc_[1 - cur_];
+        const int c = (cur_ + parity) & 1;
+        A.gT = gT_[c]; A.hT = hT_[c];
+        A.gTn = gT_[1 - c]; A.hTn = hT_[1 - c];
+        A.Gbg = Gg_[c]; A.Gbh = Gh_[c];
+        A.Gbgn = Gg_[1 - c]; A.Gbhn = Gh_[1 - c];
+        A.cc = cc_[c]; A.ccn = cc_[1 - c];
         A.rhoN = rhoN_; A.UN = UN_; A.TN = TN_; A.qN = qN_; A.tauN = tauN_;
+        if (parity & 1) {  // endStep swaps the cell macros into the base arguments
+            std::swap(A.b.rho, A.rhoN); std::swap(A.b.U, A.UN); std::swap(A.b.T, A.TN);
+            std::swap(A.b.q, A.qN); std::swap(A.b.tau, A.tauN);
+        }
+        return A;
+    }
+
+    bool batchable() const override { return fp32_; }
+    void batchArgs(const StepArgs& a, int parity, void* out) const override {
+        const FusedArgs<S> A = stepArgs(a, parity);
+        std::memcpy(out, &A, sizeof(A));
+    }
+    size_t batchArgsBytes() const override { return sizeof(FusedArgs<S>); }
+    int batchTiles() const override { return plan_.nTiles; }
+    size_t batchSmemFace() const override { return smemA_; }
+    int batchGatherMF() const override { return gatherMF_; }
+    int batchNpl() const override { return npl_; }
+
+    void launch(int k, const StepArgs& a, int sms, cudaStream_t s) override {
+        (void)sms;
+        const FusedArgs<S> A = stepArgs(a, 0);
         if (k == 0) kFace_<<<plan_.nTiles, kWarps * 32, smemA_, s>>>(A);
         else if (!fp32_) kCell_<<<plan_.nTiles, kWarps * 32, smemB_, s>>>(A);
         else if (k == 1) kMacros_<<<sms * 4, 128, 0, s>>>(A);

@@ -1,0 +1,222 @@
+// Batched stepping of independent cases (see batch.h).
+#include "batch.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace dugks {
+
+Batch::~Batch() { release(); }
+
+void Batch::release() {
+    for (auto& g : graph_)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (void* p : dev_) cudaFree(p);
+    dev_.clear();
+    cases_.clear();
+    if (stream_) { cudaStreamDestroy(stream_); stream_ = nullptr; }
+}
+
+int Batch::check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return DUGKS_OK;
+    cudaGetLastError();
+    return fail(DUGKS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap) {
+    release();
+    npl_ = npl;
+    tileCap_ = tileCap;
+    if (int e = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream")) return e;
+    fused_set_tuning(npl, tileCap);
+    cells_ = cellDV_ = 0;
+    for (int i = 0; i < n; ++i) {
+        dugks_case_desc d = descs[i];
+        d.precision = DUGKS_FP32_FP64MOM;
+        d.pipeline = DUGKS_PIPE_FUSED;
+        std::string err;
+        int code = DUGKS_OK;
+        auto s = Solver::create(d, err, code);
+        if (!s) {
+            fused_set_tuning(0, 0);
+            return fail(code, "case " + std::to_string(i) + ": " + err);
+        }
+        FusedPipeline* fp = s->fusedPipeline();
+        if (!fp || !fp->batchable()) { fused_set_tuning(0, 0); return fail(DUGKS_ERR_UNSUPPORTED, "case is not batchable"); }
+        if (s->stepArgs().D != 2) { fused_set_tuning(0, 0); return fail(DUGKS_ERR_UNSUPPORTED, "batched cases must be 2D"); }
+        if (int e = s->setStream(stream_)) { fused_set_tuning(0, 0); return fail(e, s->error()); }
+        cells_ += s->stepArgs().nC;
+        cellDV_ += (long long)s->stepArgs().nC * s->stepArgs().nV;
+        cases_.push_back(std::move(s));
+    }
+    fused_set_tuning(0, 0);
+    const StepArgs a0 = cases_[0]->stepArgs();
+    for (auto& c : cases_)
+        if (c->stepArgs().hasH != a0.hasH) return fail(DUGKS_ERR_UNSUPPORTED, "batched cases must agree on h");
+    sms_ = cases_[0]->sms();
+    dirty_ = true;
+    parity_ = 0;
+    return DUGKS_OK;
+}
+
+int Batch::prepare() {
+    for (auto& g : graph_)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    const int n = (int)cases_.size();
+    const size_t ab = cases_[0]->fusedPipeline()->batchArgsBytes();
+    std::vector<unsigned char> host[2] = {std::vector<unsigned char>(ab * n), std::vector<unsigned char>(ab * n)};
+    std::vector<int2> work;
+    std::vector<int> faceOff(n + 1, 0), cellOff(n + 1, 0);
+    size_t smem = 0;
+    int MF = 0;
+    for (int i = 0; i < n; ++i) {
+        Solver& s = *cases_[i];
+        FusedPipeline* fp = s.fusedPipeline();
+        const StepArgs a = s.stepArgs();
+        for (int p = 0; p < 2; ++p) fp->batchArgs(a, p, host[p].data() + ab * i);
+        for (int t = 0; t < fp->batchTiles(); ++t) work.push_back(make_int2(i, t));
+        faceOff[i + 1] = faceOff[i] + a.nA;
+        cellOff[i + 1] = cellOff[i] + a.nC;
+        smem = std::max(smem, fp->batchSmemFace());
+        MF = std::max(MF, fp->batchGatherMF());
+    }
+    auto up = [&](const void* src, size_t bytes) -> void* {
+        void* p = nullptr;
+        if (cudaMalloc(&p, std::max<size_t>(bytes, 1)) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        dev_.push_back(p);
+        cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
+        return p;
+    };
+    void* args[2] = {up(host[0].data(), host[0].size()), up(host[1].data(), host[1].size())};
+    int2* w = static_cast<int2*>(up(work.data(), work.size() * sizeof(int2)));
+    int* fo = static_cast<int*>(up(faceOff.data(), faceOff.size() * sizeof(int)));
+    int* co = static_cast<int*>(up(cellOff.data(), cellOff.size() * sizeof(int)));
+    if (!args[0] || !args[1] || !w || !fo || !co) return fail(DUGKS_ERR_OOM, "batch: device allocation failed");
+    const StepArgs a0 = cases_[0]->stepArgs();
+    for (int p = 0; p < 2; ++p) {
+        BatchLaunch& L = L_[p];
+        L = BatchLaunch();
+        L.args = args[p];
+        L.work = w;
+        L.nWork = (int)work.size();
+        L.faceOff = fo;
+        L.cellOff = co;
+        L.nCases = n;
+        L.smemFace = smem;
+        L.MF = MF;
+        L.gatherSmem = (size_t)8 * 2 * (1 + MF) * (a0.hasH ? 2 : 1) * 32 * npl_ * sizeof(float);
+        L.D = 2;
+        L.H = a0.hasH;
+        L.npl = npl_;
+        if (!fused_batch_prepare(L, sms_)) return fail(DUGKS_ERR_UNSUPPORTED, "batch: no kernels for this case shape");
+    }
+    // graphs: two steps starting at parity 0 and at parity 1
+    for (int q = 0; q < 2; ++q) {
+        cudaGraph_t g = nullptr;
+        if (int e = check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "graph capture")) return e;
+        for (int s2 = 0; s2 < 2; ++s2)
+            for (int k = 0; k < 3; ++k) fused_batch_launch(k, L_[(q + s2) & 1], sms_, stream_);
+        if (int e = check(cudaStreamEndCapture(stream_, &g), "graph capture")) return e;
+        cudaError_t ce = cudaGraphInstantiate(&graph_[q], g, 0);
+        cudaGraphDestroy(g);
+        if (int e = check(ce, "graph instantiate")) return e;
+    }
+    dirty_ = false;
+    parity_ = 0;
+    return DUGKS_OK;
+}
+
+int Batch::step(int n) {
+    if (n < 0) return fail(DUGKS_ERR_ARG, "negative step count");
+    for (auto& c : cases_)
+        if (!(c->dt() > 0)) return fail(DUGKS_ERR_ARG, "set every case's dt before stepping");
+    if (dirty_)
+        if (int e = prepare()) return e;
+    int left = n;
+    while (left >= 2) {
+        if (int e = check(cudaGraphLaunch(graph_[parity_], stream_), "graph launch")) return e;
+        left -= 2;
+    }
+    if (left == 1) {
+        for (int k = 0; k < 3; ++k) fused_batch_launch(k, L_[parity_], sms_, stream_);
+        parity_ ^= 1;
+    }
+    if (int e = check(cudaGetLastError(), "batch step")) return e;
+    for (auto& c : cases_) c->advanceExternal(n);
+    return DUGKS_OK;
+}
+
+int Batch::synchronize() {
+    if (int e = check(cudaStreamSynchronize(stream_), "batch synchronize")) return e;
+    for (size_t i = 0; i < cases_.size(); ++i)
+        if (int e = cases_[i]->synchronize()) return fail(e, "case " + std::to_string(i) + ": " + cases_[i]->error());
+    return DUGKS_OK;
+}
+
+int Batch::setDt(int i, double dt) {
+    if (i < 0 || i >= (int)cases_.size()) return fail(DUGKS_ERR_ARG, "case index out of range");
+    if (!(dt > 0)) return fail(DUGKS_ERR_ARG, "dt must be positive");
+    cases_[i]->setDt(dt);
+    dirty_ = true;  // dt is part of the captured kernel arguments
+    return DUGKS_OK;
+}
+
+void Batch::info(dugks_batch_info& o) const {
+    std::memset(&o, 0, sizeof(o));
+    o.n_cases = (int32_t)cases_.size();
+    o.dv_per_lane = npl_;
+    o.tile_cap = tileCap_;
+    o.launches_per_step = 3;
+    o.steps_per_graph = 2;
+    o.cells = cells_;
+    o.cell_dv = cellDV_;
+    o.n_tuned = (int32_t)std::min<size_t>(tuneMs_.size(), 8);
+    for (int k = 0; k < o.n_tuned; ++k) {
+        o.tuned_dv_per_lane[k] = tuneNpl_[k];
+        o.tuned_tile_cap[k] = tuneCap_[k];
+        o.tuned_ms_per_step[k] = tuneMs_[k];
+    }
+}
+
+std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int autotune, std::string& err, int& code) {
+    std::unique_ptr<Batch> b(new Batch());
+    code = DUGKS_OK;
+    if (!descs || n < 1) { err = "batch: need at least one case"; code = DUGKS_ERR_ARG; return nullptr; }
+    int bestNpl = 4, bestCap = 0;
+    if (autotune) {
+        // candidates: DVs per lane x cap on cells per tile (0: the largest that fits)
+        const int cand[][2] = {{4, 0}, {4, 32}, {2, 0}};
+        double best = 1e300;
+        for (auto& c : cand) {
+            if (int e = b->build(descs, n, c[0], c[1])) { err = b->err_; code = e; return nullptr; }
+            for (auto& s : b->cases_) s->setDt(1e-30);  // timing only: a vanishing step
+            b->dirty_ = true;
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            int rc = b->step(2);
+            cudaEventRecord(e0, b->stream_);
+            if (!rc) rc = b->step(6);
+            cudaEventRecord(e1, b->stream_);
+            if (!rc) rc = b->check(cudaEventSynchronize(e1), "autotune");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            if (rc) { err = b->err_; code = rc; return nullptr; }
+            b->tuneNpl_.push_back(c[0]);
+            b->tuneCap_.push_back(c[1]);
+            b->tuneMs_.push_back(ms / 6.0);
+            if (ms < best) { best = ms; bestNpl = c[0]; bestCap = c[1]; }
+        }
+    }
+    std::vector<double> ms = b->tuneMs_;
+    std::vector<int> tn = b->tuneNpl_, tc = b->tuneCap_;
+    if (int e = b->build(descs, n, bestNpl, bestCap)) { err = b->err_; code = e; return nullptr; }
+    b->tuneMs_ = ms;
+    b->tuneNpl_ = tn;
+    b->tuneCap_ = tc;
+    return b;
+}
+
+}  // namespace dugks

@@ -10,6 +10,7 @@
 #include "dugks/dugks.h"
 #include "foam_io.h"
 #include "objective.h"
+#include "batch.h"
 #include "solver.h"
 
 struct dugks_handle {
@@ -349,3 +350,80 @@ int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J
 }
 
 }  // extern "C"
+
+struct dugks_batch {
+    std::unique_ptr<dugks::Batch> b;
+};
+
+namespace {
+template <typename F>
+int bcall(dugks_batch* h, F&& f) {
+    if (!h || !h->b) return DUGKS_ERR_ARG;
+    try {
+        return f(*h->b);
+    } catch (const std::exception& e) {
+        h->b->fail(DUGKS_ERR_ARG, e.what());
+        return DUGKS_ERR_ARG;
+    }
+}
+}  // namespace
+
+extern "C" {
+
+int dugks_batch_create(const dugks_case_desc* descs, int32_t n_cases, int32_t autotune, dugks_batch** out) {
+    if (!descs || !out || n_cases < 1) { g_err = "batch: null argument or no cases"; return DUGKS_ERR_ARG; }
+    *out = nullptr;
+    try {
+        std::string err;
+        int code = DUGKS_OK;
+        auto b = dugks::Batch::create(descs, n_cases, autotune, err, code);
+        if (!b) { g_err = err; return code; }
+        *out = new dugks_batch{std::move(b)};
+        return DUGKS_OK;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return DUGKS_ERR_ARG;
+    }
+}
+
+int dugks_batch_destroy(dugks_batch* b) {
+    delete b;
+    return DUGKS_OK;
+}
+
+const char* dugks_batch_last_error(const dugks_batch* b) {
+    if (!b || !b->b) return g_err.c_str();
+    return b->b->error().c_str();
+}
+
+int dugks_batch_set_dt(dugks_batch* b, int32_t i, double dt) {
+    return bcall(b, [&](dugks::Batch& x) { return x.setDt(i, dt); });
+}
+
+int dugks_batch_step(dugks_batch* b, int32_t nsteps) {
+    return bcall(b, [&](dugks::Batch& x) { return x.step(nsteps); });
+}
+
+int dugks_batch_synchronize(dugks_batch* b) {
+    return bcall(b, [&](dugks::Batch& x) { return x.synchronize(); });
+}
+
+int dugks_batch_get_macros(dugks_batch* b, int32_t i, double* rho, double* U, double* T, double* q) {
+    return bcall(b, [&](dugks::Batch& x) {
+        if (i < 0 || i >= x.nCases()) return x.fail(DUGKS_ERR_ARG, "case index out of range");
+        if (int e = x.synchronize()) return e;
+        if (int e = x.at(i).macros(rho, U, T, q, nullptr)) return x.fail(e, x.at(i).error());
+        return (int)DUGKS_OK;
+    });
+}
+
+int dugks_batch_get_info(dugks_batch* b, dugks_batch_info* out) {
+    if (!out) return DUGKS_ERR_ARG;
+    return bcall(b, [&](dugks::Batch& x) {
+        x.info(*out);
+        return (int)DUGKS_OK;
+    });
+}
+
+}  // extern "C"
+

@@ -329,6 +329,12 @@ int Solver::synchronize() {
     return DUGKS_OK;
 }
 
+void Solver::advanceExternal(int n) {
+    for (int i = 0; i < n; ++i)
+        if (fused_) fused_->endStep(base_);
+    steps_ += n;
+}
+
 int Solver::getCoNum(double& maxCo, double& meanCo) {
     if (int e = synchronize()) return e;
     launch_conum(argsNow(), dcI_, xiMax_, red_, stream_);

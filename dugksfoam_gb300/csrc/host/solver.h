@@ -52,6 +52,10 @@ public:
     StepArgs stepArgs() const { return argsNow(); }
     int device() const { return device_; }
     int sms() const { return sms_; }
+    // batched stepping: the FP32 pipeline, and the bookkeeping of n steps that
+    // ran outside evolution() (double-buffer swaps, step count)
+    FusedPipeline* fusedPipeline() const { return fused_.get(); }
+    void advanceExternal(int n);
     // initial fields rho0, U0, T0 on the device (the state dugks_create starts from)
     const double* initRho() const { return initRho_; }
     const double* initU() const { return initU_; }

@@ -33,6 +33,8 @@ EXPORTS = [
     "dugks_checkpoint_load", "dugks_profile_step", "dugks_launches_per_step", "dugks_macros_noalloc",
     "dugks_inspect_case_dir", "dugks_write_time",
     "dugks_objective_value", "dugks_objective_tangent", "dugks_objective_adjoint",
+    "dugks_batch_create", "dugks_batch_destroy", "dugks_batch_last_error", "dugks_batch_set_dt", "dugks_batch_step",
+    "dugks_batch_synchronize", "dugks_batch_get_macros", "dugks_batch_get_info",
 ]
 
 
@@ -86,6 +88,14 @@ class ObjectiveDesc(C.Structure):
                 ("stress_patch", C.c_int32), ("checkpoint_every", C.c_int32)]
 
 
+class BatchInfo(C.Structure):
+    _fields_ = [("n_cases", C.c_int32), ("dv_per_lane", C.c_int32), ("tile_cap", C.c_int32),
+                ("launches_per_step", C.c_int32), ("steps_per_graph", C.c_int32), ("n_tuned", C.c_int32),
+                ("cells", C.c_int64), ("cell_dv", C.c_int64),
+                ("tuned_dv_per_lane", C.c_int32 * 8), ("tuned_tile_cap", C.c_int32 * 8),
+                ("tuned_ms_per_step", C.c_double * 8)]
+
+
 _lib = None
 
 
@@ -130,6 +140,15 @@ def load_library(path: str | None = None):
     lib.dugks_objective_value.argtypes = [vp, op, _dp]
     lib.dugks_objective_tangent.argtypes = [vp, op, _dp, C.c_double, _dp, _dp]
     lib.dugks_objective_adjoint.argtypes = [vp, op, _dp, _dp, _dp]
+    lib.dugks_batch_create.argtypes = [C.POINTER(CaseDesc), C.c_int32, C.c_int32, C.POINTER(vp)]
+    lib.dugks_batch_destroy.argtypes = [vp]
+    lib.dugks_batch_last_error.argtypes = [vp]
+    lib.dugks_batch_last_error.restype = C.c_char_p
+    lib.dugks_batch_set_dt.argtypes = [vp, C.c_int32, C.c_double]
+    lib.dugks_batch_step.argtypes = [vp, C.c_int32]
+    lib.dugks_batch_synchronize.argtypes = [vp]
+    lib.dugks_batch_get_macros.argtypes = [vp, C.c_int32] + [_dp] * 4
+    lib.dugks_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
     _lib = lib
     return lib
 
@@ -159,6 +178,41 @@ def _kinds(mesh):
     return np.array(out, np.int32)
 
 
+def case_desc(case, precision=FP64, pipeline=PIPE_AUTO, device=0):
+    """dugks_case_desc of a case dict; returns (desc, arrays the desc points into)."""
+    m = case["mesh"]
+    g = case["gas"]
+    keep = dict(
+        points=np.ascontiguousarray(m["points"], np.float64),
+        off=np.ascontiguousarray(m["face_offsets"], np.int32),
+        fv=np.ascontiguousarray(m["face_verts"], np.int32),
+        own=np.ascontiguousarray(m["owner"], np.int32),
+        nei=np.ascontiguousarray(m["neighbour"], np.int32),
+        ps=np.array([p["startFace"] for p in m["patches"]], np.int32),
+        pn=np.array([p["nFaces"] for p in m["patches"]], np.int32),
+        pk=_kinds(m),
+        Ub=np.ascontiguousarray(case["Ub"], np.float64),
+        Tb=np.ascontiguousarray(case["Tb"], np.float64),
+        xis=np.ascontiguousarray(case["xis"], np.float64),
+        w=np.ascontiguousarray(case["weights"], np.float64),
+        rho0=np.ascontiguousarray(case["rho0"], np.float64),
+        U0=np.ascontiguousarray(case["U0"], np.float64),
+        T0=np.ascontiguousarray(case["T0"], np.float64),
+    )
+    d = CaseDesc(
+        n_points=len(keep["points"]), points=_d(keep["points"]), n_cells=int(m["n_cells"]),
+        n_faces=len(keep["off"]) - 1, n_internal_faces=len(keep["nei"]), face_offsets=_i(keep["off"]),
+        face_verts=_i(keep["fv"]), owner=_i(keep["own"]), neighbour=_i(keep["nei"]),
+        n_patches=len(keep["ps"]), patch_start=_i(keep["ps"]), patch_size=_i(keep["pn"]),
+        patch_kind=_i(keep["pk"]), wall_U=_d(keep["Ub"]), wall_T=_d(keep["Tb"]),
+        n_xi_per_dim=len(keep["xis"]), xis=_d(keep["xis"]), weights=_d(keep["w"]),
+        xi_max=float(case["xi_max"]), R=g["R"], omega=g["omega"], Tref=g["Tref"], muRef=g["muRef"],
+        Pr=g["Pr"], KInner=int(g["KInner"]), rho0=_d(keep["rho0"]), U0=_d(keep["U0"]), T0=_d(keep["T0"]),
+        precision=int(precision), pipeline=int(pipeline), device=int(device),
+    )
+    return d, keep
+
+
 class FvDVM:
     """One DUGKS case resident on one GPU (the reference's fvDVM)."""
 
@@ -168,36 +222,7 @@ class FvDVM:
         if _handle is not None:
             self._h = _handle
         else:
-            m = case["mesh"]
-            g = case["gas"]
-            keep = dict(
-                points=np.ascontiguousarray(m["points"], np.float64),
-                off=np.ascontiguousarray(m["face_offsets"], np.int32),
-                fv=np.ascontiguousarray(m["face_verts"], np.int32),
-                own=np.ascontiguousarray(m["owner"], np.int32),
-                nei=np.ascontiguousarray(m["neighbour"], np.int32),
-                ps=np.array([p["startFace"] for p in m["patches"]], np.int32),
-                pn=np.array([p["nFaces"] for p in m["patches"]], np.int32),
-                pk=_kinds(m),
-                Ub=np.ascontiguousarray(case["Ub"], np.float64),
-                Tb=np.ascontiguousarray(case["Tb"], np.float64),
-                xis=np.ascontiguousarray(case["xis"], np.float64),
-                w=np.ascontiguousarray(case["weights"], np.float64),
-                rho0=np.ascontiguousarray(case["rho0"], np.float64),
-                U0=np.ascontiguousarray(case["U0"], np.float64),
-                T0=np.ascontiguousarray(case["T0"], np.float64),
-            )
-            d = CaseDesc(
-                n_points=len(keep["points"]), points=_d(keep["points"]), n_cells=int(m["n_cells"]),
-                n_faces=len(keep["off"]) - 1, n_internal_faces=len(keep["nei"]), face_offsets=_i(keep["off"]),
-                face_verts=_i(keep["fv"]), owner=_i(keep["own"]), neighbour=_i(keep["nei"]),
-                n_patches=len(keep["ps"]), patch_start=_i(keep["ps"]), patch_size=_i(keep["pn"]),
-                patch_kind=_i(keep["pk"]), wall_U=_d(keep["Ub"]), wall_T=_d(keep["Tb"]),
-                n_xi_per_dim=len(keep["xis"]), xis=_d(keep["xis"]), weights=_d(keep["w"]),
-                xi_max=float(case["xi_max"]), R=g["R"], omega=g["omega"], Tref=g["Tref"], muRef=g["muRef"],
-                Pr=g["Pr"], KInner=int(g["KInner"]), rho0=_d(keep["rho0"]), U0=_d(keep["U0"]), T0=_d(keep["T0"]),
-                precision=int(precision), pipeline=int(pipeline), device=int(device),
-            )
+            d, self._keep = case_desc(case, precision, pipeline, device)
             rc = self._lib.dugks_create(C.byref(d), C.byref(self._h))
             if rc != 0:
                 raise DugksError(rc, self._lib.dugks_global_error().decode())
@@ -377,3 +402,65 @@ class FvDVM:
         n = C.c_int32()
         self._check(self._lib.dugks_launches_per_step(self._h, C.byref(n)))
         return n.value
+
+
+class Batch:
+    """Independent 2D cases advanced together (dugks_batch_*): one launch per
+    pass over all cases, two steps per CUDA graph, autotuned DVs per lane and
+    tile cap.  Every case uses the FP32 / FP64-moment pipeline."""
+
+    def __init__(self, case_list, autotune=True, device=0):
+        self._lib = load_library()
+        self._h = C.c_void_p()
+        descs, self._keep = [], []
+        for c in case_list:
+            d, k = case_desc(c, FP32_FP64MOM, PIPE_FUSED, device)
+            descs.append(d)
+            self._keep.append(k)
+        arr = (CaseDesc * len(descs))(*descs)
+        rc = self._lib.dugks_batch_create(arr, len(descs), int(bool(autotune)), C.byref(self._h))
+        if rc != 0:
+            raise DugksError(rc, self._lib.dugks_global_error().decode())
+        self.cells = [int(c["mesh"]["n_cells"]) for c in case_list]
+
+    def _check(self, rc):
+        if rc != 0:
+            raise DugksError(rc, self._lib.dugks_batch_last_error(self._h).decode())
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.dugks_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_dt(self, i, dt):
+        self._check(self._lib.dugks_batch_set_dt(self._h, int(i), float(dt)))
+
+    def step(self, n):
+        self._check(self._lib.dugks_batch_step(self._h, int(n)))
+
+    def synchronize(self):
+        self._check(self._lib.dugks_batch_synchronize(self._h))
+
+    def macros(self, i):
+        n = self.cells[i]
+        out = dict(rho=np.empty(n), U=np.empty((n, 3)), T=np.empty(n), q=np.empty((n, 3)))
+        self._check(self._lib.dugks_batch_get_macros(self._h, int(i), _d(out["rho"]), _d(out["U"]), _d(out["T"]),
+                                                     _d(out["q"])))
+        return out
+
+    def info(self):
+        b = BatchInfo()
+        self._check(self._lib.dugks_batch_get_info(self._h, C.byref(b)))
+        r = {k: getattr(b, k) for k, _ in BatchInfo._fields_}
+        n = b.n_tuned
+        r["tuned"] = [dict(dv_per_lane=b.tuned_dv_per_lane[k], tile_cap=b.tuned_tile_cap[k],
+                           ms_per_step=b.tuned_ms_per_step[k]) for k in range(n)]
+        for k in ("tuned_dv_per_lane", "tuned_tile_cap", "tuned_ms_per_step"):
+            r.pop(k)
+        return r

@@ -240,6 +240,30 @@ int dugks_objective_tangent(dugks_handle* h, const dugks_objective* o, const dou
 /* Adjoint gradient: dJ/dTw [n_wall_faces] and dJ/ds, with J. */
 int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J, double* dJ_dTw, double* dJ_ds);
 
+/* ---- batched cases (no counterpart in the reference; SURVEY config 3) ----
+ * Independent 2D cases (uneven meshes and velocity grids) advanced together
+ * with the FP32 pipeline: every pass of the step is one launch over all cases,
+ * two steps are captured in a CUDA graph and replayed.  With autotune != 0
+ * the DVs per lane (2 or 4) and the cap on cells per tile are chosen by timing
+ * a few steps of each candidate.  Each case starts from its own initial state;
+ * set each case's dt before stepping. */
+typedef struct dugks_batch dugks_batch;
+typedef struct dugks_batch_info {
+    int32_t n_cases, dv_per_lane, tile_cap, launches_per_step, steps_per_graph, n_tuned;
+    int64_t cells, cell_dv;               /* summed over the cases (cell*DV uses unpadded DVs) */
+    int32_t tuned_dv_per_lane[8], tuned_tile_cap[8];
+    double tuned_ms_per_step[8];          /* timing of each candidate */
+} dugks_batch_info;
+
+int dugks_batch_create(const dugks_case_desc* descs, int32_t n_cases, int32_t autotune, dugks_batch** out);
+int dugks_batch_destroy(dugks_batch* b);
+const char* dugks_batch_last_error(const dugks_batch* b);
+int dugks_batch_set_dt(dugks_batch* b, int32_t i, double dt);
+int dugks_batch_step(dugks_batch* b, int32_t nsteps);      /* asynchronous */
+int dugks_batch_synchronize(dugks_batch* b);
+int dugks_batch_get_macros(dugks_batch* b, int32_t i, double* rho, double* U, double* T, double* q);
+int dugks_batch_get_info(dugks_batch* b, dugks_batch_info* out);
+
 #ifdef __cplusplus
 }
 #endif
