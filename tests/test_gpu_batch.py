@@ -1,8 +1,10 @@
 """Batched cases (GPU): uneven meshes and velocity grids advanced together
-give, for every case, the same bits as the case stepped alone with the FP32
-pipeline under the same tuning; the autotuner times its candidates; an odd
-step count (one step outside the two-step graph) and a dt change (graph
-re-capture) are covered."""
+agree with each case stepped alone with the FP32 pipeline under the same
+tuning to FP32 rounding (the batched kernels are separate instantiations of
+the same device code, so the compiler may contract multiply-adds differently),
+and are bit-reproducible from run to run; the autotuner times its candidates;
+an odd step count (one step outside the two-step graph) and a dt change
+(graph re-capture) are covered."""
 import numpy as np
 import pytest
 
@@ -16,11 +18,9 @@ def _instances():
             dict(N=7, M=6, Kn=0.01, lid_u=80.0, Tw=260.0)]
 
 
-def test_batch_matches_single_cases(built_lib, monkeypatch):
-    from dugksfoam_gb300 import cases, solver
+def _run_batch(cs, dts):
+    from dugksfoam_gb300 import solver
 
-    cs = [cases.batch_case(i) for i in _instances()]
-    dts = [cases.stable_dt(c) for c in cs]
     b = solver.Batch(cs, autotune=False)
     info = b.info()
     assert info["n_cases"] == 3 and info["launches_per_step"] == 3 and info["dv_per_lane"] == 4
@@ -29,6 +29,22 @@ def test_batch_matches_single_cases(built_lib, monkeypatch):
     b.step(7)          # three graph replays and one single step
     b.set_dt(1, 0.9 * dts[1])
     b.step(4)          # re-captured graphs
+    out = [b.macros(i) for i in range(len(cs))]
+    b.close()
+    return out
+
+
+def test_batch_matches_single_cases(built_lib):
+    from conftest import rel_err
+    from dugksfoam_gb300 import cases, solver
+
+    cs = [cases.batch_case(i) for i in _instances()]
+    dts = [cases.stable_dt(c) for c in cs]
+    got_all = _run_batch(cs, dts)
+    again = _run_batch(cs, dts)
+    for i in range(len(cs)):
+        for k in ("rho", "U", "T", "q"):
+            assert np.array_equal(got_all[i][k], again[i][k]), ("reproducible", i, k)
     for i, c in enumerate(cs):
         s = solver.FvDVM(c, precision=solver.FP32_FP64MOM, pipeline=solver.PIPE_FUSED)
         s.set_dt(dts[i])
@@ -36,11 +52,11 @@ def test_batch_matches_single_cases(built_lib, monkeypatch):
         if i == 1:
             s.set_dt(0.9 * dts[1])
         s.evolution(4)
-        want, got = s.macros(), b.macros(i)
+        want, got = s.macros(), got_all[i]
         for k in ("rho", "U", "T", "q"):
-            assert np.array_equal(got[k], want[k]), (i, k)
+            einf, el2 = rel_err(got[k], want[k])
+            assert einf <= 1e-6 and el2 <= 1e-6, (i, k, einf, el2)
         s.close()
-    b.close()
 
 
 def test_batch_autotune(built_lib):
