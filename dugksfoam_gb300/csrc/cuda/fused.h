@@ -64,6 +64,21 @@ struct BatchLaunch {
 bool fused_batch_prepare(BatchLaunch& L, int sms);
 void fused_batch_launch(int k, const BatchLaunch& L, int sms, cudaStream_t s);
 
+// Allow a kernel the device's opt-in maximum of dynamic shared memory (less
+// its static shared memory).  The limit belongs to the kernel function, which
+// every case launching it shares, so it is set once to the maximum and each
+// launch asks for its own size.
+template <typename F>
+inline cudaError_t allow_max_dynamic_smem(F* func) {
+    int dev = 0, maxSmem = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (cudaError_t e = cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(func))) return e;
+    return cudaFuncSetAttribute(reinterpret_cast<const void*>(func), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                maxSmem - (int)fa.sharedSizeBytes);
+}
+
 // Tuning override for pipelines created while it is set (0 = default):
 // DVs per lane and the tile-size cap of the face sweep.
 void fused_set_tuning(int npl, int maxTileCells);

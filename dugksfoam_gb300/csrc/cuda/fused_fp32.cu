@@ -22,8 +22,7 @@ struct BatchKernels {
     static bool prepare(BatchLaunch& L, int sms) {
         auto kf = k_face_sides32_batch<D, H, NPL, kBatchWarps>;
         auto kg = k_cell_gather32_batch<D, H, NPL, kBatchGather>;
-        if (cudaFuncSetAttribute(kf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.smemFace) != cudaSuccess ||
-            cudaFuncSetAttribute(kg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.gatherSmem) != cudaSuccess) {
+        if (allow_max_dynamic_smem(kf) != cudaSuccess || allow_max_dynamic_smem(kg) != cudaSuccess) {
             cudaGetLastError();
             return false;
         }

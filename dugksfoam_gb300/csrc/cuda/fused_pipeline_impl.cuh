@@ -54,8 +54,11 @@ public:
             smemA_ = std::max(smemA_, smemFace(d));
             if (!fp32_) smemB_ = std::max(smemB_, smemCell(d));
         }
-        cudaFuncSetAttribute(kFace_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemA_);
-        if (!fp32_) cudaFuncSetAttribute(kCell_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemB_);
+        // The limit is a property of the kernel function, shared by every
+        // pipeline (case) that launches it: allow the device maximum, each
+        // launch then asks for its own size.
+        allow_max_dynamic_smem(kFace_);
+        if (!fp32_) allow_max_dynamic_smem(kCell_);
 
         // ---- upload plan
         args_.hdr = upload(plan_.hdr);
@@ -147,7 +150,7 @@ public:
                 for (int c = 0; c < m.nC; ++c) gatherMF_ = std::max(gatherMF_, cfOff[c + 1] - cfOff[c]);
                 gatherMF_ = std::min(gatherMF_, 8);  // further faces of a cell are read directly
                 gatherSmem_ = gather_smem(kGatherWarps, gatherMF_, KC, H_);
-                cudaFuncSetAttribute(kGather_, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gatherSmem_);
+                allow_max_dynamic_smem(kGather_);
                 int per = 0, nsm = 0;
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kGather_, kGatherWarps * 32, gatherSmem_);
                 cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
