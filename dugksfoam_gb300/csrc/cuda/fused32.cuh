@@ -685,7 +685,11 @@ __global__ void __launch_bounds__(NW * 32, 1) k_face_sides32_batch(const FusedAr
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ FusedArgs<float> sA;
     const int2 w = work[blockIdx.x];
-    if (threadIdx.x == 0) sA = AA[w.x];
+    {
+        const long long* src = reinterpret_cast<const long long*>(AA + w.x);
+        long long* dst = reinterpret_cast<long long*>(&sA);
+        for (int k = threadIdx.x; k < (int)(sizeof(FusedArgs<float>) / 8); k += blockDim.x) dst[k] = src[k];
+    }
     __syncthreads();
     face_sides_body<D, H, NPL, NW>(sA, w.y, smem);
 }
@@ -924,16 +928,26 @@ __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32_batch(const FusedA
     constexpr int NS = Slots<D, H>::NS, KC = 32 * NPL, NR = H ? 2 : 1;
     __shared__ double sM[NW][kGatherBatch][NS];
     __shared__ int sC[NW][kGatherBatch], sI[NW][kGatherBatch];
+    __shared__ FusedArgs<float> sA[NW];  // the warp's current case
     extern __shared__ __align__(16) float gsm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* wb = gsm + (size_t)warp * 2 * (1 + MF) * NR * KC + lane * NPL;
     const int myslot = slot_of<NS>(lane);
     const bool writer = NS == 16 ? (lane & 1) == 0 : true;
     const int TW = gridDim.x * NW, total = cellOff[nCases];
-    int nb = 0;
+    int nb = 0, cur = -1;
     for (int g = blockIdx.x * NW + warp; g < total; g += TW) {
         const int i = case_of(cellOff, nCases, g), c = g - cellOff[i];
-        const double tot = gather_cell<D, H, NPL>(AA[i], c, MF, wb, lane);
+        if (i != cur) {  // consecutive cells mostly share a case: copy its arguments once
+            static_assert(sizeof(FusedArgs<float>) % 8 == 0, "argument block is copied in 8-byte words");
+            const long long* src = reinterpret_cast<const long long*>(AA + i);
+            long long* dst = reinterpret_cast<long long*>(&sA[warp]);
+            __syncwarp();
+            for (int k = lane; k < (int)(sizeof(FusedArgs<float>) / 8); k += 32) dst[k] = src[k];
+            __syncwarp();
+            cur = i;
+        }
+        const double tot = gather_cell<D, H, NPL>(sA[warp], c, MF, wb, lane);
         if (writer) sM[warp][nb][myslot] = tot;
         if (lane == 0) { sC[warp][nb] = c; sI[warp][nb] = i; }
         ++nb;
