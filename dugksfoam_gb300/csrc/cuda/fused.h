@@ -53,6 +53,7 @@ struct BatchLaunch {
     const int* faceOff = nullptr;  // [nCases+1] first global active face of each case
     const int* cellOff = nullptr;  // [nCases+1] first global cell of each case
     int nCases = 0;
+    int nFaces = 0;  // active faces of all cases
     size_t smemFace = 0;
     int MF = 0;
     size_t gatherSmem = 0;

@@ -35,8 +35,8 @@ struct BatchKernels {
         const FusedArgs<float>* AA = static_cast<const FusedArgs<float>*>(L.args);
         if (k == 0)
             k_face_sides32_batch<D, H, NPL, kBatchWarps><<<L.nWork, kBatchWarps * 32, L.smemFace, s>>>(AA, L.work);
-        else if (k == 1)
-            k_face_macros32_batch<D, H><<<sms * 4, 128, 0, s>>>(AA, L.faceOff, L.nCases);
+        else if (k == 1)  // one face per thread: FP64-bound, wants every warp it can get
+            k_face_macros32_batch<D, H><<<std::max(1, (L.nFaces + 127) / 128), 128, 0, s>>>(AA, L.faceOff, L.nCases);
         else
             k_cell_gather32_batch<D, H, NPL, kBatchGather><<<L.gatherBlocks, kBatchGather * 32, L.gatherSmem, s>>>(
                 AA, L.cellOff, L.nCases, L.MF);

@@ -298,7 +298,7 @@ public:
         const FusedArgs<S> A = stepArgs(a, 0);
         if (k == 0) kFace_<<<plan_.nTiles, kWarps * 32, smemA_, s>>>(A);
         else if (!fp32_) kCell_<<<plan_.nTiles, kWarps * 32, smemB_, s>>>(A);
-        else if (k == 1) kMacros_<<<sms * 4, 128, 0, s>>>(A);
+        else if (k == 1) kMacros_<<<std::max(1, (a.nA + 127) / 128), 128, 0, s>>>(A);  // one face per thread
         else
             kGather_<<<std::min((a.nC + kGatherWarps - 1) / kGatherWarps, gatherBlocks_), kGatherWarps * 32, gatherSmem_,
                        s>>>(A, gatherMF_);

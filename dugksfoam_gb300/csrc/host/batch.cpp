@@ -102,6 +102,7 @@ int Batch::prepare() {
         L.faceOff = fo;
         L.cellOff = co;
         L.nCases = n;
+        L.nFaces = faceOff[n];
         L.smemFace = smem;
         L.MF = MF;
         L.gatherSmem = (size_t)8 * 2 * (1 + MF) * (a0.hasH ? 2 : 1) * 32 * npl_ * sizeof(float);
