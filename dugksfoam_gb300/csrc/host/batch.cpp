@@ -11,6 +11,12 @@ Batch::~Batch() { release(); }
 void Batch::release() {
     for (auto& g : graph_)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (auto& g : single_)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (auto e : ev_) cudaEventDestroy(e);
+    ev_.clear();
+    for (auto st : side_) cudaStreamDestroy(st);
+    side_.clear();
     for (void* p : dev_) cudaFree(p);
     dev_.clear();
     cases_.clear();
@@ -23,11 +29,22 @@ int Batch::check(cudaError_t e, const char* what) {
     return fail(DUGKS_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap) {
+int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap, int groups) {
     release();
     npl_ = npl;
     tileCap_ = tileCap;
+    groups_ = std::max(1, std::min(groups, n));
     if (int e = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream")) return e;
+    for (int g = 1; g < groups_; ++g) {
+        cudaStream_t st = nullptr;
+        if (int e = check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")) return e;
+        side_.push_back(st);
+    }
+    for (int g = 0; g < 2 * groups_; ++g) {
+        cudaEvent_t e = nullptr;
+        if (int r = check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event")) return r;
+        ev_.push_back(e);
+    }
     fused_set_tuning(npl, tileCap);
     cells_ = cellDV_ = 0;
     for (int i = 0; i < n; ++i) {
@@ -62,69 +79,110 @@ int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap) {
 int Batch::prepare() {
     for (auto& g : graph_)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    for (auto& g : single_)
+        if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     const int n = (int)cases_.size();
     const size_t ab = cases_[0]->fusedPipeline()->batchArgsBytes();
-    std::vector<unsigned char> host[2] = {std::vector<unsigned char>(ab * n), std::vector<unsigned char>(ab * n)};
-    std::vector<int2> work;
-    std::vector<int> faceOff(n + 1, 0), cellOff(n + 1, 0);
-    size_t smem = 0;
-    int MF = 0;
-    for (int i = 0; i < n; ++i) {
-        Solver& s = *cases_[i];
-        FusedPipeline* fp = s.fusedPipeline();
-        const StepArgs a = s.stepArgs();
-        for (int p = 0; p < 2; ++p) fp->batchArgs(a, p, host[p].data() + ab * i);
-        for (int t = 0; t < fp->batchTiles(); ++t) work.push_back(make_int2(i, t));
-        faceOff[i + 1] = faceOff[i] + a.nA;
-        cellOff[i + 1] = cellOff[i] + a.nC;
-        smem = std::max(smem, fp->batchSmemFace());
-        MF = std::max(MF, fp->batchGatherMF());
+    // groups of about equal work (cells x DVs), largest cases first
+    std::vector<int> order(n), group(n, 0);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    auto work = [&](int i) { return (double)cases_[i]->stepArgs().nC * cases_[i]->stepArgs().Vp; };
+    std::sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
+    std::vector<double> load(groups_, 0.0);
+    for (int i : order) {
+        const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        group[i] = g;
+        load[g] += work(i);
     }
-    auto up = [&](const void* src, size_t bytes) -> void* {
-        void* p = nullptr;
-        if (cudaMalloc(&p, std::max<size_t>(bytes, 1)) != cudaSuccess) { cudaGetLastError(); return nullptr; }
-        dev_.push_back(p);
-        cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice);
-        return p;
-    };
-    void* args[2] = {up(host[0].data(), host[0].size()), up(host[1].data(), host[1].size())};
-    int2* w = static_cast<int2*>(up(work.data(), work.size() * sizeof(int2)));
-    int* fo = static_cast<int*>(up(faceOff.data(), faceOff.size() * sizeof(int)));
-    int* co = static_cast<int*>(up(cellOff.data(), cellOff.size() * sizeof(int)));
-    if (!args[0] || !args[1] || !w || !fo || !co) return fail(DUGKS_ERR_OOM, "batch: device allocation failed");
     const StepArgs a0 = cases_[0]->stepArgs();
-    for (int p = 0; p < 2; ++p) {
-        BatchLaunch& L = L_[p];
-        L = BatchLaunch();
-        L.args = args[p];
-        L.work = w;
-        L.nWork = (int)work.size();
-        L.faceOff = fo;
-        L.cellOff = co;
-        L.nCases = n;
-        L.nFaces = faceOff[n];
-        L.smemFace = smem;
-        L.MF = MF;
-        L.gatherSmem = (size_t)8 * 2 * (1 + MF) * (a0.hasH ? 2 : 1) * 32 * npl_ * sizeof(float);
-        L.D = 2;
-        L.H = a0.hasH;
-        L.npl = npl_;
-        if (!fused_batch_prepare(L, sms_)) return fail(DUGKS_ERR_UNSUPPORTED, "batch: no kernels for this case shape");
+    for (int p = 0; p < 2; ++p) L_[p].assign(groups_, BatchLaunch());
+    auto up = [&](const void* src, size_t bytes) -> void* {
+        void* ptr = nullptr;
+        if (cudaMalloc(&ptr, std::max<size_t>(bytes, 1)) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+        dev_.push_back(ptr);
+        cudaMemcpy(ptr, src, bytes, cudaMemcpyHostToDevice);
+        return ptr;
+    };
+    for (int g = 0; g < groups_; ++g) {
+        std::vector<int> members;
+        for (int i = 0; i < n; ++i)
+            if (group[i] == g) members.push_back(i);
+        const int m = (int)members.size();
+        std::vector<unsigned char> host[2] = {std::vector<unsigned char>(ab * m), std::vector<unsigned char>(ab * m)};
+        std::vector<int2> wl;
+        std::vector<int> faceOff(m + 1, 0), cellOff(m + 1, 0);
+        size_t smem = 0;
+        int MF = 0;
+        for (int j = 0; j < m; ++j) {
+            Solver& sv = *cases_[members[j]];
+            FusedPipeline* fp = sv.fusedPipeline();
+            const StepArgs a = sv.stepArgs();
+            for (int p = 0; p < 2; ++p) fp->batchArgs(a, p, host[p].data() + ab * j);
+            for (int t = 0; t < fp->batchTiles(); ++t) wl.push_back(make_int2(j, t));
+            faceOff[j + 1] = faceOff[j] + a.nA;
+            cellOff[j + 1] = cellOff[j] + a.nC;
+            smem = std::max(smem, fp->batchSmemFace());
+            MF = std::max(MF, fp->batchGatherMF());
+        }
+        void* args[2] = {up(host[0].data(), host[0].size()), up(host[1].data(), host[1].size())};
+        int2* w = static_cast<int2*>(up(wl.data(), wl.size() * sizeof(int2)));
+        int* fo = static_cast<int*>(up(faceOff.data(), faceOff.size() * sizeof(int)));
+        int* co = static_cast<int*>(up(cellOff.data(), cellOff.size() * sizeof(int)));
+        if (!args[0] || !args[1] || !w || !fo || !co) return fail(DUGKS_ERR_OOM, "batch: device allocation failed");
+        for (int p = 0; p < 2; ++p) {
+            BatchLaunch& L = L_[p][g];
+            L.args = args[p];
+            L.work = w;
+            L.nWork = (int)wl.size();
+            L.faceOff = fo;
+            L.cellOff = co;
+            L.nCases = m;
+            L.nFaces = faceOff[m];
+            L.smemFace = smem;
+            L.MF = MF;
+            L.gatherSmem = (size_t)8 * 2 * (1 + MF) * (a0.hasH ? 2 : 1) * 32 * npl_ * sizeof(float);
+            L.D = 2;
+            L.H = a0.hasH;
+            L.npl = npl_;
+            if (!fused_batch_prepare(L, sms_)) return fail(DUGKS_ERR_UNSUPPORTED, "batch: no kernels for this case shape");
+            // the groups run side by side: share the SMs in the persistent gather grid
+            L.gatherBlocks = std::max(1, L.gatherBlocks / groups_);
+        }
     }
-    // graphs: two steps starting at parity 0 and at parity 1
     for (int q = 0; q < 2; ++q) {
-        cudaGraph_t g = nullptr;
-        if (int e = check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "graph capture")) return e;
-        for (int s2 = 0; s2 < 2; ++s2)
-            for (int k = 0; k < 3; ++k) fused_batch_launch(k, L_[(q + s2) & 1], sms_, stream_);
-        if (int e = check(cudaStreamEndCapture(stream_, &g), "graph capture")) return e;
-        cudaError_t ce = cudaGraphInstantiate(&graph_[q], g, 0);
-        cudaGraphDestroy(g);
-        if (int e = check(ce, "graph instantiate")) return e;
+        if (int e = capture(q, 2, graph_[q])) return e;
+        if (int e = capture(q, 1, single_[q])) return e;
     }
     dirty_ = false;
     parity_ = 0;
     return DUGKS_OK;
+}
+
+// Graph of `steps` steps from parity q: group 0 on the batch stream, the
+// other groups forked onto their own streams and joined at the end.
+int Batch::capture(int q, int steps, cudaGraphExec_t& out) {
+    cudaGraph_t g = nullptr;
+    if (int e = check(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal), "graph capture")) return e;
+    cudaError_t ce = cudaEventRecord(ev_[0], stream_);
+    for (int k = 1; k < groups_ && ce == cudaSuccess; ++k) ce = cudaStreamWaitEvent(side_[k - 1], ev_[0], 0);
+    for (int k = 0; k < groups_; ++k) {
+        cudaStream_t st = k == 0 ? stream_ : side_[k - 1];
+        for (int s2 = 0; s2 < steps; ++s2)
+            for (int pass = 0; pass < 3; ++pass) fused_batch_launch(pass, L_[(q + s2) & 1][k], sms_, st);
+    }
+    for (int k = 1; k < groups_ && ce == cudaSuccess; ++k) {
+        ce = cudaEventRecord(ev_[groups_ + k], side_[k - 1]);
+        if (ce == cudaSuccess) ce = cudaStreamWaitEvent(stream_, ev_[groups_ + k], 0);
+    }
+    cudaError_t ce2 = cudaStreamEndCapture(stream_, &g);
+    if (ce == cudaSuccess) ce = ce2;
+    if (int e = check(ce, "graph capture")) {
+        if (g) cudaGraphDestroy(g);
+        return e;
+    }
+    ce = cudaGraphInstantiate(&out, g, 0);
+    cudaGraphDestroy(g);
+    return check(ce, "graph instantiate");
 }
 
 int Batch::step(int n) {
@@ -139,7 +197,7 @@ int Batch::step(int n) {
         left -= 2;
     }
     if (left == 1) {
-        for (int k = 0; k < 3; ++k) fused_batch_launch(k, L_[parity_], sms_, stream_);
+        if (int e = check(cudaGraphLaunch(single_[parity_], stream_), "graph launch")) return e;
         parity_ ^= 1;
     }
     if (int e = check(cudaGetLastError(), "batch step")) return e;
@@ -169,6 +227,7 @@ void Batch::info(dugks_batch_info& o) const {
     o.tile_cap = tileCap_;
     o.launches_per_step = 3;
     o.steps_per_graph = 2;
+    o.groups = groups_;
     o.cells = cells_;
     o.cell_dv = cellDV_;
     o.n_tuned = (int32_t)std::min<size_t>(tuneMs_.size(), 8);
@@ -176,6 +235,7 @@ void Batch::info(dugks_batch_info& o) const {
         o.tuned_dv_per_lane[k] = tuneNpl_[k];
         o.tuned_tile_cap[k] = tuneCap_[k];
         o.tuned_ms_per_step[k] = tuneMs_[k];
+        o.tuned_groups[k] = tuneGroups_[k];
     }
 }
 
@@ -183,13 +243,14 @@ std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int au
     std::unique_ptr<Batch> b(new Batch());
     code = DUGKS_OK;
     if (!descs || n < 1) { err = "batch: need at least one case"; code = DUGKS_ERR_ARG; return nullptr; }
-    int bestNpl = 4, bestCap = 0;
+    int bestNpl = 4, bestCap = 0, bestGroups = 4;
     if (autotune) {
-        // candidates: DVs per lane x cap on cells per tile (0: the largest that fits)
-        const int cand[][2] = {{4, 0}, {4, 32}, {2, 0}};
+        // candidates: DVs per lane, cap on cells per tile (0: the largest that
+        // fits), concurrent groups
+        const int cand[][3] = {{4, 0, 1}, {4, 0, 4}, {4, 0, 8}, {4, 32, 4}, {2, 0, 4}};
         double best = 1e300;
         for (auto& c : cand) {
-            if (int e = b->build(descs, n, c[0], c[1])) { err = b->err_; code = e; return nullptr; }
+            if (int e = b->build(descs, n, c[0], c[1], c[2])) { err = b->err_; code = e; return nullptr; }
             for (auto& s : b->cases_) s->setDt(1e-30);  // timing only: a vanishing step
             b->dirty_ = true;
             cudaEvent_t e0, e1;
@@ -207,16 +268,18 @@ std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int au
             if (rc) { err = b->err_; code = rc; return nullptr; }
             b->tuneNpl_.push_back(c[0]);
             b->tuneCap_.push_back(c[1]);
+            b->tuneGroups_.push_back(b->groups_);
             b->tuneMs_.push_back(ms / 6.0);
-            if (ms < best) { best = ms; bestNpl = c[0]; bestCap = c[1]; }
+            if (ms < best) { best = ms; bestNpl = c[0]; bestCap = c[1]; bestGroups = c[2]; }
         }
     }
     std::vector<double> ms = b->tuneMs_;
-    std::vector<int> tn = b->tuneNpl_, tc = b->tuneCap_;
-    if (int e = b->build(descs, n, bestNpl, bestCap)) { err = b->err_; code = e; return nullptr; }
+    std::vector<int> tn = b->tuneNpl_, tc = b->tuneCap_, tg = b->tuneGroups_;
+    if (int e = b->build(descs, n, bestNpl, bestCap, bestGroups)) { err = b->err_; code = e; return nullptr; }
     b->tuneMs_ = ms;
     b->tuneNpl_ = tn;
     b->tuneCap_ = tc;
+    b->tuneGroups_ = tg;
     return b;
 }
 

@@ -1,7 +1,10 @@
 // Batched stepping of independent cases (uneven meshes and velocity grids):
-// each FP32 pass runs as one launch over every case (tiles, faces and cells of
-// all cases in one grid), two steps are captured in a CUDA graph and replayed,
-// and an autotuner picks the DVs per lane and the tile-size cap by timing.
+// the cases are split into G groups of about equal work; each FP32 pass runs
+// as one launch over every case of a group (tiles, faces and cells of all its
+// cases in one grid); the groups' launch chains are independent branches of
+// one CUDA graph (two steps per graph, replayed), so one group's face sweep
+// overlaps another's cell gather; an autotuner picks the DVs per lane, the
+// tile-size cap and G by timing.
 #pragma once
 
 #include <memory>
@@ -34,22 +37,26 @@ public:
 
 private:
     Batch() = default;
-    int build(const dugks_case_desc* descs, int n, int npl, int tileCap);
+    int build(const dugks_case_desc* descs, int n, int npl, int tileCap, int groups);
     int prepare();  // argument arrays, work lists, graphs
     void release();
     int check(cudaError_t e, const char* what);
 
     std::vector<std::unique_ptr<Solver>> cases_;
     cudaStream_t stream_ = nullptr;
-    int sms_ = 1, npl_ = 4, tileCap_ = 0;
-    BatchLaunch L_[2];
+    std::vector<cudaStream_t> side_;   // one per group beyond the first (graph capture fork)
+    std::vector<cudaEvent_t> ev_;
+    int sms_ = 1, npl_ = 4, tileCap_ = 0, groups_ = 1;
+    std::vector<BatchLaunch> L_[2];    // per parity, per group
     std::vector<void*> dev_;
-    cudaGraphExec_t graph_[2] = {nullptr, nullptr};
+    cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // two steps from parity q
+    cudaGraphExec_t single_[2] = {nullptr, nullptr};  // one step from parity q
+    int capture(int q, int steps, cudaGraphExec_t& out);
     int parity_ = 0;
     bool dirty_ = true;
     long long cells_ = 0, cellDV_ = 0;
     std::vector<double> tuneMs_;
-    std::vector<int> tuneNpl_, tuneCap_;
+    std::vector<int> tuneNpl_, tuneCap_, tuneGroups_;
     std::string err_;
 };
 

@@ -89,10 +89,10 @@ class ObjectiveDesc(C.Structure):
 
 
 class BatchInfo(C.Structure):
-    _fields_ = [("n_cases", C.c_int32), ("dv_per_lane", C.c_int32), ("tile_cap", C.c_int32),
+    _fields_ = [("n_cases", C.c_int32), ("dv_per_lane", C.c_int32), ("tile_cap", C.c_int32), ("groups", C.c_int32),
                 ("launches_per_step", C.c_int32), ("steps_per_graph", C.c_int32), ("n_tuned", C.c_int32),
                 ("cells", C.c_int64), ("cell_dv", C.c_int64),
-                ("tuned_dv_per_lane", C.c_int32 * 8), ("tuned_tile_cap", C.c_int32 * 8),
+                ("tuned_dv_per_lane", C.c_int32 * 8), ("tuned_tile_cap", C.c_int32 * 8), ("tuned_groups", C.c_int32 * 8),
                 ("tuned_ms_per_step", C.c_double * 8)]
 
 
@@ -459,8 +459,8 @@ class Batch:
         self._check(self._lib.dugks_batch_get_info(self._h, C.byref(b)))
         r = {k: getattr(b, k) for k, _ in BatchInfo._fields_}
         n = b.n_tuned
-        r["tuned"] = [dict(dv_per_lane=b.tuned_dv_per_lane[k], tile_cap=b.tuned_tile_cap[k],
+        r["tuned"] = [dict(dv_per_lane=b.tuned_dv_per_lane[k], tile_cap=b.tuned_tile_cap[k], groups=b.tuned_groups[k],
                            ms_per_step=b.tuned_ms_per_step[k]) for k in range(n)]
-        for k in ("tuned_dv_per_lane", "tuned_tile_cap", "tuned_ms_per_step"):
+        for k in ("tuned_dv_per_lane", "tuned_tile_cap", "tuned_groups", "tuned_ms_per_step"):
             r.pop(k)
         return r

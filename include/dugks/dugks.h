@@ -243,15 +243,17 @@ int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J
 /* ---- batched cases (no counterpart in the reference; SURVEY config 3) ----
  * Independent 2D cases (uneven meshes and velocity grids) advanced together
  * with the FP32 pipeline: every pass of the step is one launch over all cases,
- * two steps are captured in a CUDA graph and replayed.  With autotune != 0
- * the DVs per lane (2 or 4) and the cap on cells per tile are chosen by timing
- * a few steps of each candidate.  Each case starts from its own initial state;
+ * the cases are split into groups whose launch chains are independent
+ * branches of one CUDA graph (two steps per graph, replayed).  With
+ * autotune != 0 the DVs per lane (2 or 4), the cap on cells per tile and the
+ * number of groups are chosen by timing a few steps of each candidate
+ * (otherwise 4 DVs per lane, no cap, 4 groups).  Each case starts from its own initial state;
  * set each case's dt before stepping. */
 typedef struct dugks_batch dugks_batch;
 typedef struct dugks_batch_info {
-    int32_t n_cases, dv_per_lane, tile_cap, launches_per_step, steps_per_graph, n_tuned;
+    int32_t n_cases, dv_per_lane, tile_cap, groups, launches_per_step, steps_per_graph, n_tuned;
     int64_t cells, cell_dv;               /* summed over the cases (cell*DV uses unpadded DVs) */
-    int32_t tuned_dv_per_lane[8], tuned_tile_cap[8];
+    int32_t tuned_dv_per_lane[8], tuned_tile_cap[8], tuned_groups[8];
     double tuned_ms_per_step[8];          /* timing of each candidate */
 } dugks_batch_info;
 
