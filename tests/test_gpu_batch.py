@@ -71,9 +71,10 @@ def test_batch_autotune(built_lib):
     cs = [cases.batch_case(i) for i in _instances()]
     b = solver.Batch(cs, autotune=True)
     info = b.info()
-    assert len(info["tuned"]) == 3 and all(t["ms_per_step"] > 0 for t in info["tuned"])
+    assert len(info["tuned"]) == 5 and all(t["ms_per_step"] > 0 for t in info["tuned"])
     best = min(info["tuned"], key=lambda t: t["ms_per_step"])
-    assert (info["dv_per_lane"], info["tile_cap"]) == (best["dv_per_lane"], best["tile_cap"])
+    assert (info["dv_per_lane"], info["tile_cap"], info["groups"]) == (best["dv_per_lane"], best["tile_cap"],
+                                                                      best["groups"])
     for i, c in enumerate(cs):
         b.set_dt(i, cases.stable_dt(c))
     b.step(3)
