@@ -42,6 +42,11 @@ public:
     virtual size_t batchSmemFace() const { return 0; }
     virtual int batchGatherMF() const { return 0; }
     virtual int batchNpl() const { return 0; }
+    // Launch the step `parity` steps ahead (kernels only: no host bookkeeping),
+    // e.g. into a graph capture.
+    virtual void launchParity(const StepArgs& a, int parity, int sms, cudaStream_t s) {
+        (void)a; (void)parity; (void)sms; (void)s;
+    }
 };
 
 // One launch over several cases: kernel k (0 face sides, 1 face macros,

@@ -293,9 +293,14 @@ public:
     int batchGatherMF() const override { return gatherMF_; }
     int batchNpl() const override { return npl_; }
 
-    void launch(int k, const StepArgs& a, int sms, cudaStream_t s) override {
+    void launchParity(const StepArgs& a, int parity, int sms, cudaStream_t s) override {
+        for (int k = 0; k < nKernels(); ++k) launchArgs(k, stepArgs(a, parity), a, sms, s);
+    }
+
+    void launch(int k, const StepArgs& a, int sms, cudaStream_t s) override { launchArgs(k, stepArgs(a, 0), a, sms, s); }
+
+    void launchArgs(int k, const FusedArgs<S>& A, const StepArgs& a, int sms, cudaStream_t s) {
         (void)sms;
-        const FusedArgs<S> A = stepArgs(a, 0);
         if (k == 0) kFace_<<<plan_.nTiles, kWarps * 32, smemA_, s>>>(A);
         else if (!fp32_) kCell_<<<plan_.nTiles, kWarps * 32, smemB_, s>>>(A);
         else if (k == 1) kMacros_<<<std::max(1, (a.nA + 127) / 128), 128, 0, s>>>(A);  // one face per thread

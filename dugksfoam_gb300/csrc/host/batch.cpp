@@ -33,7 +33,8 @@ int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap, int 
     release();
     npl_ = npl;
     tileCap_ = tileCap;
-    groups_ = std::max(1, std::min(groups, n));
+    perCase_ = groups == 0;  // every case its own graph branch with its own kernels
+    groups_ = perCase_ ? n : std::max(1, std::min(groups, n));
     if (int e = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream")) return e;
     for (int g = 1; g < groups_; ++g) {
         cudaStream_t st = nullptr;
@@ -95,6 +96,17 @@ int Batch::prepare() {
         load[g] += work(i);
     }
     const StepArgs a0 = cases_[0]->stepArgs();
+    base_.clear();
+    for (int i = 0; i < n; ++i) base_.push_back(cases_[i]->stepArgs());
+    if (perCase_) {
+        for (int q = 0; q < 2; ++q) {
+            if (int e = capture(q, 2, graph_[q])) return e;
+            if (int e = capture(q, 1, single_[q])) return e;
+        }
+        dirty_ = false;
+        parity_ = 0;
+        return DUGKS_OK;
+    }
     for (int p = 0; p < 2; ++p) L_[p].assign(groups_, BatchLaunch());
     auto up = [&](const void* src, size_t bytes) -> void* {
         void* ptr = nullptr;
@@ -167,8 +179,12 @@ int Batch::capture(int q, int steps, cudaGraphExec_t& out) {
     for (int k = 1; k < groups_ && ce == cudaSuccess; ++k) ce = cudaStreamWaitEvent(side_[k - 1], ev_[0], 0);
     for (int k = 0; k < groups_; ++k) {
         cudaStream_t st = k == 0 ? stream_ : side_[k - 1];
-        for (int s2 = 0; s2 < steps; ++s2)
-            for (int pass = 0; pass < 3; ++pass) fused_batch_launch(pass, L_[(q + s2) & 1][k], sms_, st);
+        for (int s2 = 0; s2 < steps; ++s2) {
+            if (perCase_)
+                cases_[k]->fusedPipeline()->launchParity(base_[k], (q + s2) & 1, sms_, st);
+            else
+                for (int pass = 0; pass < 3; ++pass) fused_batch_launch(pass, L_[(q + s2) & 1][k], sms_, st);
+        }
     }
     for (int k = 1; k < groups_ && ce == cudaSuccess; ++k) {
         ce = cudaEventRecord(ev_[groups_ + k], side_[k - 1]);
@@ -227,7 +243,7 @@ void Batch::info(dugks_batch_info& o) const {
     o.tile_cap = tileCap_;
     o.launches_per_step = 3;
     o.steps_per_graph = 2;
-    o.groups = groups_;
+    o.groups = perCase_ ? 0 : groups_;
     o.cells = cells_;
     o.cell_dv = cellDV_;
     o.n_tuned = (int32_t)std::min<size_t>(tuneMs_.size(), 8);
@@ -243,11 +259,12 @@ std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int au
     std::unique_ptr<Batch> b(new Batch());
     code = DUGKS_OK;
     if (!descs || n < 1) { err = "batch: need at least one case"; code = DUGKS_ERR_ARG; return nullptr; }
-    int bestNpl = 4, bestCap = 0, bestGroups = 4;
+    int bestNpl = 4, bestCap = 0, bestGroups = 1;
     if (autotune) {
         // candidates: DVs per lane, cap on cells per tile (0: the largest that
         // fits), concurrent groups
-        const int cand[][3] = {{4, 0, 1}, {4, 0, 4}, {4, 0, 8}, {4, 32, 4}, {2, 0, 4}};
+        // (groups 0: every case its own graph branch with its own kernels)
+        const int cand[][3] = {{4, 0, 1}, {4, 0, 4}, {4, 0, 0}, {4, 32, 1}, {2, 0, 1}};
         double best = 1e300;
         for (auto& c : cand) {
             if (int e = b->build(descs, n, c[0], c[1], c[2])) { err = b->err_; code = e; return nullptr; }
@@ -268,7 +285,7 @@ std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int au
             if (rc) { err = b->err_; code = rc; return nullptr; }
             b->tuneNpl_.push_back(c[0]);
             b->tuneCap_.push_back(c[1]);
-            b->tuneGroups_.push_back(b->groups_);
+            b->tuneGroups_.push_back(b->perCase_ ? 0 : b->groups_);
             b->tuneMs_.push_back(ms / 6.0);
             if (ms < best) { best = ms; bestNpl = c[0]; bestCap = c[1]; bestGroups = c[2]; }
         }

@@ -4,7 +4,8 @@
 // cases in one grid); the groups' launch chains are independent branches of
 // one CUDA graph (two steps per graph, replayed), so one group's face sweep
 // overlaps another's cell gather; an autotuner picks the DVs per lane, the
-// tile-size cap and G by timing.
+// tile-size cap and G by timing, or every case as its own branch with its own
+// kernels (G = 0).
 #pragma once
 
 #include <memory>
@@ -47,6 +48,8 @@ private:
     std::vector<cudaStream_t> side_;   // one per group beyond the first (graph capture fork)
     std::vector<cudaEvent_t> ev_;
     int sms_ = 1, npl_ = 4, tileCap_ = 0, groups_ = 1;
+    bool perCase_ = false;
+    std::vector<StepArgs> base_;       // base step arguments of each case at graph build
     std::vector<BatchLaunch> L_[2];    // per parity, per group
     std::vector<void*> dev_;
     cudaGraphExec_t graph_[2] = {nullptr, nullptr};   // two steps from parity q

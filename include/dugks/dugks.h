@@ -246,8 +246,9 @@ int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J
  * the cases are split into groups whose launch chains are independent
  * branches of one CUDA graph (two steps per graph, replayed).  With
  * autotune != 0 the DVs per lane (2 or 4), the cap on cells per tile and the
- * number of groups are chosen by timing a few steps of each candidate
- * (otherwise 4 DVs per lane, no cap, 4 groups).  Each case starts from its own initial state;
+ * number of groups (0: every case its own graph branch with its own kernels)
+ * are chosen by timing a few steps of each candidate (otherwise 4 DVs per
+ * lane, no cap, one group).  Each case starts from its own initial state;
  * set each case's dt before stepping. */
 typedef struct dugks_batch dugks_batch;
 typedef struct dugks_batch_info {
