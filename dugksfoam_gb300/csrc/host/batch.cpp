@@ -241,7 +241,7 @@ void Batch::info(dugks_batch_info& o) const {
     o.n_cases = (int32_t)cases_.size();
     o.dv_per_lane = npl_;
     o.tile_cap = tileCap_;
-    o.launches_per_step = 3;
+    o.launches_per_step = 3 * groups_;  // kernel nodes per step inside the graph (per case or per group)
     o.steps_per_graph = 2;
     o.groups = perCase_ ? 0 : groups_;
     o.cells = cells_;

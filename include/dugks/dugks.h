@@ -252,7 +252,8 @@ int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J
  * set each case's dt before stepping. */
 typedef struct dugks_batch dugks_batch;
 typedef struct dugks_batch_info {
-    int32_t n_cases, dv_per_lane, tile_cap, groups, launches_per_step, steps_per_graph, n_tuned;
+    int32_t n_cases, dv_per_lane, tile_cap, groups, launches_per_step /* kernel nodes per step */, steps_per_graph,
+        n_tuned;
     int64_t cells, cell_dv;               /* summed over the cases (cell*DV uses unpadded DVs) */
     int32_t tuned_dv_per_lane[8], tuned_tile_cap[8], tuned_groups[8];
     double tuned_ms_per_step[8];          /* timing of each candidate */

@@ -23,7 +23,8 @@ def _run_batch(cs, dts):
 
     b = solver.Batch(cs, autotune=False)
     info = b.info()
-    assert info["n_cases"] == 3 and info["launches_per_step"] == 3 and info["dv_per_lane"] == 4
+    assert info["n_cases"] == 3 and info["groups"] == 1 and info["launches_per_step"] == 3
+    assert info["dv_per_lane"] == 4
     for i, dt in enumerate(dts):
         b.set_dt(i, dt)
     b.step(7)          # three graph replays and one single step
