@@ -92,6 +92,8 @@ int fused_tile_cap();
 
 // DVs per lane of the fused kernels for a precision (FP32: DUGKS_NPL, default 4).
 int fused_npl(int precision);
+// FP32 face sweep with per-cell gradients also in 2D (DUGKS_FACE_GRAD=1; 3D always).
+bool fused_face_grad();
 // DV chunk granularity the fused kernels need (the padded DV count must be a multiple).
 int fused_dv_granule(int precision);
 

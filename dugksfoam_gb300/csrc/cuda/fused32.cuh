@@ -75,24 +75,27 @@ __device__ __forceinline__ void stp_cs(float* p, const float2 (&d)[NP]) {
 //             ranges relative to the tile's first entry) and geometry
 //             {S, 1/Vo} {dO, 1/Vn} {dN or wall normal}
 //   [nEnt]    stencil entries {Lx, Ly, Lz, other}
-//   cells (nT2), colour order (nFB), colour offsets (nColors + 1), as ints
-//   padded to whole int4.  The bound allows the planner's 64 colours.
+//   cells (nT2), first stencil entry of each cell of T (nT + 1), as ints
+//   padded to whole int4.
 __host__ __device__ constexpr int tile_meta32_bound(int nFB, int nEnt, int nT2) {
-    return 5 * nFB + nEnt + (nT2 + 3) / 4 + (nFB + 3) / 4 + 17;
+    return 5 * nFB + nEnt + (nT2 + 3) / 4 + (nT2 + 4) / 4;
 }
 
 // Shared memory of the face-sides sweep (all offsets multiples of 16 bytes):
 //   2 x rows(T u H1) | face moments | metadata | face Uref | cell equilibria
 // (the next DV chunk's raw rows stream into the second row buffer).
-template <int D, bool H, int NPL>
+// (GR: gradients of the cells of T kept per chunk, [nT][D][g, h][KC], after the rows.)
+template <int D, bool H, int NPL, bool GR = false>
 struct SmemLayout32 {
     static constexpr int KC = 32 * NPL, NS = Slots<D, H>::NS;
     __host__ __device__ static size_t rows(int n) { return (size_t)n * KC * sizeof(float) * (H ? 2 : 1); }
-    __host__ __device__ static size_t meta(int nRows, int nF) {
-        return 2 * rows(nRows) + (size_t)nF * NS * sizeof(Acc<float>);
+    __host__ __device__ static size_t grad(int nT) { return GR ? (size_t)nT * D * rows(1) : 0; }
+    __host__ __device__ static size_t mom(int nRows, int nT) { return 2 * rows(nRows) + grad(nT); }
+    __host__ __device__ static size_t meta(int nRows, int nF, int nT) {
+        return mom(nRows, nT) + (size_t)nF * NS * sizeof(Acc<float>);
     }
     static size_t sides(const TileDims& d) {
-        return meta(d.nT2, d.nFB) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 16 * (size_t)d.nFB +
+        return meta(d.nT2, d.nFB, d.nT) + 16 * (size_t)tile_meta32_bound(d.nFB, d.nEnt, d.nT2) + 16 * (size_t)d.nFB +
                48 * (size_t)d.nT2;
     }
 };
@@ -101,8 +104,7 @@ struct TileMeta32 {
     const int4* F;    // face records [nFB][5]
     const float4* E;  // stencil entries
     const int* C;     // local -> global cell
-    const int* P;     // faces in colour order
-    const int* O;     // colour offsets
+    const int* S;     // first stencil entry of each cell of T [nT+1]
     float4* dyn;      // per-step tables after the block
 };
 
@@ -118,8 +120,7 @@ __device__ __forceinline__ TileMeta32 stage_meta(const FusedArgs<float>& A, cons
     m.F = sm;
     m.E = reinterpret_cast<const float4*>(sm + 5 * hd.nFB);
     m.C = reinterpret_cast<const int*>(sm + 5 * hd.nFB + hd.nEnt);
-    m.P = reinterpret_cast<const int*>(sm + 5 * hd.nFB + hd.nEnt + (hd.nT2 + 3) / 4);
-    m.O = m.P + 4 * ((hd.nFB + 3) / 4);
+    m.S = reinterpret_cast<const int*>(sm + 5 * hd.nFB + hd.nEnt + (hd.nT2 + 3) / 4);
     m.dyn = reinterpret_cast<float4*>(sm + tile_meta32_bound(hd.nFB, hd.nEnt, hd.nT2));
     return m;
 }
@@ -545,7 +546,94 @@ __device__ __forceinline__ void recon_one32(const FusedArgs<float>& A, const flo
 // face macros.  Face values are stored for the velocities this side owns
 // (tie values are never read: their flux is zero).  Raw rows of the next DV
 // chunk stream into the second row buffer while this chunk's faces run.
+// Least-squares gradients of the cells of T for the chunk (one warp per cell):
+// grad_c = sum_e L_e (gbar+_e - gbar+_c), a wall entry contributing
+// L_b G_b / deltaCoeff (the lagged boundary gradient).
 template <int D, bool H, int NPL, int NW>
+__device__ __forceinline__ void cell_gradients32(const FusedArgs<float>& A, const TileHdr& hd, const TileMeta32& tm,
+                                                 const float* sg, const float* sh, float* gbuf, int lane, int warp,
+                                                 int v0) {
+    constexpr int KC = 32 * NPL, NP = NPL / 2, NR = H ? 2 : 1;
+    const int col = lane * NPL, Vp = A.b.Vp;
+    for (int lc = warp; lc < hd.nT; lc += NW) {
+        float2 c[NP], hc[NP], gg[D][NP], hg[D][NP];
+        ldp<NP>(c, sg + lc * KC + col);
+        if (H) ldp<NP>(hc, sh + lc * KC + col);
+#pragma unroll
+        for (int k = 0; k < D; ++k)
+#pragma unroll
+            for (int p = 0; p < NP; ++p) { gg[k][p] = f2(0.f); hg[k][p] = f2(0.f); }
+        for (int e = tm.S[lc]; e < tm.S[lc + 1]; ++e) {
+            const float4 ent = tm.E[e];
+            const int o = __float_as_int(ent.w);
+            const float Lk[3] = {ent.x, ent.y, ent.z};
+            float2 dg[NP], dh[NP];
+            if (o >= 0) {
+                float2 r[NP], q[NP];
+                ldp<NP>(r, sg + o * KC + col);
+                if (H) ldp<NP>(q, sh + o * KC + col);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    dg[p] = sub2(r[p], c[p]);
+                    if (H) dh[p] = sub2(q[p], hc[p]);
+                }
+            } else {
+                const int wf = -o - 1;
+                const float idc = A.wall4[wf].y;
+                float2 tg[NP], th[NP];
+                ldp<NP>(tg, A.Gbg + (size_t)wf * Vp + v0 + col);
+                if (H) ldp<NP>(th, A.Gbh + (size_t)wf * Vp + v0 + col);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    dg[p] = mul2(tg[p], f2(idc));
+                    if (H) dh[p] = mul2(th[p], f2(idc));
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < D; ++k)
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    gg[k][p] = fma2(f2(Lk[k]), dg[p], gg[k][p]);
+                    if (H) hg[k][p] = fma2(f2(Lk[k]), dh[p], hg[k][p]);
+                }
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            stp<NP>(gbuf + ((lc * D + k) * NR) * KC + col, gg[k]);
+            if (H) stp<NP>(gbuf + ((lc * D + k) * NR + 1) * KC + col, hg[k]);
+        }
+    }
+}
+
+// Face value from cell lc of T: gbar+_c + grad_c . (d - xi dt/2); optionally
+// the normal gradient grad_c . nh (wall update).
+template <int D, bool H, int NPL>
+__device__ __forceinline__ void side_value_g(const Lane32<D, NPL>& L, const float* sg, const float* sh,
+                                             const float* gbuf, int lc, const float* d, float dt, int col,
+                                             float2 (&gv)[NPL / 2], float2 (&hv)[NPL / 2]) {
+    constexpr int KC = 32 * NPL, NP = NPL / 2, NR = H ? 2 : 1;
+    ldp<NP>(gv, sg + lc * KC + col);
+    if (H) ldp<NP>(hv, sh + lc * KC + col);
+    else
+#pragma unroll
+        for (int p = 0; p < NP; ++p) hv[p] = f2(0.f);
+    const float2 hdt = f2(-0.5f * dt);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        float2 gk[NP], hk[NP];
+        ldp<NP>(gk, gbuf + ((lc * D + k) * NR) * KC + col);
+        if (H) ldp<NP>(hk, gbuf + ((lc * D + k) * NR + 1) * KC + col);
+        const float2* xk = k == 0 ? L.x : (k == 1 ? L.y : L.z);
+#pragma unroll
+        for (int p = 0; p < NP; ++p) {
+            const float2 beta = fma2(xk[p], hdt, f2(d[k]));
+            gv[p] = fma2(gk[p], beta, gv[p]);
+            if (H) hv[p] = fma2(hk[p], beta, hv[p]);
+        }
+    }
+}
+
+template <int D, bool H, int NPL, int NW, bool GR>
 __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int tile, unsigned char* smem) {
     using SL = Slots<D, H>;
     constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
@@ -553,13 +641,14 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
     const StepArgs& b = A.b;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Vp = b.Vp, col = lane * NPL;
-    using LY = SmemLayout32<D, H, NPL>;
+    using LY = SmemLayout32<D, H, NPL, GR>;
     float* sg = reinterpret_cast<float*>(smem);
     float* sh = sg + (size_t)hd.nT2 * KC;
     const size_t bufStride = LY::rows(hd.nT2) / sizeof(float);
-    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + 2 * LY::rows(hd.nT2));
+    float* gbuf = reinterpret_cast<float*>(smem + 2 * LY::rows(hd.nT2));  // GR: gradients of T
+    Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + LY::mom(hd.nT2, hd.nT));
     for (int i = threadIdx.x; i < hd.nFB * NS; i += NW * 32) mom[i].zero();
-    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, tile, smem + LY::meta(hd.nT2, hd.nFB));
+    const TileMeta32 tm = stage_meta<NW * 32>(A, hd, tile, smem + LY::meta(hd.nT2, hd.nFB, hd.nT));
     float4* sU = tm.dyn;            // [nFB] face Uref
     float4* ceq = tm.dyn + hd.nFB;  // [nT2][3] cell equilibria
     __syncthreads();
@@ -586,6 +675,10 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
                                           v0 + KC);
         relax_rows32<D, H, NPL, NW>(A, hd, ceq, L, lane, warp, cg, chh);
         __syncthreads();
+        if (GR) {
+            cell_gradients32<D, H, NPL, NW>(A, hd, tm, cg, chh, gbuf, lane, warp, v0);
+            __syncthreads();
+        }
         for (int lf = warp; lf < hd.nFB; lf += NW) {
             Face32 F;
             F.load(tm.F + 5 * lf);
@@ -599,8 +692,18 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
 #pragma unroll
             for (int s = 0; s < NS; ++s) m[s] = 0.0f;
             const size_t fi = (size_t)F.r.a * Vp + v0 + col;
+            const float dO[3] = {F.dOx, F.dOy, F.dOz}, dN[3] = {F.dNx, F.dNy, F.dNz};
             if (F.r.w >= 0) {
-                recon32<D, H, NPL, true>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
+                if (GR) {  // wall: owner side; gw = the owner's gradient (for grad . n)
+                    side_value_g<D, H, NPL>(L, cg, chh, gbuf, F.r.ownL, dO, A.dt, col, gf, hf);
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        ldp<NP>(gw[k], gbuf + ((F.r.ownL * D + k) * (H ? 2 : 1)) * KC + col);
+                        if (H) ldp<NP>(hw[k], gbuf + ((F.r.ownL * D + k) * 2 + 1) * KC + col);
+                    }
+                } else {
+                    recon32<D, H, NPL, true>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
+                }
                 float2 gn[NP], hn[NP], use[NP];
                 float fl = 0.0f;
 #pragma unroll
@@ -623,13 +726,27 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
                 stp<NP>(A.gF + fi, gf);
                 if (H) stp<NP>(A.hF + fi, hf);
             } else if (F.r.ownL < hd.nT && F.r.neiL < hd.nT) {  // both sides in T: complete
-                recon32<D, H, NPL, false>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
+                if (GR) {
+                    float2 go[NP], ho[NP], gn2[NP], hn2[NP];
+                    side_value_g<D, H, NPL>(L, cg, chh, gbuf, F.r.ownL, dO, A.dt, col, go, ho);
+                    side_value_g<D, H, NPL>(L, cg, chh, gbuf, F.r.neiL, dN, A.dt, col, gn2, hn2);
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f, n0 = xs[p].x < 0.f, n1 = xs[p].y < 0.f;
+                        gf[p] = sel2(o0, o1, go[p], sel2(n0, n1, gn2[p], mul2(add2(gn2[p], go[p]), f2(0.5f))));
+                        hf[p] = H ? sel2(o0, o1, ho[p], sel2(n0, n1, hn2[p], mul2(add2(hn2[p], ho[p]), f2(0.5f)))) : f2(0.f);
+                    }
+                } else {
+                    recon32<D, H, NPL, false>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
+                }
                 mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
                 stp<NP>(A.gF + fi, gf);
                 if (H) stp<NP>(A.hF + fi, hf);
             } else {  // one side in T
                 const bool own = F.r.ownL < hd.nT;
-                if (own)
+                if (GR)
+                    side_value_g<D, H, NPL>(L, cg, chh, gbuf, own ? F.r.ownL : F.r.neiL, own ? dO : dN, A.dt, col, gf, hf);
+                else if (own)
                     recon_one32<D, H, NPL>(A, tm.E, F.r.stO0, F.r.stO1, F.r.ownL, F.dOx, F.dOy, F.dOz, L, cg, chh, lane,
                                            v0, gf, hf);
                 else
@@ -670,10 +787,10 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
     }
 }
 
-template <int D, bool H, int NPL, int NW>
+template <int D, bool H, int NPL, int NW, bool GR>
 __global__ void __launch_bounds__(NW * 32, 1) k_face_sides32(FusedArgs<float> A) {
     extern __shared__ __align__(16) unsigned char smem[];
-    face_sides_body<D, H, NPL, NW>(A, blockIdx.x, smem);
+    face_sides_body<D, H, NPL, NW, GR>(A, blockIdx.x, smem);
 }
 
 // Several independent cases in one launch: block b runs tile work[b].y of
@@ -691,7 +808,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_face_sides32_batch(const FusedAr
         for (int k = threadIdx.x; k < (int)(sizeof(FusedArgs<float>) / 8); k += blockDim.x) dst[k] = src[k];
     }
     __syncthreads();
-    face_sides_body<D, H, NPL, NW>(sA, w.y, smem);
+    face_sides_body<D, H, NPL, NW, false>(sA, w.y, smem);
 }
 
 // Face macros of every active face from the two per-side moment totals.

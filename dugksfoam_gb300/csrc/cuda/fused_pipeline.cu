@@ -25,6 +25,11 @@ int fused_npl(int precision) {
     return (npl == 2 || npl == 4) ? npl : 4;  // packed pairs: an even count per lane
 }
 
+bool fused_face_grad() {
+    const char* e = std::getenv("DUGKS_FACE_GRAD");
+    return e && e[0] == '1';
+}
+
 int fused_dv_granule(int precision) { return 32 * fused_npl(precision); }
 
 std::unique_ptr<FusedPipeline> make_fused_pipeline(Solver& s, const StepArgs& a, int precision, std::string& err) {

@@ -122,8 +122,9 @@ public:
                 }
                 for (int e = 0; e < h.nEnt; ++e) meta.push_back(f4i(st4[(size_t)base + e]));
                 ints(&plan_.cells[h.cellStart], h.nT2);
-                ints(&plan_.colorPerm[h.permStart], h.nFB);
-                ints(&plan_.colorOff[h.colStart], h.nColors + 1);
+                std::vector<int32_t> cst(h.nT + 1);  // T cells' stencil ranges, tile-relative
+                for (int i = 0; i <= h.nT; ++i) cst[i] = plan_.stOff[h.stStart + i] - base;
+                ints(cst.data(), h.nT + 1);
                 const int n16 = (int)meta.size() - metaOff.back();
                 if (n16 > tile_meta32_bound(h.nFB, h.nEnt, h.nT2)) { err = "tile metadata exceeds its bound"; return false; }
             }
@@ -345,9 +346,9 @@ public:
     size_t bytes() const override { return bytes_; }
     std::string describe() const override {
         char buf[256];
-        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d smemA=%zu smemB=%zu gatherMF=%d",
+        snprintf(buf, sizeof(buf), "tiles=%d maxT=%d meanT=%.1f halo=%.2f maxT2=%d maxFB=%d npl=%d grad=%d smemA=%zu smemB=%zu gatherMF=%d",
                  plan_.nTiles, plan_.maxT, (double)plan_.sumT / std::max(1, plan_.nTiles),
-                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, smemA_, smemB_, gatherMF_);
+                 (double)plan_.sumT2 / std::max(1LL, plan_.sumT), plan_.maxT2, plan_.maxFB, npl_, (int)grad_, smemA_, smemB_, gatherMF_);
         return buf;
     }
 
@@ -375,7 +376,9 @@ private:
     template <int D, bool H, int NPL>
     void set() {
         if constexpr (sizeof(S) == 4) {
-            kFace_ = k_face_sides32<D, H, NPL, kWarps>;
+            // 3D: per-cell gradients once per chunk (six stencil entries a side, three faces a cell)
+            grad_ = D == 3 || fused_face_grad();
+            kFace_ = grad_ ? k_face_sides32<D, H, NPL, kWarps, true> : k_face_sides32<D, H, NPL, kWarps, false>;
             kMacros_ = k_face_macros32<D, H>;
             kGather_ = k_cell_gather32<D, H, NPL, kGatherWarps>;
             kRef_ = k_ref_tables<D, H>;
@@ -385,7 +388,7 @@ private:
         }
         kTables_ = k_wall_tables<S, D, H>;
         if constexpr (sizeof(S) == 4) {
-            smemFaceFn_ = &SmemLayout32<D, H, NPL>::sides;
+            smemFaceFn_ = grad_ ? &SmemLayout32<D, H, NPL, true>::sides : &SmemLayout32<D, H, NPL, false>::sides;
             smemCellFn_ = nullptr;
         } else {
             smemFaceFn_ = &SmemLayout<S, D, H, NPL>::face;
@@ -409,7 +412,7 @@ private:
     size_t smemCell(const TileDims& d) const { return smemCellFn_(d); }
 
     int D_ = 2, npl_ = 1;
-    bool fp32_ = false;
+    bool fp32_ = false, grad_ = false;
     KernelFn kMacros_ = nullptr;
     int gatherMF_ = 0, gatherBlocks_ = 1;
     size_t gatherSmem_ = 0;
