@@ -73,42 +73,56 @@ __device__ __forceinline__ R tauT(R T, R rho, R muRef, double omega, double Tref
 // a = |c|^2/theta, G0 = (2 pi theta)^(-D/2) exp(-a/2), kap = (1-Pr)/(5 theta^2):
 //   gE = rho G0 + kap (c.q)(a - D - 2) G0
 //   hE = theta [k3 rho G0 + kap (c.q) B G0],  k3 = K+3-D,  B = (a-D) k3 - 2K.
-__device__ __forceinline__ void shakhov_jac(const double* m, double x0, double x1, double x2, double Rg, double Pr,
-                                            int D, int K, double& gE, double& hE, double* dg, double* dh) {
-    const double rho = m[0], th = Rg * m[4];
-    const double c[3] = {x0 - m[1], x1 - m[2], x2 - m[3]};
-    const double q[3] = {m[5], m[6], m[7]};
-    const double a = (c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) / th;
-    const double s = sqrt(2.0 * kPi * th);
-    const double pw = (D == 2) ? s * s : (D == 3 ? s * s * s : s);
-    const double G0 = exp(-a / 2.0) / pw;
-    const double kap = (1.0 - Pr) / (5.0 * th * th);
-    const double cq = c[0] * q[0] + c[1] * q[1] + c[2] * q[2];
-    const double k3 = K + 3.0 - D, B = (a - D) * k3 - 2.0 * K, P = a - D - 2.0;
-    gE = rho * G0 + kap * cq * P * G0;
-    const double H = k3 * rho * G0 + kap * cq * B * G0;
-    hE = th * H;
-    // rho
-    dg[0] = G0;
-    dh[0] = th * k3 * G0;
-    // U_k
-    for (int k = 0; k < 3; ++k) {
-        const double ck = c[k] / th;
-        dg[1 + k] = rho * G0 * ck + kap * G0 * (-q[k] * P + cq * (-2.0 * ck) + cq * P * ck);
-        dh[1 + k] = th * (k3 * rho * G0 * ck + kap * G0 * (-q[k] * B + cq * k3 * (-2.0 * ck) + cq * B * ck));
+// The per-entity factors (1/theta, the normalisation, kap) are formed once
+// (ShakhovJac::prep); each velocity then costs one exp and products.
+struct ShakhovJac {
+    double rho, U[3], q[3], th, ith, N, kap, R, k3, K2;
+    int D;
+    __device__ __forceinline__ void prep(const double* m, double Rg, double Pr, int Dd, int K) {
+        rho = m[0];
+        for (int k = 0; k < 3; ++k) { U[k] = m[1 + k]; q[k] = m[5 + k]; }
+        th = Rg * m[4];
+        ith = 1.0 / th;
+        const double s = sqrt(2.0 * kPi * th);
+        N = 1.0 / ((Dd == 2) ? s * s : (Dd == 3 ? s * s * s : s));
+        kap = (1.0 - Pr) / 5.0 * ith * ith;
+        R = Rg;
+        D = Dd;
+        k3 = K + 3.0 - Dd;
+        K2 = 2.0 * K;
     }
-    // T (via theta)
-    const double dG0 = G0 * (a - D) / (2.0 * th);
-    const double dgth = rho * dG0 + cq * (-2.0 * kap / th * P * G0 + kap * (-a / th) * G0 + kap * P * dG0);
-    const double dHth = k3 * rho * dG0 + cq * (-2.0 * kap / th * B * G0 + kap * k3 * (-a / th) * G0 + kap * B * dG0);
-    dg[4] = Rg * dgth;
-    dh[4] = Rg * (H + th * dHth);
-    // q_k
-    for (int k = 0; k < 3; ++k) {
-        dg[5 + k] = kap * c[k] * P * G0;
-        dh[5 + k] = th * kap * c[k] * B * G0;
+    __device__ __forceinline__ void eval(double x0, double x1, double x2, double& gE, double& hE, double* dg,
+                                         double* dh) const {
+        const double c[3] = {x0 - U[0], x1 - U[1], x2 - U[2]};
+        const double a = (c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) * ith;
+        const double G0 = N * exp(-0.5 * a);
+        const double cq = c[0] * q[0] + c[1] * q[1] + c[2] * q[2];
+        const double B = (a - D) * k3 - K2, P = a - D - 2.0;
+        const double kG = kap * G0, kGcq = kG * cq;
+        gE = rho * G0 + kGcq * P;
+        const double H = k3 * rho * G0 + kGcq * B;
+        hE = th * H;
+        dg[0] = G0;
+        dh[0] = th * k3 * G0;
+        // U_k: with ck = c_k / theta
+        const double gU = rho * G0 + kGcq * (P - 2.0), hU = k3 * rho * G0 + kGcq * (B - 2.0 * k3);
+        for (int k = 0; k < 3; ++k) {
+            const double ck = c[k] * ith;
+            dg[1 + k] = gU * ck - kG * q[k] * P;
+            dh[1 + k] = hU * c[k] - th * kG * q[k] * B;
+        }
+        // T via theta: dG0/dtheta = G0 (a - D) / (2 theta)
+        const double hd = 0.5 * (a - D) * ith;
+        const double dgth = rho * G0 * hd + kGcq * ith * (-2.0 * P - a + P * (a - D) * 0.5);
+        const double dHth = k3 * rho * G0 * hd + kGcq * ith * (-2.0 * B - k3 * a + B * (a - D) * 0.5);
+        dg[4] = R * dgth;
+        dh[4] = R * (H + th * dHth);
+        for (int k = 0; k < 3; ++k) {
+            dg[5 + k] = kG * c[k] * P;
+            dh[5 + k] = th * kG * c[k] * B;
+        }
     }
-}
+};
 
 // ============================================================ tangent-linear
 struct TArgs {
@@ -692,11 +706,13 @@ __global__ void r_face(AArgs A, const double* gS, const double* hS, const double
     // P7: relaxed = (1-b) gS + b gE(mF) on relaxed DVs
     double acc[kM];
     for (int i = 0; i < kM; ++i) acc[i] = 0.0;
+    ShakhovJac J;
+    J.prep(m, a.R, a.Pr, a.D, a.K);
     for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
         double x0 = a.xi[v], x1 = a.xi[Vp + v], x2 = a.xi[2 * Vp + v];
         if (wall && !(x0 * S[0] + x1 * S[1] + x2 * S[2] > 0)) continue;
         double gE, hE, dg[8], dh[8];
-        shakhov_jac(m, x0, x1, x2, a.R, a.Pr, a.D, a.K, gE, hE, dg, dh);
+        J.eval(x0, x1, x2, gE, hE, dg, dh);
         const double lg = lgS[base + v], lh = a.hasH ? lhS[base + v] : 0.0;
         for (int k = 0; k < 8; ++k) acc[k] += b * (dg[k] * lg + (a.hasH ? dh[k] * lh : 0.0));
         acc[8] += db * ((gE - gS[base + v]) * lg + (a.hasH ? (hE - hS[base + v]) * lh : 0.0));
@@ -869,9 +885,11 @@ __global__ void r_barp(AArgs A, const double* gT, const double* hT, const double
     const double dr = -3.0 * a.dt / ((2.0 * m[8] + a.dt) * (2.0 * m[8] + a.dt));
     double acc[kM];
     for (int i = 0; i < kM; ++i) acc[i] = 0.0;
+    ShakhovJac J;
+    J.prep(m, a.R, a.Pr, a.D, a.K);
     for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
         double gE, hE, dg[8], dh[8];
-        shakhov_jac(m, a.xi[v], a.xi[Vp + v], a.xi[2 * Vp + v], a.R, a.Pr, a.D, a.K, gE, hE, dg, dh);
+        J.eval(a.xi[v], a.xi[Vp + v], a.xi[2 * Vp + v], gE, hE, dg, dh);
         const double lg = lgB[base + v], lh = a.hasH ? lhB[base + v] : 0.0;
         for (int k = 0; k < 8; ++k) acc[k] += r * (dg[k] * lg + (a.hasH ? dh[k] * lh : 0.0));
         acc[8] += dr * ((gE - gT[base + v]) * lg + (a.hasH ? (hE - hT[base + v]) * lh : 0.0));
