@@ -176,7 +176,7 @@ def make_case(args):
     if args.workload == "cavity2d":
         return cases.cavity2d(61, nxi=28), "cavity2d: 61x61 quads, 28x28 DV, Kn 0.075"
     if args.workload == "cavity3d":
-        return cases.cavity3d(48, nxi=20), "cavity3d: 48^3 hexes, 20^3 DV, Kn 0.1"
+        return cases.cavity3d(args.n3d, nxi=20), f"cavity3d: {args.n3d}^3 hexes, 20^3 DV, Kn 0.1"
     raise SystemExit(f"unknown workload {args.workload}")
 
 
@@ -356,6 +356,7 @@ def main():
     ap.add_argument("--delaunay-interior", type=int, default=49200,
                     help="interior points of the delaunay2d mesh (49200 -> ~100k triangles)")
     ap.add_argument("--delaunay-side", type=int, default=400, help="points per side of the delaunay2d boundary")
+    ap.add_argument("--n3d", type=int, default=48, help="hexes per side of the cavity3d mesh")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
