@@ -1,0 +1,51 @@
+"""Accuracy of the FP32 / FP64-moment step against the plain FP64 step on a
+workload, after a stated number of steps: field-normalised L-inf and L2
+errors of rho, U, T, q (vector fields by the magnitude of the difference).
+The FP64 reference is the plain FP64 GPU pipeline, which the parity tests pin
+to the CPU oracle at 1e-12.  One JSON line on stdout."""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    if a.ndim == 2:
+        d, r = np.linalg.norm(a - b, axis=1), np.linalg.norm(b, axis=1)
+    else:
+        d, r = np.abs(a - b), np.abs(b)
+    return dict(linf=float(d.max() / r.max()), l2=float(np.linalg.norm(d) / np.linalg.norm(r)))
+
+
+def main(argv=None):
+    from . import cases, solver
+
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--workload", default="delaunay2d", choices=["delaunay2d", "cavity2d", "cavity3d"])
+    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--n3d", type=int, default=48)
+    a = ap.parse_args(argv)
+    case = {"delaunay2d": lambda: cases.delaunay2d(), "cavity2d": lambda: cases.cavity2d(61, nxi=28),
+            "cavity3d": lambda: cases.cavity3d(a.n3d, nxi=20)}[a.workload]()
+    dt = cases.case_dt(case)
+    out = dict(workload=a.workload, steps=a.steps, dt=dt)
+    fields = {}
+    for name, prec, pipe in (("fp32", solver.FP32_FP64MOM, solver.PIPE_FUSED), ("fp64", solver.FP64, solver.PIPE_REFERENCE)):
+        s = solver.FvDVM(case, precision=prec, pipeline=pipe)
+        s.set_dt(dt)
+        t = time.perf_counter()
+        s.evolution(a.steps)
+        fields[name] = s.macros()
+        out[f"seconds_{name}"] = time.perf_counter() - t
+        out["cells"], out["dvs"] = s.nCells, s.nDV
+        s.close()
+    out["error_fp32_vs_fp64"] = {k: rel_err(fields["fp32"][k], fields["fp64"][k]) for k in ("rho", "U", "T", "q")}
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()
