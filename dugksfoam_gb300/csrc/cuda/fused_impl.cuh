@@ -1,8 +1,12 @@
-// Fused tile sweeps of one DUGKS step (fvDVM::evolution, fvDVM.C:1086-1108).
+// Shared pieces of the fused steps (fvDVM::evolution, fvDVM.C:1086-1108): the
+// argument block, moment slots and the warp reduce-scatter, compensated
+// accumulators, macros from one-pass central moments, the FP32 equilibrium
+// coefficient block; and the FP64 two-sweep tile algorithm of
+// fused_kernels.cuh (the FP32 step, fused32.cuh, reuses the shared pieces).
 //
-// One CTA owns one tile T of cells plus its two-ring halo (H1, H2) and walks
-// the discrete-velocity axis in chunks of KC = 32*NPL velocities (lane <-> DV,
-// the DV index is innermost in HBM so every row load is coalesced).
+// FP64 sweeps: one CTA owns one tile T of cells plus its two-ring halo (H1,
+// H2) and walks the discrete-velocity axis in chunks of KC velocities (lane
+// <-> DV, the DV index is innermost in HBM so every row load is coalesced).
 //
 // Sweep A (k_sweep_face): per chunk
 //   1. g~ rows of T u H1 u H2 -> gbar+ = (1-a) g~ + a g^S(cell macros) in smem
@@ -11,8 +15,8 @@
 //      recomputed from smem (P2, discreteVelocity.C:420-470), upwind linear
 //      reconstruction with the -xi dt/2 shift (P3, :472-691), lagged boundary
 //      gradient update on walls, and the face moments (per-lane products,
-//      warp reduce-scatter, compensated accumulation per face in smem).
-//   After the chunk loop (FP64): Maxwell-wall density (P4, fvDVM.C:347-367),
+//      warp reduce-scatter, accumulation per face in smem).
+//   After the chunk loop: Maxwell-wall density (P4, fvDVM.C:347-367),
 //   incoming wall moments rho_w * M (P5), face macros rho,U,T,tau,q (P6, :456-582).
 // Sweep B (k_sweep_cell): per chunk
 //   1. gbar+ rows again; g~new partial = -1/3 g~ + 4/3 gbar+ for T;
@@ -21,16 +25,16 @@
 //      flux (xi.S) g_f dt/V scattered into T's rows colour by colour (no two
 //      faces of a colour share a cell: deterministic, no atomics) (P8, :934-978);
 //   3. g~new written to HBM, cell moments accumulated (P9, fvDVM.C:597-728).
-//   After the chunk loop (FP64): cell macros rho,U,T,tau,q for the next step.
+//   After the chunk loop: cell macros rho,U,T,tau,q for the next step.
 //
 // Moments are accumulated about a reference velocity Uref (previous face /
 // cell velocity, or the wall velocity), so the heat flux needs one pass:
 //   q_i = 1/2 [M3_i - 2 M2_ij d_j + M1_i |d|^2 - d_i tr M2 + 2 d_i (M1.d)
 //              - d_i |d|^2 M0] + 1/2 (H1_i - d_i H0),   d = M1/M0 = U - Uref.
 //
-// FP32 path: no FP64 instruction runs inside the chunk loops (GB300 issues
-// FP64 at 1/64 of the FP32 rate); per-chunk warp totals are added into an
-// FP32 Kahan pair per face/cell and finished in FP64.
+// FP32 accumulation (fused32.cuh): no FP64 instruction inside the chunk loops
+// (GB300 issues FP64 at 1/64 of the FP32 rate); per-chunk warp totals go into
+// an FP32 Kahan pair per face/cell and are finished in FP64.
 #pragma once
 
 #include "../host/tile_plan.h"
@@ -52,13 +56,10 @@ struct FusedArgs {
     const TileFace* faces;
     const int* colorOff;
     const int* colorPerm;
-    // stencils: FP32 packs (Lx, Ly, Lz, other) in a float4; FP64 uses stEnt/stL
-    const float4* st4;
+    // stencils (FP64 sweeps): other local cell (>= 0) or -(wall+1), LS vector
     const int* stEnt;
     const double* stL;
-    // face geometry: FP32 [rec][3] float4 {S,1/Vo} {dO,1/Vn} {dN or wall normal};
-    // FP64 [rec][9] S, dO, dN
-    const float4* fg4;
+    // face geometry (FP64 sweeps): [rec][9] S, dO, dN
     const double* fgeo;
     // discrete velocities
     const S* xi;                // [3][Vp]
@@ -208,49 +209,6 @@ struct Relax<double, D, H> {
     }
 };
 
-template <int D, bool H>
-struct Relax<float, D, H> {
-    float U[3], kexp, invRT, qk[3], a, aA, RT;
-    float KD, K2;
-    __device__ __forceinline__ void loadBlock(const float* blk, float aw, int K) {
-        const float4 b0 = reinterpret_cast<const float4*>(blk)[0];
-        const float4 b1 = reinterpret_cast<const float4*>(blk)[1];
-        const float4 b2 = reinterpret_cast<const float4*>(blk)[2];
-        U[0] = b0.x; U[1] = b0.y; U[2] = b0.z; kexp = b0.w;
-        invRT = b1.x; qk[0] = b1.y; qk[1] = b1.z; qk[2] = b1.w;
-        RT = b2.y;
-        a = aw;
-        aA = aw * b2.x;
-        KD = (float)(K + 3 - D);
-        K2 = -2.0f * (float)K;
-    }
-    __device__ __forceinline__ void loadCell(const FusedArgs<float>& A, int c) {
-        const float* blk = A.cc + (size_t)c * kNCoef;
-        const float tau = blk[10];
-        loadBlock(blk, 1.5f * A.dt / (2.0f * tau + A.dt), A.b.K);
-    }
-    __device__ __forceinline__ void loadFace(const FusedArgs<float>& A, int f) {
-        const float* blk = A.fc + (size_t)f * kNCoef;
-        const float tau = blk[10];
-        const float hh = 0.5f * A.dt;
-        loadBlock(blk, hh / (2.0f * tau + hh), A.b.K);
-    }
-    // g <- g - a g + a g^S: the weight 1-a is never formed, so a state already
-    // at equilibrium is a fixed point in FP32 (no per-step mass bias).
-    __device__ __forceinline__ void apply(const float* xi, float& g, float& h) const {
-        const float cx = xi[0] - U[0], cy = xi[1] - U[1];
-        const float cz = D == 3 ? xi[2] - U[2] : 0.0f;
-        const float c2 = D == 3 ? fmaf(cz, cz, fmaf(cy, cy, cx * cx)) : fmaf(cy, cy, cx * cx);
-        const float e = exp2f(kexp * c2) * aA;
-        const float phi = D == 3 ? fmaf(cz, qk[2], fmaf(cy, qk[1], cx * qk[0])) : fmaf(cy, qk[1], cx * qk[0]);
-        const float c2n = c2 * invRT;
-        g = fmaf(-a, g, g) + fmaf(e * phi, c2n - (float)(D + 2), e);
-        if (H) {
-            const float eh = e * RT;
-            h = fmaf(-a, h, h) + fmaf(eh * phi, fmaf(c2n - (float)D, KD, K2), eh * KD);
-        }
-    }
-};
 
 // ------------------------------------------------------------- gradient
 // Least-squares gradient of gbar+ at a local cell from its stencil entries
@@ -261,46 +219,23 @@ __device__ __forceinline__ void stencil_grad(const FusedArgs<S>& A, int e0, int 
 #pragma unroll
     for (int k = 0; k < D; ++k) { gg[k] = S(0); if (H) hg[k] = S(0); }
     for (int e = e0; e < e1; ++e) {
-        if constexpr (sizeof(S) == 4) {
-            const float4 ent = A.st4[e];
-            const int o = __float_as_int(ent.w);
-            float dg, dh = 0.0f;
-            if (o >= 0) {
-                dg = sg[o * KC + col] - gc;
-                if (H) dh = sh[o * KC + col] - hc;
-            } else {
-                const int wf = -o - 1;
-                const float idc = A.wall4[wf].y;
-                dg = A.Gbg[(size_t)wf * A.b.Vp + v] * idc;
-                if (H) dh = A.Gbh[(size_t)wf * A.b.Vp + v] * idc;
-            }
-            gg[0] = fmaf(ent.x, dg, gg[0]);
-            gg[1] = fmaf(ent.y, dg, gg[1]);
-            if (D == 3) gg[2] = fmaf(ent.z, dg, gg[2]);
-            if (H) {
-                hg[0] = fmaf(ent.x, dh, hg[0]);
-                hg[1] = fmaf(ent.y, dh, hg[1]);
-                if (D == 3) hg[2] = fmaf(ent.z, dh, hg[2]);
-            }
-        } else {
-            const int o = A.stEnt[e];
-            double dg, dh = 0.0;
-            if (o >= 0) {
-                dg = sg[o * KC + col] - gc;
-                if (H) dh = sh[o * KC + col] - hc;
-            } else {  // fixedGradient evaluate, then difference (reference order)
-                const int wf = -o - 1;
-                const size_t wi = (size_t)wf * A.b.Vp + v;
-                const double dc = A.b.dcW[wf];
-                dg = (gc + A.Gbg[wi] / dc) - gc;
-                if (H) dh = (hc + A.Gbh[wi] / dc) - hc;
-            }
-            const double* L = A.stL + 3 * (size_t)e;
+        const int o = A.stEnt[e];
+        double dg, dh = 0.0;
+        if (o >= 0) {
+            dg = sg[o * KC + col] - gc;
+            if (H) dh = sh[o * KC + col] - hc;
+        } else {  // fixedGradient evaluate, then difference (reference order)
+            const int wf = -o - 1;
+            const size_t wi = (size_t)wf * A.b.Vp + v;
+            const double dc = A.b.dcW[wf];
+            dg = (gc + A.Gbg[wi] / dc) - gc;
+            if (H) dh = (hc + A.Gbh[wi] / dc) - hc;
+        }
+        const double* L = A.stL + 3 * (size_t)e;
 #pragma unroll
-            for (int k = 0; k < D; ++k) {
-                gg[k] += L[k] * dg;
-                if (H) hg[k] += L[k] * dh;
-            }
+        for (int k = 0; k < D; ++k) {
+            gg[k] += L[k] * dg;
+            if (H) hg[k] += L[k] * dh;
         }
     }
 }
@@ -320,17 +255,10 @@ struct FaceGeo {
     S Sv[3], dO[3], dN[3];
     S invVo, invVn;
     __device__ __forceinline__ void load(const FusedArgs<S>& A, int rec) {
-        if constexpr (sizeof(S) == 4) {
-            const float4 a = A.fg4[3 * (size_t)rec], b = A.fg4[3 * (size_t)rec + 1], c = A.fg4[3 * (size_t)rec + 2];
-            Sv[0] = a.x; Sv[1] = a.y; Sv[2] = a.z; invVo = a.w;
-            dO[0] = b.x; dO[1] = b.y; dO[2] = b.z; invVn = b.w;
-            dN[0] = c.x; dN[1] = c.y; dN[2] = c.z;
-        } else {
-            const double* g = A.fgeo + 9 * (size_t)rec;
+        const double* g = A.fgeo + 9 * (size_t)rec;
 #pragma unroll
-            for (int k = 0; k < 3; ++k) { Sv[k] = g[k]; dO[k] = g[3 + k]; dN[k] = g[6 + k]; }
-            invVo = invVn = 0.0;
-        }
+        for (int k = 0; k < 3; ++k) { Sv[k] = g[k]; dO[k] = g[3 + k]; dN[k] = g[6 + k]; }
+        invVo = invVn = 0.0;
     }
 };
 

@@ -62,10 +62,12 @@ public:
 
         // ---- upload plan
         args_.hdr = upload(plan_.hdr);
-        args_.cells = upload(plan_.cells);
-        args_.faces = upload(plan_.faces);
-        args_.colorOff = upload(plan_.colorOff);
-        args_.colorPerm = upload(plan_.colorPerm);
+        if (!fp32_) {  // the FP32 kernels read per-tile metadata blocks instead
+            args_.cells = upload(plan_.cells);
+            args_.faces = upload(plan_.faces);
+            args_.colorOff = upload(plan_.colorOff);
+            args_.colorPerm = upload(plan_.colorPerm);
+        }
         const size_t nRec = plan_.faces.size();
         if (sizeof(S) == 4) {
             std::vector<float4> st4(plan_.stEnt.size());
@@ -75,7 +77,6 @@ public:
                 std::memcpy(&ow, &o, 4);
                 st4[e] = make_float4((float)plan_.stL[3 * e], (float)plan_.stL[3 * e + 1], (float)plan_.stL[3 * e + 2], ow);
             }
-            args_.st4 = upload(st4);
             std::vector<float4> fg4(3 * nRec);
             for (size_t k = 0; k < nRec; ++k) {
                 const TileFace& r = plan_.faces[k];
@@ -93,7 +94,6 @@ public:
                 fg4[3 * k + 1] = make_float4((float)dO[0], (float)dO[1], (float)dO[2], (float)iVn);
                 fg4[3 * k + 2] = make_float4((float)dN[0], (float)dN[1], (float)dN[2], 0.0f);
             }
-            args_.fg4 = upload(fg4);
             // per-tile blocks: face records (stencil ranges relative to the
             // tile's first entry) + geometry, entries, cells, colour order
             std::vector<int4> meta;
