@@ -68,62 +68,6 @@ __device__ __forceinline__ R tauT(R T, R rho, R muRef, double omega, double Tref
     return muRef * exp(omega * log(T / Tref)) / rho / T / Rg;
 }
 
-// Shakhov equilibrium and its partial derivatives with respect to
-// m = (rho, Ux, Uy, Uz, T, qx, qy, qz).  With theta = R T, c = xi - U,
-// a = |c|^2/theta, G0 = (2 pi theta)^(-D/2) exp(-a/2), kap = (1-Pr)/(5 theta^2):
-//   gE = rho G0 + kap (c.q)(a - D - 2) G0
-//   hE = theta [k3 rho G0 + kap (c.q) B G0],  k3 = K+3-D,  B = (a-D) k3 - 2K.
-// The per-entity factors (1/theta, the normalisation, kap) are formed once
-// (ShakhovJac::prep); each velocity then costs one exp and products.
-struct ShakhovJac {
-    double rho, U[3], q[3], th, ith, N, kap, R, k3, K2;
-    int D;
-    __device__ __forceinline__ void prep(const double* m, double Rg, double Pr, int Dd, int K) {
-        rho = m[0];
-        for (int k = 0; k < 3; ++k) { U[k] = m[1 + k]; q[k] = m[5 + k]; }
-        th = Rg * m[4];
-        ith = 1.0 / th;
-        const double s = sqrt(2.0 * kPi * th);
-        N = 1.0 / ((Dd == 2) ? s * s : (Dd == 3 ? s * s * s : s));
-        kap = (1.0 - Pr) / 5.0 * ith * ith;
-        R = Rg;
-        D = Dd;
-        k3 = K + 3.0 - Dd;
-        K2 = 2.0 * K;
-    }
-    __device__ __forceinline__ void eval(double x0, double x1, double x2, double& gE, double& hE, double* dg,
-                                         double* dh) const {
-        const double c[3] = {x0 - U[0], x1 - U[1], x2 - U[2]};
-        const double a = (c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) * ith;
-        const double G0 = N * exp(-0.5 * a);
-        const double cq = c[0] * q[0] + c[1] * q[1] + c[2] * q[2];
-        const double B = (a - D) * k3 - K2, P = a - D - 2.0;
-        const double kG = kap * G0, kGcq = kG * cq;
-        gE = rho * G0 + kGcq * P;
-        const double H = k3 * rho * G0 + kGcq * B;
-        hE = th * H;
-        dg[0] = G0;
-        dh[0] = th * k3 * G0;
-        // U_k: with ck = c_k / theta
-        const double gU = rho * G0 + kGcq * (P - 2.0), hU = k3 * rho * G0 + kGcq * (B - 2.0 * k3);
-        for (int k = 0; k < 3; ++k) {
-            const double ck = c[k] * ith;
-            dg[1 + k] = gU * ck - kG * q[k] * P;
-            dh[1 + k] = hU * c[k] - th * kG * q[k] * B;
-        }
-        // T via theta: dG0/dtheta = G0 (a - D) / (2 theta)
-        const double hd = 0.5 * (a - D) * ith;
-        const double dgth = rho * G0 * hd + kGcq * ith * (-2.0 * P - a + P * (a - D) * 0.5);
-        const double dHth = k3 * rho * G0 * hd + kGcq * ith * (-2.0 * B - k3 * a + B * (a - D) * 0.5);
-        dg[4] = R * dgth;
-        dh[4] = R * (H + th * dHth);
-        for (int k = 0; k < 3; ++k) {
-            dg[5 + k] = kG * c[k] * P;
-            dh[5 + k] = th * kG * c[k] * B;
-        }
-    }
-};
-
 // ============================================================ tangent-linear
 struct TArgs {
     StepArgs a;
@@ -513,143 +457,336 @@ __global__ void k_objective(int nW, const double* wq, const double* ws, const R*
 // Per-cell adjoint of the macro tuple m = (rho, Ux, Uy, Uz, T, qx, qy, qz, tau)
 // (9 doubles per cell; P1 of the next step reads all nine).
 constexpr int kM = 9;
+constexpr int kAW = 4;  // warps per block of the warp-per-entity reverse kernels
 
 struct AArgs {
     StepArgs a;
     const double* Tw;   // wall temperatures (forward values)
     double muRef;
+    int M;              // velocities per direction: v = (iz M + iy) M + ix (fvDVM.C:151-221)
 };
 
-// Reverse of the macro evaluation (P9 for cells, P6 for faces) for one
-// entity: given lm (adjoint of rho, U, T, q, tau with q = fac(tau) Q) and the
-// distributions, accumulate the adjoint of g, h and return the mu_ref part.
-// facA: fac = 2 tau / (2 tau + facA) (cells: dt Pr, faces: dt Pr / 2).
-// Optional wall seeds: lqw (adjoint of qWall), lsw (adjoint of stressWall) with
-// fq = fac, fs = 2 tau / (2 tau + dt/2), moments about the wall velocity Uw.
-__device__ void macro_reverse(const StepArgs& a, const double* g, const double* h, double* lg, double* lh,
-                              const double* lm, double facA, double muRef, bool wall, const double* Uw,
-                              const double* lqw, const double* lsw, double* red, double& lmu) {
-    const int Vp = a.Vp;
-    double m[5] = {0, 0, 0, 0, 0};
-    for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
-        double x0 = a.xi[v], x1 = a.xi[Vp + v], x2 = a.xi[2 * Vp + v], w = a.w[v];
-        double gv = g[v], hv = a.hasH ? h[v] : 0.0;
-        m[0] += w * gv;
-        m[1] += w * gv * x0;
-        m[2] += w * gv * x1;
-        m[3] += w * gv * x2;
-        m[4] += 0.5 * w * ((x0 * x0 + x1 * x1 + x2 * x2) * gv + hv);
+// Butterfly sum of N values over the warp; every lane gets the totals (fixed
+// order, so the result does not depend on the launch).
+template <int N>
+__device__ __forceinline__ void wsum(double* v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+}
+
+// Tensor-product position (ix, iy, iz) of velocity v, advanced by a lane stride.
+template <int D>
+struct DvIdx {
+    int ix, iy, iz;
+    __device__ __forceinline__ void init(int v, int M) {
+        ix = v % M;
+        const int r = v / M;
+        iy = D == 3 ? r % M : r;
+        iz = D == 3 ? r / M : 0;
     }
-    block_sum<5>(m, red);
-    __syncthreads();
-    const double rho = m[0];
-    const double U[3] = {m[1] / rho, m[2] / rho, m[3] / rho};
-    const double cv = (a.K + 3) / 2.0 * a.R;
-    const double uu = U[0] * U[0] + U[1] * U[1] + U[2] * U[2];
-    const double T = (m[4] - 0.5 * rho * uu) / (cv * rho);
-    const double tau = tau_ref(T, rho, muRef, a.omega, a.Tref, a.R);
-    // second pass: Q_i, S0, S_ik (about U); wall: Qw_i (about Uw), stress sums
-    double s2[1 + 3 + 6 + 3 + 9];
-    for (int i = 0; i < 22; ++i) s2[i] = 0.0;
-    for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
-        double x[3] = {a.xi[v], a.xi[Vp + v], a.xi[2 * Vp + v]};
-        double w = a.w[v], gv = g[v], hv = a.hasH ? h[v] : 0.0;
-        double c[3] = {x[0] - U[0], x[1] - U[1], x[2] - U[2]};
-        double cc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
-        double s = cc * gv + hv;
-        s2[0] += w * s;
-        for (int i = 0; i < 3; ++i) s2[1 + i] += 0.5 * w * c[i] * s;
-        s2[4] += w * c[0] * c[0] * gv; s2[5] += w * c[0] * c[1] * gv; s2[6] += w * c[0] * c[2] * gv;
-        s2[7] += w * c[1] * c[1] * gv; s2[8] += w * c[1] * c[2] * gv; s2[9] += w * c[2] * c[2] * gv;
+    __device__ __forceinline__ void advance(int s, int M) {
+        ix += s;
+        while (ix >= M) { ix -= M; ++iy; }
+        if (D == 3)
+            while (iy >= M) { iy -= M; ++iz; }
+    }
+};
+
+// exp(-(xi_d - U_d)^2 / (2 theta)) for the M abscissae of every direction of
+// the tensor-product grid, so that the Maxwellian factor of velocity
+// (ix, iy, iz) is N E[ix] E[M + iy] E[2M + iz]: D M exponentials per entity
+// instead of one per velocity.  E holds D*M doubles of this warp.
+template <int D>
+__device__ __forceinline__ void gauss_table(const StepArgs& a, int M, const double* U, double ith, double* E) {
+    const int lane = threadIdx.x & 31;
+    __syncwarp();  // the previous entity's reads of E are done
+    for (int i = lane; i < M; i += 32) {
+        const double c0 = a.xi[i] - U[0];                    // x of velocity (i, 0, 0)
+        E[i] = exp(-0.5 * (c0 * c0 * ith));
+        const double c1 = a.xi[a.Vp + i * M] - U[1];        // y of velocity (0, i, 0)
+        E[M + i] = exp(-0.5 * (c1 * c1 * ith));
+        if (D == 3) {
+            const double c2 = a.xi[2 * a.Vp + i * M * M] - U[2];  // z of velocity (0, 0, i)
+            E[2 * M + i] = exp(-0.5 * (c2 * c2 * ith));
+        }
+    }
+    __syncwarp();
+}
+
+// Transposed Jacobian of the Shakhov equilibrium (gE, hE)(rho, U, T, q)
+// applied to one velocity's adjoints (lg, lh).  With theta = R T, c = xi - U,
+// a = |c|^2/theta, G0 = (2 pi theta)^(-D/2) exp(-a/2), kap = (1-Pr)/(5 theta^2),
+// k3 = K+3-D, B = (a-D) k3 - 2K, P = a-D-2:
+//   gE = rho G0 + kap (c.q) P G0,   hE = theta [k3 rho G0 + kap (c.q) B G0]
+//   dgE/drho = G0,                          dhE/drho = theta k3 G0
+//   dgE/dU_k = gU c_k/theta - kap G0 q_k P,  gU = rho G0 + kap (c.q)(P-2) G0
+//   dhE/dU_k = hU c_k - theta kap G0 q_k B,  hU = k3 rho G0 + kap (c.q)(B-2 k3) G0
+//   dgE/dq_k = kap G0 c_k P,                dhE/dq_k = theta kap G0 c_k B
+//   dG0/dtheta = G0 (a-D) / (2 theta).
+// Accumulators (NJ = 2D+4): J[0] rho; J[1..D] sum c_k t1; J[D+1] sum t2 (the
+// U_k part -q_k t2 is applied once in finish); J[D+2..2D+1] q; J[2D+2] theta;
+// J[2D+3] sum (gE-g) lg + (hE-h) lh (the relaxation-rate part).
+template <int D>
+struct ShakhovJacT {
+    static constexpr int NJ = 2 * D + 4;
+    double rho, U[3], q[3], th, ith, N, kap, k3, K2;
+    __device__ __forceinline__ void prep(const double* m, double Rg, double Pr, int K) {
+        rho = m[0];
+        for (int k = 0; k < 3; ++k) { U[k] = m[1 + k]; q[k] = m[5 + k]; }
+        th = Rg * m[4];
+        ith = 1.0 / th;
+        const double s = sqrt(2.0 * kPi * th);
+        N = 1.0 / (D == 2 ? s * s : s * s * s);
+        kap = (1.0 - Pr) / 5.0 * ith * ith;
+        k3 = K + 3.0 - D;
+        K2 = 2.0 * K;
+    }
+    __device__ __forceinline__ void apply(const double* c, double cc, double G0, double g, double h, double lg,
+                                          double lh, double* J) const {
+        double cq = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) cq += c[k] * q[k];
+        const double a = cc * ith;
+        const double P = a - D - 2.0, B = (a - D) * k3 - K2;
+        const double rG = rho * G0, kG = kap * G0, kGcq = kG * cq;
+        const double gE = rG + kGcq * P;
+        const double H = k3 * rG + kGcq * B;
+        const double hE = th * H;
+        const double gU = rG + kGcq * (P - 2.0), hU = k3 * rG + kGcq * (B - 2.0 * k3);
+        const double t1 = gU * ith * lg + hU * lh;
+        const double t2 = kG * (P * lg + th * B * lh);
+        J[0] += G0 * (lg + th * k3 * lh);
+#pragma unroll
+        for (int k = 0; k < D; ++k) J[1 + k] += c[k] * t1;
+        J[D + 1] += t2;
+#pragma unroll
+        for (int k = 0; k < D; ++k) J[D + 2 + k] += c[k] * t2;
+        const double hd = 0.5 * (a - D) * ith;
+        const double dgth = rG * hd + kGcq * ith * (-2.0 * P - a + P * (a - D) * 0.5);
+        const double dHth = k3 * rG * hd + kGcq * ith * (-2.0 * B - k3 * a + B * (a - D) * 0.5);
+        J[2 * D + 2] += dgth * lg + (H + th * dHth) * lh;
+        J[2 * D + 3] += (gE - g) * lg + (hE - h) * lh;
+    }
+    // Adjoint of (rho, U, T, q, tau) from the summed accumulators; s scales the
+    // equilibrium part (the relaxation weight), ds the rate part (d weight/d tau).
+    __device__ __forceinline__ void finish(const double* J, double s, double ds, double Rg, double* lm) const {
+        lm[0] = s * J[0];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            lm[1 + k] = k < D ? s * (J[1 + k] - q[k] * J[D + 1]) : 0.0;
+            lm[5 + k] = k < D ? s * J[D + 2 + k] : 0.0;
+        }
+        lm[4] = s * (Rg * J[2 * D + 2]);
+        lm[8] = ds * J[2 * D + 3];
+    }
+};
+
+// Second moments of one entity about its velocity U (and, on walls, about the
+// wall velocity Uw) that the macro reverse needs:
+//   S0 = sum w (|c|^2 g + h),  Q_i = 1/2 sum w c_i (|c|^2 g + h),  S_ij = sum w c_i c_j g (i <= j)
+//   wall: Qw_i = 1/2 sum w e_i (|e|^2 g + h) (e = xi - Uw),  X_ij = sum w xi_i xi_j g.
+template <int D>
+struct Mom2 {
+    static constexpr int NS = D * (D + 1) / 2;
+    static constexpr int N = 1 + D + NS;
+    static constexpr int NWALL = D + D * D;
+    static __device__ __forceinline__ constexpr int sidx(int i, int j) {  // upper triangle, row-major
+        return i <= j ? i * D - i * (i - 1) / 2 + (j - i) : j * D - j * (j - 1) / 2 + (i - j);
+    }
+    static __device__ __forceinline__ void add(const double* c, double cc, double w, double g, double h, double* s) {
+        const double ws = w * (cc * g + h), wg = w * g;
+        s[0] += ws;
+#pragma unroll
+        for (int i = 0; i < D; ++i) s[1 + i] += 0.5 * ws * c[i];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = i; j < D; ++j) s[1 + D + sidx(i, j)] += wg * c[i] * c[j];
+    }
+    static __device__ __forceinline__ void add_wall(const double* x, const double* Uw, double w, double g, double h,
+                                                    double* s) {
+        double e[D], ee = 0.0;
+#pragma unroll
+        for (int i = 0; i < D; ++i) { e[i] = x[i] - Uw[i]; ee += e[i] * e[i]; }
+        const double sw = w * (ee * g + h), wg = w * g;
+#pragma unroll
+        for (int i = 0; i < D; ++i) s[i] += 0.5 * sw * e[i];
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+#pragma unroll
+            for (int j = 0; j < D; ++j) s[D + D * i + j] += wg * x[i] * x[j];
+    }
+};
+
+// Reverse of the macro evaluation of one entity (P9 for cells, P6 for faces;
+// fvDVM::updateMacroVol fvDVM.C:597-728, updateMacroSurf :456-582).  Inputs:
+// the forward macros (rho, U, T, tau) of the entity, lm = adjoint of
+// (rho, U, T, q, tau) with q = fac(tau) Q and fac = 2 tau / (2 tau + facA)
+// (cells facA = dt Pr, faces dt Pr / 2), the second moments s (Mom2 layout,
+// wall part after the first Mom2::N), and on walls the seeds lqw (adjoint of
+// qWall = fac Qw) and lsw (adjoint of stressWall = fs X, fs = 2 tau / (2 tau + dt/2)).
+// Output: per-velocity coefficients so that
+//   lg += w [lrho + lP.xi + lE/2 |xi|^2 + 1/2 (lQ.c)|c|^2 + 1/2 (lQw.e)|e|^2 + xi.lX.xi]
+//   lh += w [lE/2 + 1/2 lQ.c + 1/2 lQw.e],
+// and the mu_ref adjoint (tau = mu_ref (T/Tref)^omega / (rho R T)).
+template <int D>
+struct MacroAdj {
+    double lrho, lP[D], hE, hQ[D], hQw[D], lX[D * D], U[D], Uw[D];
+    bool wall;
+    __device__ __forceinline__ double chain(const StepArgs& a, double rho, const double* Um, double T, double tau,
+                                            const double* lm, const double* s, double facA, double muRef, bool isWall,
+                                            const double* Uwall, const double* lqw, const double* lsw) {
+        using M2 = Mom2<D>;
+        wall = isWall;
+        const double cv = (a.K + 3) / 2.0 * a.R;
+        double uu = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; ++k) { U[k] = Um[k]; uu += U[k] * U[k]; }
+        const double fac = 2.0 * tau / (2.0 * tau + facA);
+        const double dfac = 2.0 * facA / ((2.0 * tau + facA) * (2.0 * tau + facA));
+        double lU[D], lQ[D], lT = lm[4], ltau = lm[8];
+        lrho = lm[0];
+#pragma unroll
+        for (int i = 0; i < D; ++i) {
+            lU[i] = lm[1 + i];
+            lQ[i] = lm[5 + i] * fac;
+            ltau += lm[5 + i] * s[1 + i] * dfac;
+        }
         if (wall) {
-            double e[3] = {x[0] - Uw[0], x[1] - Uw[1], x[2] - Uw[2]};
-            double sw = (e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * gv + hv;
-            for (int i = 0; i < 3; ++i) s2[10 + i] += 0.5 * w * e[i] * sw;
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) s2[13 + 3 * i + j] += w * gv * x[i] * x[j];
-        }
-    }
-    block_sum<22>(s2, red);
-    const double S0 = s2[0], Q[3] = {s2[1], s2[2], s2[3]};
-    const double Sik[3][3] = {{s2[4], s2[5], s2[6]}, {s2[5], s2[7], s2[8]}, {s2[6], s2[8], s2[9]}};
-    // scalar chain
-    const double fac = 2.0 * tau / (2.0 * tau + facA);
-    const double dfac = 2.0 * facA / ((2.0 * tau + facA) * (2.0 * tau + facA));
-    double lrho = lm[0], lU[3] = {lm[1], lm[2], lm[3]}, lT = lm[4], ltau = lm[8];
-    double lQ[3];
-    for (int i = 0; i < 3; ++i) {
-        lQ[i] = lm[5 + i] * fac;
-        ltau += lm[5 + i] * Q[i] * dfac;
-    }
-    double lQw[3] = {0, 0, 0}, lS = 0.0;
-    if (wall) {
-        const double fs = 2.0 * tau / (2.0 * tau + 0.5 * a.dt);
-        const double dfs = 2.0 * (0.5 * a.dt) / ((2.0 * tau + 0.5 * a.dt) * (2.0 * tau + 0.5 * a.dt));
-        for (int i = 0; i < 3; ++i) {
-            lQw[i] = lqw[i] * fac;
-            ltau += lqw[i] * s2[10 + i] * dfac;
-        }
-        for (int k = 0; k < 9; ++k) ltau += lsw[k] * s2[13 + k] * dfs;
-        lS = fs;  // multiplies lsw in the per-DV pass
-    }
-    // tau = mu (T/Tref)^omega / (rho R T)
-    lT += ltau * tau * (a.omega - 1.0) / T;
-    lrho += -ltau * tau / rho;
-    lmu += ltau * tau / muRef;
-    // Q_i depends on U through c = xi - U
-    for (int k = 0; k < 3; ++k)
-        for (int i = 0; i < 3; ++i) lU[k] += lQ[i] * (-0.5 * ((i == k ? S0 : 0.0) + 2.0 * Sik[i][k]));
-    // T = (E - rho |U|^2 / 2) / (cv rho)
-    const double lE = lT / (cv * rho);
-    lrho += lT * (-0.5 * uu / (cv * rho) - T / rho);
-    for (int k = 0; k < 3; ++k) lU[k] += lT * (-U[k] / cv);
-    // U = P / rho
-    double lP[3];
-    for (int k = 0; k < 3; ++k) {
-        lP[k] = lU[k] / rho;
-        lrho += -lU[k] * U[k] / rho;
-    }
-    for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
-        double x[3] = {a.xi[v], a.xi[Vp + v], a.xi[2 * Vp + v]};
-        double w = a.w[v];
-        double c[3] = {x[0] - U[0], x[1] - U[1], x[2] - U[2]};
-        double cc = c[0] * c[0] + c[1] * c[1] + c[2] * c[2];
-        double xx = x[0] * x[0] + x[1] * x[1] + x[2] * x[2];
-        double dg = lrho + lP[0] * x[0] + lP[1] * x[1] + lP[2] * x[2] + 0.5 * lE * xx;
-        double dh = 0.5 * lE;
-        for (int i = 0; i < 3; ++i) {
-            dg += 0.5 * lQ[i] * c[i] * cc;
-            dh += 0.5 * lQ[i] * c[i];
-        }
-        if (wall) {
-            double e[3] = {x[0] - Uw[0], x[1] - Uw[1], x[2] - Uw[2]};
-            double ee = e[0] * e[0] + e[1] * e[1] + e[2] * e[2];
-            for (int i = 0; i < 3; ++i) {
-                dg += 0.5 * lQw[i] * e[i] * ee;
-                dh += 0.5 * lQw[i] * e[i];
+            const double fs = 2.0 * tau / (2.0 * tau + 0.5 * a.dt);
+            const double dfs = 2.0 * (0.5 * a.dt) / ((2.0 * tau + 0.5 * a.dt) * (2.0 * tau + 0.5 * a.dt));
+            const double* sw = s + M2::N;
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+                Uw[i] = Uwall[i];
+                hQw[i] = 0.5 * (lqw[i] * fac);
+                ltau += lqw[i] * sw[i] * dfac;
             }
-            for (int i = 0; i < 3; ++i)
-                for (int j = 0; j < 3; ++j) dg += lS * lsw[3 * i + j] * x[i] * x[j];
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+#pragma unroll
+                for (int j = 0; j < D; ++j) {
+                    ltau += lsw[3 * i + j] * sw[D + D * i + j] * dfs;
+                    lX[D * i + j] = fs * lsw[3 * i + j];
+                }
         }
-        lg[v] += w * dg;
-        if (a.hasH) lh[v] += w * dh;
+        lT += ltau * tau * (a.omega - 1.0) / T;
+        lrho += -ltau * tau / rho;
+        const double lmu = ltau * tau / muRef;
+        // Q_i depends on U through c = xi - U
+        const double S0 = s[0];
+#pragma unroll
+        for (int k = 0; k < D; ++k)
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+                lU[k] += lQ[i] * (-0.5 * ((i == k ? S0 : 0.0) + 2.0 * s[1 + D + M2::sidx(i, k)]));
+        // T = (E - rho |U|^2 / 2) / (cv rho)
+        const double lE = lT / (cv * rho);
+        lrho += lT * (-0.5 * uu / (cv * rho) - T / rho);
+#pragma unroll
+        for (int k = 0; k < D; ++k) lU[k] += lT * (-U[k] / cv);
+        // U = P / rho
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            lP[k] = lU[k] / rho;
+            lrho += -lU[k] * U[k] / rho;
+        }
+        hE = 0.5 * lE;
+#pragma unroll
+        for (int i = 0; i < D; ++i) hQ[i] = 0.5 * lQ[i];
+        return lmu;
+    }
+    __device__ __forceinline__ void dgh(const double* x, double& dg, double& dh) const {
+        double c[D], cc = 0.0, xx = 0.0, lc = 0.0;
+        dg = lrho;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+            c[k] = x[k] - U[k];
+            cc += c[k] * c[k];
+            xx += x[k] * x[k];
+            dg += lP[k] * x[k];
+            lc += hQ[k] * c[k];
+        }
+        dg += hE * xx + lc * cc;
+        dh = hE + lc;
+        if (wall) {
+            double e[D], ee = 0.0, le = 0.0;
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                e[k] = x[k] - Uw[k];
+                ee += e[k] * e[k];
+                le += hQw[k] * e[k];
+            }
+            dg += le * ee;
+            dh += le;
+#pragma unroll
+            for (int i = 0; i < D; ++i)
+#pragma unroll
+                for (int j = 0; j < D; ++j) dg += lX[D * i + j] * x[i] * x[j];
+        }
+    }
+};
+
+template <int D>
+__device__ __forceinline__ void load_xi(const StepArgs& a, int v, double* x) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) x[k] = a.xi[k * a.Vp + v];
+}
+
+// P9 reverse fused with the cell part of P8: one warp per cell.  lgN (adjoint
+// of state n+1) += J9^T lmN; then lgT(n) = -lgN/3 and lgB = 4/3 lgN.  mN holds
+// the macros of state n+1 as stored (rho [nC], U [nC][3], T [nC], q [nC][3], tau [nC]).
+template <int D, bool HH>
+__global__ void __launch_bounds__(kAW * 32) r_cell_mom(AArgs A, const double* gT, const double* hT, const double* mN,
+                                                       double* lgN, double* lhN, double* lgT, double* lhT,
+                                                       double* lgB, double* lhB, const double* lmN, double* lmuC) {
+    using M2 = Mom2<D>;
+    const StepArgs& a = A.a;
+    const int lane = threadIdx.x & 31, Vp = a.Vp, nC = a.nC;
+    for (int c = blockIdx.x * kAW + (threadIdx.x >> 5); c < nC; c += gridDim.x * kAW) {
+        const long long base = (long long)c * Vp;
+        const double rho = mN[c], T = mN[4 * nC + c], tau = mN[8 * nC + c];
+        double U[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) U[k] = mN[nC + 3 * c + k];
+        double s[M2::N];
+#pragma unroll
+        for (int i = 0; i < M2::N; ++i) s[i] = 0.0;
+        for (int v = lane; v < a.nV; v += 32) {
+            double x[D], cv[D], cc = 0.0;
+            load_xi<D>(a, v, x);
+#pragma unroll
+            for (int k = 0; k < D; ++k) { cv[k] = x[k] - U[k]; cc += cv[k] * cv[k]; }
+            M2::add(cv, cc, a.w[v], gT[base + v], HH ? hT[base + v] : 0.0, s);
+        }
+        wsum<M2::N>(s);
+        MacroAdj<D> o;
+        const double lmu = o.chain(a, rho, U, T, tau, lmN + (size_t)kM * c, s, a.dt * a.Pr, A.muRef, false, nullptr,
+                                   nullptr, nullptr);
+        for (int v = lane; v < Vp; v += 32) {  // padding: w = 0, the copies below still run
+            double x[D], dg, dh;
+            load_xi<D>(a, v, x);
+            o.dgh(x, dg, dh);
+            const double w = a.w[v];
+            const double lg = lgN[base + v] + w * dg;
+            lgN[base + v] = lg;
+            lgT[base + v] = -1.0 / 3 * lg;
+            lgB[base + v] = 4.0 / 3 * lg;
+            if (HH) {
+                const double lh = lhN[base + v] + w * dh;
+                lhN[base + v] = lh;
+                lhT[base + v] = -1.0 / 3 * lh;
+                lhB[base + v] = 4.0 / 3 * lh;
+            }
+        }
+        if (lane == 0) lmuC[c] += lmu;
     }
 }
 
-// P9 reverse: one block per cell.
-__global__ void r_cell_mom(AArgs A, const double* gT, const double* hT, double* lgT, double* lhT, const double* lm,
-                           double* lmuC) {
-    __shared__ double red[32 * 22];
-    const StepArgs& a = A.a;
-    const int c = blockIdx.x;
-    const long long base = (long long)c * a.Vp;
-    double lmu = 0.0;
-    macro_reverse(a, gT + base, a.hasH ? hT + base : nullptr, lgT + base, a.hasH ? lhT + base : nullptr,
-                  lm + (size_t)kM * c, a.dt * a.Pr, A.muRef, false, nullptr, nullptr, nullptr, red, lmu);
-    if (threadIdx.x == 0) lmuC[c] += lmu;
-}
-
-// P8 reverse, cell part: lgT(n) = -lgT(n+1)/3, lgB = 4/3 lgT(n+1).
+// P8 reverse, cell part alone (the last step, where the macros of n+1 carry no
+// adjoint): lgT(n) = -lgT(n+1)/3, lgB = 4/3 lgT(n+1).
 __global__ void r_cell_flux(AArgs A, const double* lgN, const double* lhN, double* lgT, double* lhT, double* lgB,
                             double* lhB) {
     const StepArgs& a = A.a;
@@ -664,76 +801,127 @@ __global__ void r_cell_flux(AArgs A, const double* lgN, const double* lhN, doubl
     }
 }
 
-// P8 reverse, face part: adjoint of the relaxed face values.
-__global__ void r_face_flux(AArgs A, const double* lgN, const double* lhN, double* lgS, double* lhS) {
+// P8 reverse, face part: adjoint of the relaxed face values; one warp per face.
+template <int D, bool HH>
+__global__ void __launch_bounds__(kAW * 32) r_face_flux(AArgs A, const double* lgN, const double* lhN, double* lgS,
+                                                        double* lhS) {
     const StepArgs& a = A.a;
-    const long long n = (long long)a.nA * a.Vp;
-    const int Vp = a.Vp;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        int f, v;
-        dvi(i, Vp, f, v);
-        if (v >= a.nV) { lgS[i] = 0.0; if (a.hasH) lhS[i] = 0.0; continue; }
+    const int lane = threadIdx.x & 31, Vp = a.Vp;
+    for (int f = blockIdx.x * kAW + (threadIdx.x >> 5); f < a.nA; f += gridDim.x * kAW) {
+        const long long base = (long long)f * Vp;
         const double* S = a.Sf + 3 * f;
-        double xs = a.xi[v] * S[0] + a.xi[Vp + v] * S[1] + a.xi[2 * Vp + v] * S[2];
         const int o = a.own[f];
-        double kg = -lgN[(long long)o * Vp + v] / a.vol[o];
-        double kh = a.hasH ? -lhN[(long long)o * Vp + v] / a.vol[o] : 0.0;
-        if (f < a.nI) {
-            const int nb = a.nei[f];
-            kg += lgN[(long long)nb * Vp + v] / a.vol[nb];
-            if (a.hasH) kh += lhN[(long long)nb * Vp + v] / a.vol[nb];
+        const bool inner = f < a.nI;
+        const int nb = inner ? a.nei[f] : o;
+        const double iVo = 1.0 / a.vol[o], iVn = inner ? 1.0 / a.vol[nb] : 0.0;
+        const double* lgo = lgN + (long long)o * Vp;
+        const double* lgn = lgN + (long long)nb * Vp;
+        for (int v = lane; v < Vp; v += 32) {
+            if (v >= a.nV) {
+                lgS[base + v] = 0.0;
+                if (HH) lhS[base + v] = 0.0;
+                continue;
+            }
+            double x[D], xs = 0.0;
+            load_xi<D>(a, v, x);
+#pragma unroll
+            for (int k = 0; k < D; ++k) xs += x[k] * S[k];
+            double kg = -lgo[v] * iVo;
+            if (inner) kg += lgn[v] * iVn;
+            lgS[base + v] = xs * a.dt * kg;
+            if (HH) {
+                double kh = -lhN[(long long)o * Vp + v] * iVo;
+                if (inner) kh += lhN[(long long)nb * Vp + v] * iVn;
+                lhS[base + v] = xs * a.dt * kh;
+            }
         }
-        lgS[i] = xs * a.dt * kg;
-        if (a.hasH) lhS[i] = xs * a.dt * kh;
     }
 }
 
-// P7 + P6 reverse (+ objective seeds on walls): one block per face.  In: lgS =
+// P7 + P6 reverse (+ objective seeds on walls): one warp per face.  In: lgS =
 // adjoint of the relaxed values; out: lgS = adjoint of the face values before
-// relaxation (incoming wall DVs keep theirs for r_wall).
-__global__ void r_face(AArgs A, const double* gS, const double* hS, const double* mF, double* lgS, double* lhS,
-                       const double* wq, const double* ws, double objScale, double* lmuF) {
-    __shared__ double red[32 * 22];
+// relaxation (incoming wall DVs keep theirs for r_wall).  mF: forward face
+// macros (rho, U, T, q, tau) of the step.  One pass over the velocities forms
+// the Shakhov Jacobian product and the second moments together; a second pass
+// writes the adjoints.
+template <int D, bool HH>
+__global__ void __launch_bounds__(kAW * 32) r_face(AArgs A, const double* gS, const double* hS, const double* mF,
+                                                   double* lgS, double* lhS, const double* wq, const double* ws,
+                                                   double objScale, double* lmuF) {
+    using SJ = ShakhovJacT<D>;
+    using M2 = Mom2<D>;
+    constexpr int NA = SJ::NJ + M2::N, NT = NA + M2::NWALL;
+    extern __shared__ double eTab[];
     const StepArgs& a = A.a;
-    const int f = blockIdx.x, Vp = a.Vp;
-    const long long base = (long long)f * Vp;
-    const bool wall = f >= a.nI;
-    const double* S = a.Sf + 3 * f;
-    const double* m = mF + (size_t)kM * f;  // rho, U, T, q, tau of the face
+    const int lane = threadIdx.x & 31, Vp = a.Vp, M = A.M;
+    double* E = eTab + (threadIdx.x >> 5) * D * M;
     const double hh = 0.5 * a.dt;
-    const double b = hh / (2.0 * m[8] + hh);
-    const double db = -2.0 * hh / ((2.0 * m[8] + hh) * (2.0 * m[8] + hh));
-    // P7: relaxed = (1-b) gS + b gE(mF) on relaxed DVs
-    double acc[kM];
-    for (int i = 0; i < kM; ++i) acc[i] = 0.0;
-    ShakhovJac J;
-    J.prep(m, a.R, a.Pr, a.D, a.K);
-    for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
-        double x0 = a.xi[v], x1 = a.xi[Vp + v], x2 = a.xi[2 * Vp + v];
-        if (wall && !(x0 * S[0] + x1 * S[1] + x2 * S[2] > 0)) continue;
-        double gE, hE, dg[8], dh[8];
-        J.eval(x0, x1, x2, gE, hE, dg, dh);
-        const double lg = lgS[base + v], lh = a.hasH ? lhS[base + v] : 0.0;
-        for (int k = 0; k < 8; ++k) acc[k] += b * (dg[k] * lg + (a.hasH ? dh[k] * lh : 0.0));
-        acc[8] += db * ((gE - gS[base + v]) * lg + (a.hasH ? (hE - hS[base + v]) * lh : 0.0));
-        lgS[base + v] = (1.0 - b) * lg;
-        if (a.hasH) lhS[base + v] = (1.0 - b) * lh;
+    for (int f = blockIdx.x * kAW + (threadIdx.x >> 5); f < a.nA; f += gridDim.x * kAW) {
+        const long long base = (long long)f * Vp;
+        const bool wall = f >= a.nI;
+        const double* S = a.Sf + 3 * f;
+        const double* m = mF + (size_t)kM * f;
+        const double* Uw = wall ? a.Uw + 3 * (f - a.nI) : nullptr;
+        SJ J;
+        J.prep(m, a.R, a.Pr, a.K);
+        const double b = hh / (2.0 * m[8] + hh);
+        const double db = -2.0 * hh / ((2.0 * m[8] + hh) * (2.0 * m[8] + hh));
+        gauss_table<D>(a, M, J.U, J.ith, E);
+        double acc[NT];
+#pragma unroll
+        for (int i = 0; i < NT; ++i) acc[i] = 0.0;
+        DvIdx<D> id;
+        id.init(lane, M);
+        for (int v = lane; v < a.nV; v += 32, id.advance(32, M)) {
+            double x[D], c[D], cc = 0.0, xs = 0.0;
+            load_xi<D>(a, v, x);
+#pragma unroll
+            for (int k = 0; k < D; ++k) {
+                c[k] = x[k] - J.U[k];
+                cc += c[k] * c[k];
+                xs += x[k] * S[k];
+            }
+            const double g = gS[base + v], h = HH ? hS[base + v] : 0.0;
+            if (!wall || xs > 0) {  // relaxed velocities (walls: outgoing only)
+                double G0 = J.N * E[id.ix] * E[M + id.iy];
+                if (D == 3) G0 *= E[2 * M + id.iz];
+                J.apply(c, cc, G0, g, h, lgS[base + v], HH ? lhS[base + v] : 0.0, acc);
+            }
+            M2::add(c, cc, a.w[v], g, h, acc + SJ::NJ);
+            if (wall) M2::add_wall(x, Uw, a.w[v], g, h, acc + NA);
+        }
+        if (wall) wsum<NT>(acc);
+        else wsum<NA>(acc);
+        double lm[kM];
+        J.finish(acc, b, db, a.R, lm);
+        double lqw[3] = {0.0, 0.0, 0.0}, lsw[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        if (wall) {
+            const int wf = f - a.nI;
+            for (int k = 0; k < 3; ++k) lqw[k] = objScale * wq[3 * wf + k];
+            lsw[1] = objScale * ws[wf];
+        }
+        MacroAdj<D> o;
+        const double lmu = o.chain(a, m[0], J.U, m[4], m[8], lm, acc + SJ::NJ, 0.5 * a.dt * a.Pr, A.muRef, wall, Uw,
+                                   lqw, lsw);
+        for (int v = lane; v < a.nV; v += 32) {
+            double x[D], dg, dh, xs = 0.0;
+            load_xi<D>(a, v, x);
+#pragma unroll
+            for (int k = 0; k < D; ++k) xs += x[k] * S[k];
+            o.dgh(x, dg, dh);
+            const double w = a.w[v];
+            const bool relaxed = !wall || xs > 0;
+            double lg = lgS[base + v];
+            if (relaxed) lg = (1.0 - b) * lg;
+            lgS[base + v] = lg + w * dg;
+            if (HH) {
+                double lh = lhS[base + v];
+                if (relaxed) lh = (1.0 - b) * lh;
+                lhS[base + v] = lh + w * dh;
+            }
+        }
+        if (lane == 0) lmuF[f] += lmu;
     }
-    block_sum<kM>(acc, red);
-    __syncthreads();
-    // P6: face macros (and wall outputs) from the face values
-    double lqw[3] = {0, 0, 0}, lsw[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const double* Uw = nullptr;
-    if (wall) {
-        const int wf = f - a.nI;
-        Uw = a.Uw + 3 * wf;
-        for (int k = 0; k < 3; ++k) lqw[k] = objScale * wq[3 * wf + k];
-        lsw[1] = objScale * ws[wf];
-    }
-    double lmu = 0.0;
-    macro_reverse(a, gS + base, a.hasH ? hS + base : nullptr, lgS + base, a.hasH ? lhS + base : nullptr, acc,
-                  0.5 * a.dt * a.Pr, A.muRef, wall, Uw, lqw, lsw, red, lmu);
-    if (threadIdx.x == 0) lmuF[f] += lmu;
 }
 
 // P5 + P4 reverse: one block per wall face.
@@ -775,130 +963,160 @@ __global__ void r_wall(AArgs A, const double* gS, const double* rhoW, const doub
     if (threadIdx.x == 0) lTw[wf] += acc[1] - lrw * rw / inc * acc[2];  // incoming sum is positive
 }
 
-// P3 reverse (+ the lagged wall gradient output G_b' = grad . n): per (cell, DV).
-__global__ void r_recon(AArgs A, const double* lgS, const double* lhS, const double* lGbN, const double* lGbNh,
-                        double* lgB, double* lhB, double* lG, double* lhG) {
+// P3 reverse (+ the lagged wall gradient output G_b' = grad . n): one warp per cell.
+template <int D, bool HH>
+__global__ void __launch_bounds__(kAW * 32) r_recon(AArgs A, const double* lgS, const double* lhS,
+                                                    const double* lGbN, const double* lGbNh, double* lgB, double* lhB,
+                                                    double* lG, double* lhG) {
     const StepArgs& a = A.a;
-    const long long n = (long long)a.nC * a.Vp;
-    const int D = a.D, Vp = a.Vp;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        int c, v;
-        dvi(i, Vp, c, v);
-        if (v >= a.nV) continue;
-        const double xi[3] = {a.xi[v], a.xi[Vp + v], a.xi[2 * Vp + v]};
-        double sb = 0.0, sbh = 0.0, gk[3] = {0, 0, 0}, hk[3] = {0, 0, 0};
-        for (int j = a.cellOff[c]; j < a.cellOff[c + 1]; ++j) {
-            const int e = a.cellFace[j], f = e >> 1, side = e & 1;
-            const double* S = a.Sf + 3 * f;
-            const double xs = xi[0] * S[0] + xi[1] * S[1] + xi[2] * S[2];
-            double wgt;
-            if (f < a.nI) {
-                const bool up = side == 0 ? xs >= kVSmall : xs < -kVSmall;
-                const bool tie = !(xs >= kVSmall) && !(xs < -kVSmall);
-                wgt = up ? 1.0 : (tie ? 0.5 : 0.0);
-            } else {
-                wgt = xs > 0 ? 1.0 : 0.0;
+    const int lane = threadIdx.x & 31, Vp = a.Vp;
+    for (int c = blockIdx.x * kAW + (threadIdx.x >> 5); c < a.nC; c += gridDim.x * kAW) {
+        const int j0 = a.cellOff[c], j1 = a.cellOff[c + 1];
+        const long long base = (long long)c * Vp;
+        for (int v = lane; v < a.nV; v += 32) {
+            double xi[D];
+            load_xi<D>(a, v, xi);
+            double sb = 0.0, sbh = 0.0, gk[D], hk[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) gk[k] = hk[k] = 0.0;
+            for (int j = j0; j < j1; ++j) {
+                const int e = a.cellFace[j], f = e >> 1, side = e & 1;
+                const double* S = a.Sf + 3 * f;
+                double xs = 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) xs += xi[k] * S[k];
+                double wgt;
+                if (f < a.nI) {
+                    const bool up = side == 0 ? xs >= kVSmall : xs < -kVSmall;
+                    const bool tie = !(xs >= kVSmall) && !(xs < -kVSmall);
+                    wgt = up ? 1.0 : (tie ? 0.5 : 0.0);
+                } else {
+                    wgt = xs > 0 ? 1.0 : 0.0;
+                }
+                if (wgt == 0.0) continue;
+                const double* d = side == 0 ? a.dO + 3 * f : a.dN + 3 * f;
+                const long long fi = (long long)f * Vp + v;
+                const double lg = wgt * lgS[fi], lh = HH ? wgt * lhS[fi] : 0.0;
+                sb += lg;
+                sbh += lh;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    const double dk = d[k] - 0.5 * xi[k] * a.dt;
+                    gk[k] += lg * dk;
+                    hk[k] += lh * dk;
+                }
             }
-            if (wgt == 0.0) continue;
-            const double* d = side == 0 ? a.dO + 3 * f : a.dN + 3 * f;
-            const long long fi = (long long)f * Vp + v;
-            const double lg = wgt * lgS[fi], lh = a.hasH ? wgt * lhS[fi] : 0.0;
-            sb += lg;
-            sbh += lh;
+            // G_b' = grad . n on the wall faces of this cell
+            for (int j = j0; j < j1; ++j) {
+                const int f = a.cellFace[j] >> 1;
+                if (f < a.nI) continue;
+                const int wf = f - a.nI;
+                const double* nh = a.nHatW + 3 * wf;
+                const double lb = lGbN[(long long)wf * Vp + v], lbh = HH ? lGbNh[(long long)wf * Vp + v] : 0.0;
+#pragma unroll
+                for (int k = 0; k < D; ++k) {
+                    gk[k] += lb * nh[k];
+                    hk[k] += lbh * nh[k];
+                }
+            }
+            lgB[base + v] += sb;
+            if (HH) lhB[base + v] += sbh;
+#pragma unroll
             for (int k = 0; k < D; ++k) {
-                const double dk = d[k] - 0.5 * xi[k] * a.dt;
-                gk[k] += lg * dk;
-                hk[k] += lh * dk;
+                lG[((long long)c * D + k) * Vp + v] = gk[k];
+                if (HH) lhG[((long long)c * D + k) * Vp + v] = hk[k];
             }
-        }
-        // G_b' = grad . n on the wall faces of this cell
-        for (int j = a.cellOff[c]; j < a.cellOff[c + 1]; ++j) {
-            const int f = a.cellFace[j] >> 1;
-            if (f < a.nI) continue;
-            const int wf = f - a.nI;
-            const double* nh = a.nHatW + 3 * wf;
-            const double lb = lGbN[(long long)wf * Vp + v], lbh = a.hasH ? lGbNh[(long long)wf * Vp + v] : 0.0;
-            for (int k = 0; k < D; ++k) {
-                gk[k] += lb * nh[k];
-                hk[k] += lbh * nh[k];
-            }
-        }
-        lgB[i] += sb;
-        if (a.hasH) lhB[i] += sbh;
-        for (int k = 0; k < D; ++k) {
-            lG[((long long)c * D + k) * Vp + v] = gk[k];
-            if (a.hasH) lhG[((long long)c * D + k) * Vp + v] = hk[k];
         }
     }
 }
 
 // P2 reverse: lgB += transpose of the least-squares stencil; adjoint of the
-// lagged wall gradient input.
-__global__ void r_grad(AArgs A, const double* lG, const double* lhG, double* lgB, double* lhB, double* lGb,
-                       double* lGbh) {
+// lagged wall gradient input.  One warp per cell.
+template <int D, bool HH>
+__global__ void __launch_bounds__(kAW * 32) r_grad(AArgs A, const double* lG, const double* lhG, double* lgB,
+                                                   double* lhB, double* lGb, double* lGbh) {
     const StepArgs& a = A.a;
-    const long long n = (long long)a.nC * a.Vp;
-    const int D = a.D, Vp = a.Vp;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        int c, v;
-        dvi(i, Vp, c, v);
-        if (v >= a.nV) continue;
-        double sg = 0.0, sh = 0.0;
-        for (int j = a.cellOff[c]; j < a.cellOff[c + 1]; ++j) {
-            const int e = a.cellFace[j], f = e >> 1, side = e & 1;
-            if (f < a.nI) {
-                const int other = side == 0 ? a.nei[f] : a.own[f];
-                const double* Lc = side == 0 ? a.pVec + 3 * f : a.nVec + 3 * f;  // this cell's vector
-                const double* Lo = side == 0 ? a.nVec + 3 * f : a.pVec + 3 * f;  // the other cell's vector
-                for (int k = 0; k < D; ++k) {
-                    sg += Lo[k] * lG[((long long)other * D + k) * Vp + v] - Lc[k] * lG[((long long)c * D + k) * Vp + v];
-                    if (a.hasH)
-                        sh += Lo[k] * lhG[((long long)other * D + k) * Vp + v] - Lc[k] * lhG[((long long)c * D + k) * Vp + v];
+    const int lane = threadIdx.x & 31, Vp = a.Vp;
+    for (int c = blockIdx.x * kAW + (threadIdx.x >> 5); c < a.nC; c += gridDim.x * kAW) {
+        const int j0 = a.cellOff[c], j1 = a.cellOff[c + 1];
+        const long long base = (long long)c * Vp;
+        for (int v = lane; v < a.nV; v += 32) {
+            double sg = 0.0, sh = 0.0;
+            for (int j = j0; j < j1; ++j) {
+                const int e = a.cellFace[j], f = e >> 1, side = e & 1;
+                if (f < a.nI) {
+                    const int other = side == 0 ? a.nei[f] : a.own[f];
+                    const double* Lc = side == 0 ? a.pVec + 3 * f : a.nVec + 3 * f;  // this cell's vector
+                    const double* Lo = side == 0 ? a.nVec + 3 * f : a.pVec + 3 * f;  // the other cell's vector
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        sg += Lo[k] * lG[((long long)other * D + k) * Vp + v] - Lc[k] * lG[((long long)c * D + k) * Vp + v];
+                        if (HH)
+                            sh += Lo[k] * lhG[((long long)other * D + k) * Vp + v] -
+                                  Lc[k] * lhG[((long long)c * D + k) * Vp + v];
+                    }
+                } else {
+                    const int wf = f - a.nI;
+                    const double* L = a.bVec + 3 * wf;
+                    double lb = 0.0, lbh = 0.0;
+#pragma unroll
+                    for (int k = 0; k < D; ++k) {
+                        lb += L[k] * lG[((long long)c * D + k) * Vp + v];
+                        if (HH) lbh += L[k] * lhG[((long long)c * D + k) * Vp + v];
+                    }
+                    lGb[(long long)wf * Vp + v] = lb / a.dcW[wf];
+                    if (HH) lGbh[(long long)wf * Vp + v] = lbh / a.dcW[wf];
                 }
-            } else {
-                const int wf = f - a.nI;
-                const double* L = a.bVec + 3 * wf;
-                double lb = 0.0, lbh = 0.0;
-                for (int k = 0; k < D; ++k) {
-                    lb += L[k] * lG[((long long)c * D + k) * Vp + v];
-                    if (a.hasH) lbh += L[k] * lhG[((long long)c * D + k) * Vp + v];
-                }
-                lGb[(long long)wf * Vp + v] = lb / a.dcW[wf];
-                if (a.hasH) lGbh[(long long)wf * Vp + v] = lbh / a.dcW[wf];
             }
+            lgB[base + v] += sg;
+            if (HH) lhB[base + v] += sh;
         }
-        lgB[i] += sg;
-        if (a.hasH) lhB[i] += sh;
     }
 }
 
-// P1 reverse: one block per cell.  lgT += (1-r) lgB; lm = macro adjoint of the
+// P1 reverse: one warp per cell.  lgT += (1-r) lgB; lm = macro adjoint of the
 // cell's relaxation (rho, U, T, q, tau).
-__global__ void r_barp(AArgs A, const double* gT, const double* hT, const double* mC, const double* lgB,
-                       const double* lhB, double* lgT, double* lhT, double* lm) {
-    __shared__ double red[32 * kM];
+template <int D, bool HH>
+__global__ void __launch_bounds__(kAW * 32) r_barp(AArgs A, const double* gT, const double* hT, const double* mC,
+                                                   const double* lgB, const double* lhB, double* lgT, double* lhT,
+                                                   double* lm) {
+    using SJ = ShakhovJacT<D>;
+    extern __shared__ double eTab[];
     const StepArgs& a = A.a;
-    const int c = blockIdx.x, Vp = a.Vp;
-    const long long base = (long long)c * Vp;
-    const double* m = mC + (size_t)kM * c;
-    const double r = 1.5 * a.dt / (2.0 * m[8] + a.dt);
-    const double dr = -3.0 * a.dt / ((2.0 * m[8] + a.dt) * (2.0 * m[8] + a.dt));
-    double acc[kM];
-    for (int i = 0; i < kM; ++i) acc[i] = 0.0;
-    ShakhovJac J;
-    J.prep(m, a.R, a.Pr, a.D, a.K);
-    for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
-        double gE, hE, dg[8], dh[8];
-        J.eval(a.xi[v], a.xi[Vp + v], a.xi[2 * Vp + v], gE, hE, dg, dh);
-        const double lg = lgB[base + v], lh = a.hasH ? lhB[base + v] : 0.0;
-        for (int k = 0; k < 8; ++k) acc[k] += r * (dg[k] * lg + (a.hasH ? dh[k] * lh : 0.0));
-        acc[8] += dr * ((gE - gT[base + v]) * lg + (a.hasH ? (hE - hT[base + v]) * lh : 0.0));
-        lgT[base + v] += (1.0 - r) * lg;
-        if (a.hasH) lhT[base + v] += (1.0 - r) * lh;
+    const int lane = threadIdx.x & 31, Vp = a.Vp, M = A.M;
+    double* E = eTab + (threadIdx.x >> 5) * D * M;
+    for (int c = blockIdx.x * kAW + (threadIdx.x >> 5); c < a.nC; c += gridDim.x * kAW) {
+        const long long base = (long long)c * Vp;
+        const double* m = mC + (size_t)kM * c;
+        const double r = 1.5 * a.dt / (2.0 * m[8] + a.dt);
+        const double dr = -3.0 * a.dt / ((2.0 * m[8] + a.dt) * (2.0 * m[8] + a.dt));
+        SJ J;
+        J.prep(m, a.R, a.Pr, a.K);
+        gauss_table<D>(a, M, J.U, J.ith, E);
+        double acc[SJ::NJ];
+#pragma unroll
+        for (int i = 0; i < SJ::NJ; ++i) acc[i] = 0.0;
+        DvIdx<D> id;
+        id.init(lane, M);
+        for (int v = lane; v < a.nV; v += 32, id.advance(32, M)) {
+            double x[D], cv[D], cc = 0.0;
+            load_xi<D>(a, v, x);
+#pragma unroll
+            for (int k = 0; k < D; ++k) { cv[k] = x[k] - J.U[k]; cc += cv[k] * cv[k]; }
+            double G0 = J.N * E[id.ix] * E[M + id.iy];
+            if (D == 3) G0 *= E[2 * M + id.iz];
+            const double lg = lgB[base + v], lh = HH ? lhB[base + v] : 0.0;
+            J.apply(cv, cc, G0, gT[base + v], HH ? hT[base + v] : 0.0, lg, lh, acc);
+            lgT[base + v] += (1.0 - r) * lg;
+            if (HH) lhT[base + v] += (1.0 - r) * lh;
+        }
+        wsum<SJ::NJ>(acc);
+        double out[kM];
+        J.finish(acc, r, dr, a.R, out);
+        if (lane == 0)
+#pragma unroll
+            for (int k = 0; k < kM; ++k) lm[(size_t)kM * c + k] = out[k];
     }
-    block_sum<kM>(acc, red);
-    if (threadIdx.x == 0)
-        for (int k = 0; k < kM; ++k) lm[(size_t)kM * c + k] = acc[k];
 }
 
 // Pack cell / face macros of the forward pass as (rho, U, T, q, tau) tuples.
@@ -963,27 +1181,51 @@ void adj_pack_macros(int n, const double* rho, const double* U, const double* T,
     k_pack_macros<<<grid(n, kT, sms), kT, 0, st>>>(n, rho, U, T, q, tau, out);
 }
 
-void adj_launch_step(const AdjState& s, const double* gTn, const double* hTn, bool objective, const double* wq,
-                     const double* ws, double scale, int sms, cudaStream_t st) {
-    AArgs A{s.a, s.a.Tw, s.muRef};
+namespace {
+int wgrid(int n, int sms) {  // blocks of kAW warps, one warp per entity, grid-stride
+    const long long b = ((long long)n + kAW - 1) / kAW, cap = (long long)sms * 16;
+    return (int)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+template <int D, bool HH>
+void adj_step(const AdjState& s, const double* gTn, const double* hTn, const double* mTn, bool objective,
+              double scale, int sms, cudaStream_t st) {
+    const AArgs A{s.a, s.a.Tw, s.muRef, s.M};
     const StepArgs& a = s.a;
-    const long long nCV = (long long)a.nC * a.Vp, nAV = (long long)a.nA * a.Vp;
-    // P9 reverse: lgN += J9^T lmN (state n+1 and the adjoint of its macros)
-    if (s.haveMacroAdj) r_cell_mom<<<a.nC, kRT, 0, st>>>(A, gTn, hTn, s.lgN, s.lhN, s.lmN, s.lmuC);
-    // P8 reverse
-    r_cell_flux<<<grid(nCV, kT, sms), kT, 0, st>>>(A, s.lgN, s.lhN, s.lgT, s.lhT, s.lgB, s.lhB);
-    r_face_flux<<<grid(nAV, kT, sms), kT, 0, st>>>(A, s.lgN, s.lhN, s.lgS, s.lhS);
+    const size_t eTab = (size_t)kAW * D * s.M * sizeof(double);
+    const int gC = wgrid(a.nC, sms), gF = wgrid(a.nA, sms), thr = kAW * 32;
+    // P9 reverse fused with the cell part of P8 (lgN += J9^T lmN; lgT, lgB from lgN)
+    if (s.haveMacroAdj)
+        r_cell_mom<D, HH><<<gC, thr, 0, st>>>(A, gTn, hTn, mTn, s.lgN, s.lhN, s.lgT, s.lhT, s.lgB, s.lhB, s.lmN,
+                                             s.lmuC);
+    else
+        r_cell_flux<<<grid((long long)a.nC * a.Vp, kT, sms), kT, 0, st>>>(A, s.lgN, s.lhN, s.lgT, s.lhT, s.lgB,
+                                                                           s.lhB);
+    // P8 reverse, face part
+    r_face_flux<D, HH><<<gF, thr, 0, st>>>(A, s.lgN, s.lhN, s.lgS, s.lhS);
     // P7 + P6 reverse
-    r_face<<<a.nA, kRT, 0, st>>>(A, s.gS, s.hS, s.mF, s.lgS, s.lhS, s.wq, s.ws, objective ? scale : 0.0, s.lmuF);
+    r_face<D, HH><<<gF, thr, eTab, st>>>(A, s.gS, s.hS, s.mF, s.lgS, s.lhS, s.wq, s.ws, objective ? scale : 0.0,
+                                         s.lmuF);
     // P5 + P4 reverse
     if (a.nW > 0) r_wall<<<a.nW, kRT, 0, st>>>(A, s.gS, a.rhoW, a.incAbs, s.lgS, s.lhS, s.lTw);
     // P3 reverse (+ G_b' = grad.n), P2 reverse
-    r_recon<<<grid(nCV, kT, sms), kT, 0, st>>>(A, s.lgS, s.lhS, s.lGbN, s.lGbNh, s.lgB, s.lhB, s.lG, s.lhG);
-    r_grad<<<grid(nCV, kT, sms), kT, 0, st>>>(A, s.lG, s.lhG, s.lgB, s.lhB, s.lGb, s.lGbh);
+    r_recon<D, HH><<<gC, thr, 0, st>>>(A, s.lgS, s.lhS, s.lGbN, s.lGbNh, s.lgB, s.lhB, s.lG, s.lhG);
+    r_grad<D, HH><<<gC, thr, 0, st>>>(A, s.lG, s.lhG, s.lgB, s.lhB, s.lGb, s.lGbh);
     // P1 reverse
-    r_barp<<<a.nC, kRT, 0, st>>>(A, s.gT, s.hT, s.mC, s.lgB, s.lhB, s.lgT, s.lhT, s.lm);
-    (void)wq;
-    (void)ws;
+    r_barp<D, HH><<<gC, thr, eTab, st>>>(A, s.gT, s.hT, s.mC, s.lgB, s.lhB, s.lgT, s.lhT, s.lm);
+}
+}  // namespace
+
+size_t adj_table_bytes(int D, int M) { return (size_t)kAW * D * M * sizeof(double); }
+
+void adj_launch_step(const AdjState& s, const double* gTn, const double* hTn, const double* mTn, bool objective,
+                     double scale, int sms, cudaStream_t st) {
+    if (s.a.D == 3) {
+        if (s.a.hasH) adj_step<3, true>(s, gTn, hTn, mTn, objective, scale, sms, st);
+        else adj_step<3, false>(s, gTn, hTn, mTn, objective, scale, sms, st);
+    } else {
+        adj_step<2, true>(s, gTn, hTn, mTn, objective, scale, sms, st);
+    }
 }
 
 void adj_sum(int n, const double* x, double* out, cudaStream_t st) { k_sum<<<1, kT, 0, st>>>(n, x, out); }

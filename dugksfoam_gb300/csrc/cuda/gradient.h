@@ -38,6 +38,7 @@ struct AdjState {
     const double* lmN;          // in: adjoint of the cell macros at n+1 ([nC][9])
     double* lm;                 // out: adjoint of the cell macros at n
     bool haveMacroAdj;          // lmN is nonzero
+    int M;                      // velocities per direction of the tensor-product grid
     double *lmuC, *lmuF, *lTw;  // accumulated parameter adjoints
 };
 
@@ -50,8 +51,13 @@ void tlm_launch_step(const TlmState& s, bool objective, const double* wq, const 
 void launch_objective(const StepArgs& a, const double* wq, const double* ws, double scale, double* J, cudaStream_t st);
 void adj_pack_macros(int n, const double* rho, const double* U, const double* T, const double* q, const double* tau,
                      double* out, int sms, cudaStream_t st);
-void adj_launch_step(const AdjState& s, const double* gTn, const double* hTn, bool objective, const double* wq,
-                     const double* ws, double scale, int sms, cudaStream_t st);
+// One reverse step.  gTn, hTn: state n+1; mTn: its cell macros as stored
+// (rho [nC], U [nC][3], T [nC], q [nC][3], tau [nC]).  2D cases carry h
+// (K + 3 - D > 0); 3D cases with or without it.
+void adj_launch_step(const AdjState& s, const double* gTn, const double* hTn, const double* mTn, bool objective,
+                     double scale, int sms, cudaStream_t st);
+// Shared memory of the per-warp Gaussian tables (must stay within 48 KB).
+size_t adj_table_bytes(int D, int M);
 void adj_sum(int n, const double* x, double* out, cudaStream_t st);
 
 }  // namespace dugks

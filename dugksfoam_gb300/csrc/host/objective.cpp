@@ -219,6 +219,12 @@ int objective_adjoint(Solver& s, const Objective& o, double& J, double* dJdTw, d
         cudaMemcpyAsync(a.q, m + 5 * nC, 3 * nC * 8, cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(a.tau, m + 8 * nC, nC * 8, cudaMemcpyDeviceToDevice, st);
     };
+    // the reverse kernels tabulate the Maxwellian per direction of the tensor-product grid
+    int M = 1;
+    while ((D == 3 ? (size_t)M * M * M : (size_t)M * M) < (size_t)a.nV) ++M;
+    if ((D != 2 && D != 3) || (D == 3 ? M * M * M : M * M) != a.nV || adj_table_bytes(a.D, M) > 48 * 1024)
+        return s.fail(DUGKS_ERR_UNSUPPORTED, "adjoint: needs a 2D or 3D tensor-product velocity grid of at most 512 "
+                                             "points per direction");
     const int K = o.ckptEvery, N = o.nSteps, nSeg = (N + K - 1) / K;
     double* ckpt = W.alloc<double>(stateN * (size_t)nSeg);
     double* seg = W.alloc<double>(stateN * (size_t)(K + 1));
@@ -262,6 +268,7 @@ int objective_adjoint(Solver& s, const Objective& o, double& J, double* dJdTw, d
     cudaMemcpyAsync(&J, dJ, 8, cudaMemcpyDeviceToHost, st);
     // 2. reverse, segment by segment
     A.muRef = a.muRef;
+    A.M = M;
     A.wq = wq;
     A.ws = ws;
     double* lmN = lmA;  // adjoint of the macros at n+1
@@ -307,7 +314,8 @@ int objective_adjoint(Solver& s, const Objective& o, double& J, double* dJdTw, d
             A.mC = mC;
             A.lmN = lmN; A.lm = lm;
             A.haveMacroAdj = n < N - 1;
-            adj_launch_step(A, stN1 + oG, a.hasH ? stN1 + oH : nullptr, in_window(o, n), wq, ws, window_scale(o), sms, st);
+            adj_launch_step(A, stN1 + oG, a.hasH ? stN1 + oH : nullptr, stN1 + oM, in_window(o, n), window_scale(o), sms,
+                            st);
             std::swap(A.lgN, A.lgT);
             std::swap(A.lhN, A.lhT);
             std::swap(A.lGbN, A.lGb);
