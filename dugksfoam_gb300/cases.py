@@ -60,12 +60,14 @@ def _sort_internal(owner, neigh, faces):
 
 
 def structured_mesh(nx: int, ny: int, nz: int = 1, lx=1.0, ly=1.0, lz=None, two_d=True,
-                    bottom_patch=False):
+                    bottom_patch=False, patch_defs=None):
     """Uniform hex mesh of [0,lx]x[0,ly]x[0,lz] in OpenFOAM order.
 
     2D (two_d=True): nz must be 1 and front/back form an ``empty`` patch.
     Patches: movingWall (y = ly), fixedWalls (the other walls; bottomWall
-    separately when ``bottom_patch``), frontAndBack (2D only).
+    separately when ``bottom_patch``), frontAndBack (2D only).  ``patch_defs``
+    replaces them: a list of (name, mesh type, sides, rho boundary type or
+    None) with sides among x0 x1 y0 y1 z0 z1 (2D adds frontAndBack itself).
     """
     if two_d:
         assert nz == 1
@@ -125,20 +127,25 @@ def structured_mesh(nx: int, ny: int, nz: int = 1, lx=1.0, ly=1.0, lz=None, two_
         o = np.argsort(c, kind="stable")
         return c[o], f[o]
 
-    patch_defs = [("movingWall", "wall", ["y1"])]
-    if bottom_patch:
-        patch_defs.append(("fixedWalls", "wall", ["x0", "x1"] + ([] if two_d else ["z0", "z1"])))
-        patch_defs.append(("bottomWall", "wall", ["y0"]))
+    if patch_defs is None:
+        patch_defs = [("movingWall", "wall", ["y1"], None)]
+        if bottom_patch:
+            patch_defs.append(("fixedWalls", "wall", ["x0", "x1"] + ([] if two_d else ["z0", "z1"]), None))
+            patch_defs.append(("bottomWall", "wall", ["y0"], None))
+        else:
+            patch_defs.append(("fixedWalls", "wall", ["x0", "x1", "y0"] + ([] if two_d else ["z0", "z1"]), None))
     else:
-        patch_defs.append(("fixedWalls", "wall", ["x0", "x1", "y0"] + ([] if two_d else ["z0", "z1"])))
+        patch_defs = list(patch_defs)
     if two_d:
-        patch_defs.append(("frontAndBack", "empty", ["z0", "z1"]))
+        patch_defs.append(("frontAndBack", "empty", ["z0", "z1"], None))
     b_own, b_faces, patches = [], [], []
     start = len(owner)
-    for name, ptype, sides in patch_defs:
+    for name, ptype, sides, bc in patch_defs:
         c, f = group(sides)
         b_own.append(c); b_faces.append(f)
         patches.append(dict(name=name, type=ptype, startFace=start, nFaces=len(c)))
+        if bc is not None:
+            patches[-1]["bc"] = bc
         start += len(c)
     all_faces = np.concatenate([faces] + b_faces).astype(np.int32)
     mesh = dict(
@@ -276,11 +283,13 @@ def mesh_info(mesh):
 
 # ------------------------------------------------------------------ cases
 def make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=50.0, T0=273.0, Tw=None,
-              grid="nc", C_gh=None, lid_patch="movingWall"):
+              grid="nc", C_gh=None, lid_patch="movingWall", bvals=None):
     """Assemble a case dict: mesh + gas + DV grid + initial rest equilibrium.
 
     Wall velocity: ``lid_u`` in +x on ``lid_patch``, zero elsewhere.  Wall
     temperature: ``Tw`` (scalar, or dict patch-name -> scalar/array), else T0.
+    ``bvals``: patch name -> dict(rho=, U=, T=, pressure=) patch values of the
+    other boundary types (fixedValue, farField, pressureIn/Out).
     """
     nC = mesh["n_cells"]
     nF = len(mesh["face_offsets"]) - 1
@@ -288,8 +297,17 @@ def make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=50.0, T0=273.0, Tw
     nB = nF - nI
     Ub = np.zeros((nB, 3))
     Tb = np.full(nB, float(T0))
+    rhob = np.zeros(nB)
     for p in mesh["patches"]:
         s, e = p["startFace"] - nI, p["startFace"] - nI + p["nFaces"]
+        bv = (bvals or {}).get(p["name"])
+        if bv is not None:
+            rhob[s:e] = bv.get("rho", rho0)
+            Ub[s:e] = bv.get("U", (0.0, 0.0, 0.0))
+            Tb[s:e] = bv.get("T", T0)
+            if "pressure" in bv:
+                p["pressure"] = float(bv["pressure"])
+            continue
         if p["type"] != "wall":
             Tb[s:e] = 0.0
             continue
@@ -313,6 +331,7 @@ def make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=50.0, T0=273.0, Tw
         T0=np.full(nC, float(T0)),
         Ub=Ub,
         Tb=Tb,
+        rhob=rhob,
         two_d=two_d,
     )
 
@@ -384,6 +403,51 @@ def cavity3d(n=48, Kn=0.1, nxi=20):
     xi_max = 4.0 * math.sqrt(2 * gas["R"] * 273.0)
     mesh = structured_mesh(n, n, n, lz=1.0, two_d=False)
     return make_case(mesh, gas, rho0, nxi, xi_max, two_d=False)
+
+
+def channel2d(nx=40, ny=20, Kn=0.1, nxi=16, p_ratio=1.2):
+    """2D channel [0,2]x[0,1] in reduced units (R = 1/2, T0 = 1, rho0 = 1, so
+    2 R T0 = 1): pressureIn (x = 0) at p_ratio p0, pressureOut (x = 2) at
+    p0 = rho0 R T0, diffuse walls top and bottom.  Reduced units because the
+    pressure patches start at rho_b = 1 (their constructor's value) until the
+    first update (pressureInFvPatchField.C:62-76)."""
+    gas, _ = gas_from_kn(Kn, R=0.5, T0=1.0)
+    rho0 = 1.0
+    gas["muRef"] = gas["muRef"] / _ * rho0  # mu = rho0 C L mu_bar with this rho0
+    xi_max = 4.0 * math.sqrt(2 * gas["R"] * 1.0)
+    p0 = rho0 * gas["R"] * 1.0
+    mesh = structured_mesh(nx, ny, 1, lx=2.0, ly=1.0, lz=1.0 / ny, two_d=True, patch_defs=[
+        ("inlet", "patch", ["x0"], "pressureIn"), ("outlet", "patch", ["x1"], "pressureOut"),
+        ("walls", "wall", ["y0", "y1"], None)])
+    return make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=0.0, T0=1.0, bvals={
+        "inlet": dict(T=1.0, pressure=p_ratio * p0), "outlet": dict(T=1.0, pressure=p0)})
+
+
+def open_box2d(n=24, Kn=0.1, nxi=16, u_in=60.0):
+    """2D box with one patch of each open type: farField at x = 0 (rho0, 300 K),
+    zeroGradient at x = 1, fixedValue (mixed) at y = 1 moving at u_in, a
+    diffuse wall at y = 0."""
+    gas, rho0 = gas_from_kn(Kn)
+    xi_max = 4.0 * math.sqrt(2 * gas["R"] * 273.0)
+    mesh = structured_mesh(n, n, 1, two_d=True, patch_defs=[
+        ("farfield", "patch", ["x0"], "farField"), ("outflow", "patch", ["x1"], "zeroGradient"),
+        ("top", "patch", ["y1"], "fixedValue"), ("bottom", "wall", ["y0"], None)])
+    return make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=0.0, bvals={
+        "farfield": dict(rho=rho0, T=300.0), "top": dict(rho=1.1 * rho0, U=(u_in, 0.0, 0.0), T=290.0),
+        "outflow": dict(T=273.0)})
+
+
+def half_cavity2d(nx=15, ny=30, Kn=0.075, nxi=16, sym="symmetryPlane"):
+    """Left half [0,0.5]x[0,1] of the lid-driven cavity with a symmetry patch at
+    x = 0.5 (the layout of the reference demo testSymmetry/symmetry):
+    ``sym`` = "symmetryPlane" (constraint patch) or "symmetryMod" (DVMsymmetry)."""
+    gas, rho0 = gas_from_kn(Kn)
+    xi_max = 4.0 * math.sqrt(2 * gas["R"] * 273.0)
+    mtype = "symmetryPlane" if sym == "symmetryPlane" else "wall"
+    mesh = structured_mesh(nx, ny, 1, lx=0.5, ly=1.0, lz=1.0 / ny, two_d=True, patch_defs=[
+        ("movingWall", "wall", ["y1"], None), ("fixedWalls", "wall", ["x0", "y0"], None),
+        ("symmetryWall", mtype, ["x1"], sym)])
+    return make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, bvals={"symmetryWall": dict(T=273.0)})
 
 
 def batch_case(inst):

@@ -51,7 +51,22 @@ struct StepArgs {
     double *rho, *U, *T, *q, *tau;       // cells ([nC], [nC][3], ...)
     double *rhoF, *UF, *TF, *qF, *tauF;  // active faces
     int* status;             // device status word (DUGKS_ERR_NUMERIC on bad state)
+    // boundary patches other than diffuse walls (plain FP64 pipeline only);
+    // bcMask == 1 << kBcMaxwell when every boundary face is a diffuse wall
+    int bcMask;              // bit k set when some boundary face has kind k
+    const int* bKind;        // [nW] patch kind of each boundary face (kBc*)
+    double* rhoB;            // [nW] rho patch values (pressure patches update them)
+    double* TbM;             // [nW] = Tw, writable (pressureOut updates T_b)
+    double* UbM;             // [nW][3] = Uw, writable (pressure patches update U_b)
+    const double* pB;        // [nW] pressure of the face's pressureIn/Out patch
+    const double* bS0;       // [nW][3] area vector of the first face of the face's patch
+    const int* symOff;       // [nW] row of symTab for symmetry faces, else -1
+    const int* symTab;       // [rows][nV] mirror velocity of each velocity
 };
+
+// Boundary kinds (values of dugks_patch_kind in dugks/dugks.h).
+constexpr int kBcEmpty = 0, kBcMaxwell = 1, kBcZeroGradient = 2, kBcFixedValue = 3, kBcFarField = 4,
+              kBcPressureIn = 5, kBcPressureOut = 6, kBcSymmetryMod = 7, kBcSymmetryPlane = 8;
 
 #ifdef __CUDACC__
 __device__ __forceinline__ void shakhov_ref(double rho, double Ux, double Uy, double Uz, double T,

@@ -17,10 +17,14 @@ struct RefBuffers {
     double *gG, *hG;     // [nC][D][Vp]   least-squares gradients
     double *Gbg, *Gbh;   // [nW][Vp]      lagged fixedGradient gradients
     double *gS, *hS;     // [nA][Vp]      face distributions
+    double *gSym, *hSym; // [nW][Vp]      snapshot of symmetry faces (when present)
 };
 
 // Launch pass `pass` (0..kRefKernels-1) of one reference-pipeline step.
+// Pass 3 also runs the symmetry-patch copy, pass 7 the pressure-patch update.
 void launch_ref_pass(int pass, const StepArgs& a, const RefBuffers& b, int sms, cudaStream_t s);
+// Initial face values of mixed (rho fixedValue) patches; once, at creation.
+void launch_ref_mixed_init(const StepArgs& a, const RefBuffers& b, cudaStream_t s);
 
 // ------------------------------------------------------------- fused pipeline
 struct FusedPlanDev;  // defined in fused_pipeline.cu

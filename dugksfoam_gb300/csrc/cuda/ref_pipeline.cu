@@ -7,10 +7,17 @@
 //   k_grad      P2 fvc::grad + fixedGradient   discreteVelocity.C:420-470
 //   k_recon     P3 updateGHbarSurf             discreteVelocity.C:472-691
 //   k_wall      P4+P5 MaxwellWallRho / WallIn  fvDVM.C:347-367, discreteVelocity.C:693-731
+//   k_sym_*     P5b updateGHbarSurfSymmetryIn  fvDVM.C:375-454, discreteVelocity.C:733-817
 //   k_face_mom  P6 updateMacroSurf             fvDVM.C:456-582
 //   k_relax     P7 updateGHsurf                discreteVelocity.C:819-932
 //   k_cell      P8 updateGHtildeVol            discreteVelocity.C:934-978
 //   k_cell_mom  P9 updateMacroVol              fvDVM.C:597-728
+//   k_pressure  P10 updatePressureInOutBC      fvDVM.C:730-806
+//
+// Boundary faces follow the surface patch type of their rho boundary
+// condition (discreteVelocity::setBCtype, discreteVelocity.C:250-300):
+// diffuse walls, zeroGradient, mixed (rho fixedValue), farField (also for
+// pressureIn / pressureOut) and the two symmetry types.
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -72,10 +79,13 @@ __global__ void k_grad(StepArgs a, const double* __restrict__ gB, const double* 
             } else {
                 int wf = f - a.nI;
                 long long wi = (long long)wf * Vp + v;
-                double gbv = gc + Gbg[wi] / a.dcW[wf];
+                // symmetryPlane is a constraint patch of gBarPvol: its scalar
+                // value is the internal value, so it adds nothing
+                const bool sym = a.bKind[wf] == kBcSymmetryPlane;
+                double gbv = sym ? gc : gc + Gbg[wi] / a.dcW[wf];
                 double dg = gbv - gc;
                 double dh = 0.0;
-                if (a.hasH) { double hbv = hc + Gbh[wi] / a.dcW[wf]; dh = hbv - hc; }
+                if (a.hasH) { double hbv = sym ? hc : hc + Gbh[wi] / a.dcW[wf]; dh = hbv - hc; }
                 const double* L = a.bVec + 3 * wf;
                 for (int k = 0; k < D; ++k) { g[k] += L[k] * dg; h[k] += L[k] * dh; }
             }
@@ -132,10 +142,25 @@ __global__ void k_recon(StepArgs a, const double* __restrict__ gB, const double*
                 if (a.hasH)
                     hS[i] = 0.5 * (recon(hB, hG, nb, v, Vp, D, dN, xi, a.dt) + recon(hB, hG, o, v, Vp, D, dO, xi, a.dt));
             }
-        } else if (xs > 0) {
-            int o = a.own[f];
-            gS[i] = recon(gB, gG, o, v, Vp, D, dO, xi, a.dt);
-            if (a.hasH) hS[i] = recon(hB, hG, o, v, Vp, D, dO, xi, a.dt);
+        } else {
+            const int wf = f - a.nI, kind = a.bKind[wf], o = a.own[f];
+            if (kind == kBcZeroGradient) {  // gSurf == gBarPvol patchInternalField, every DV
+                gS[i] = gB[(long long)o * Vp + v];
+                if (a.hasH) hS[i] = hB[(long long)o * Vp + v];
+                continue;
+            }
+            const bool sym = kind == kBcSymmetryMod || kind == kBcSymmetryPlane;
+            if (sym ? xs > -kVSmall : xs > 0) {  // outgoing (and tangential on symmetry patches)
+                gS[i] = recon(gB, gG, o, v, Vp, D, dO, xi, a.dt);
+                if (a.hasH) hS[i] = recon(hB, hG, o, v, Vp, D, dO, xi, a.dt);
+            } else if (kind == kBcFarField || kind == kBcPressureIn || kind == kBcPressureOut) {
+                // incoming: rho_b M(U of the owner cell, T_b) (discreteVelocity.C:570-600)
+                const double Tb = a.TbM[wf];
+                const double g = a.rhoB[wf] * maxwell_by_rho_ref(a.U[3 * o], a.U[3 * o + 1], a.U[3 * o + 2], Tb,
+                                                                 xi[0], xi[1], xi[2], a.R, a.D);
+                gS[i] = g;
+                if (a.hasH) hS[i] = g * (a.R * Tb) * (a.K + 3 - a.D);
+            }
         }
     }
 }
@@ -145,6 +170,7 @@ __global__ void k_recon(StepArgs a, const double* __restrict__ gB, const double*
 __global__ void k_wall(StepArgs a, double* __restrict__ gS, double* __restrict__ hS) {
     __shared__ double red[32];
     const int wf = blockIdx.x;
+    if (a.bKind[wf] != kBcMaxwell) return;  // uniform over the block
     const int f = a.nI + wf;
     const int Vp = a.Vp;
     const double* S = a.Sf + 3 * f;
@@ -166,6 +192,47 @@ __global__ void k_wall(StepArgs a, double* __restrict__ gS, double* __restrict__
             gS[(long long)f * Vp + v] = g;
             if (a.hasH) hS[(long long)f * Vp + v] = g * (a.R * Tw) * (a.K + 3 - a.D);
         }
+    }
+}
+
+// Symmetry patches, step 1: snapshot of the face values of every velocity.
+__global__ void k_sym_snap(StepArgs a, const double* __restrict__ gS, const double* __restrict__ hS,
+                           double* __restrict__ gSnap, double* __restrict__ hSnap) {
+    const int wf = blockIdx.x;
+    if (a.symOff[wf] < 0) return;
+    const long long fb = (long long)(a.nI + wf) * a.Vp, wb = (long long)wf * a.Vp;
+    for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
+        gSnap[wb + v] = gS[fb + v];
+        if (a.hasH) hSnap[wb + v] = hS[fb + v];
+    }
+}
+
+// Step 2: incoming velocities (xi.S0 <= 0, S0 the patch's first face) take
+// their mirror velocity's value.  DVMsymmetry reads the snapshot; symmetryPlane
+// assigns velocity by velocity in index order, so a mirror that is itself an
+// earlier incoming velocity already holds its own mirror's value: the chain is
+// followed back to a snapshot value (one step on grids symmetric about 0).
+__global__ void k_sym_in(StepArgs a, double* __restrict__ gS, double* __restrict__ hS,
+                         const double* __restrict__ gSnap, const double* __restrict__ hSnap) {
+    const int wf = blockIdx.x;
+    const int row = a.symOff[wf];
+    if (row < 0) return;
+    const int Vp = a.Vp, nV = a.nV;
+    const bool plane = a.bKind[wf] == kBcSymmetryPlane;
+    const double* S0 = a.bS0 + 3 * wf;
+    const int* tab = a.symTab + (long long)row * nV;
+    const long long fb = (long long)(a.nI + wf) * Vp, wb = (long long)wf * Vp;
+    auto incoming = [&](int u) { return a.xi[u] * S0[0] + a.xi[Vp + u] * S0[1] + a.xi[2 * Vp + u] * S0[2] <= 0; };
+    for (int v = threadIdx.x; v < nV; v += blockDim.x) {
+        if (!incoming(v)) continue;
+        int cur = v, u = tab[v];
+        if (plane)
+            for (int guard = 0; guard < nV && u < cur && incoming(u); ++guard) {
+                cur = u;
+                u = tab[u];
+            }
+        gS[fb + v] = gSnap[wb + u];
+        if (a.hasH) hS[fb + v] = hSnap[wb + u];
     }
 }
 
@@ -191,8 +258,8 @@ __global__ void k_face_mom(StepArgs a, const double* __restrict__ gS, const doub
     const double Ux = m[1] / rho, Uy = m[2] / rho, Uz = m[3] / rho;
     const double T = (m[4] - 0.5 * rho * (Ux * Ux + Uy * Uy + Uz * Uz)) / ((a.K + 3) / 2.0 * a.R * rho);
     const double tau = tau_ref(T, rho, a.muRef, a.omega, a.Tref, a.R);
-    const bool wall = f >= a.nI;
     const int wf = f - a.nI;
+    const bool wall = f >= a.nI && a.bKind[wf] == kBcMaxwell;
     double qq[15];
     for (int i = 0; i < 15; ++i) qq[i] = 0.0;
     double Uw0 = 0, Uw1 = 0, Uw2 = 0;
@@ -249,17 +316,24 @@ __global__ void k_relax(StepArgs a, double* __restrict__ gS, double* __restrict_
         dv_index(i, Vp, f, v);
         if (v >= a.nV) continue;
         double x0 = a.xi[v], x1 = a.xi[Vp + v], x2 = a.xi[2 * Vp + v];
+        int times = 1;
         if (f >= a.nI) {
+            // The project's surface patch types ignore the field assignment
+            // (e.g. maxwellWallFvsPatchField.H:163-181), symmetryPlane takes it;
+            // then every outgoing DV is relaxed once more (discreteVelocity.C:887-931).
             const double* S = a.Sf + 3 * f;
-            if (!(x0 * S[0] + x1 * S[1] + x2 * S[2] > 0)) continue;  // incoming wall DVs stay unrelaxed
+            times = (a.bKind[f - a.nI] == kBcSymmetryPlane) + (x0 * S[0] + x1 * S[1] + x2 * S[2] > 0);
+            if (times == 0) continue;  // incoming boundary DVs stay unrelaxed
         }
         const double hh = 0.5 * a.dt;
         double b = hh / (2 * a.tauF[f] + hh);
         double ge, he;
         shakhov_ref(a.rhoF[f], a.UF[3 * f], a.UF[3 * f + 1], a.UF[3 * f + 2], a.TF[f], a.qF[3 * f], a.qF[3 * f + 1],
                     a.qF[3 * f + 2], x0, x1, x2, a.R, a.Pr, a.D, a.K, ge, he);
-        gS[i] = (1.0 - b) * gS[i] + b * ge;
-        if (a.hasH) hS[i] = (1.0 - b) * hS[i] + b * he;
+        for (int t = 0; t < times; ++t) {
+            gS[i] = (1.0 - b) * gS[i] + b * ge;
+            if (a.hasH) hS[i] = (1.0 - b) * hS[i] + b * he;
+        }
     }
 }
 
@@ -335,6 +409,52 @@ __global__ void k_cell_mom(StepArgs a, const double* __restrict__ gT, const doub
     }
 }
 
+// P10: pressureIn / pressureOut patch values from the new cell macros of the
+// owner (characteristic relations of fvDVM::updatePressureInOutBC).
+__global__ void k_pressure(StepArgs a) {
+    const int wf = blockIdx.x * blockDim.x + threadIdx.x;
+    if (wf >= a.nW) return;
+    const int kind = a.bKind[wf];
+    if (kind != kBcPressureIn && kind != kBcPressureOut) return;
+    const int f = a.nI + wf, P = a.own[f];
+    const double* Sf = a.Sf + 3 * f;
+    const double magSf = sqrt(Sf[0] * Sf[0] + Sf[1] * Sf[1] + Sf[2] * Sf[2]);
+    const double n[3] = {Sf[0] / magSf, Sf[1] / magSf, Sf[2] / magSf};
+    const double Ui[3] = {a.U[3 * P], a.U[3 * P + 1], a.U[3 * P + 2]};
+    const double Ti = a.T[P], rhoi = a.rho[P], R = a.R, p = a.pB[wf];
+    const double ai = sqrt(R * Ti * (a.K + 5) / (a.K + 3));
+    const double Un = Ui[0] * n[0] + Ui[1] * n[1] + Ui[2] * n[2];
+    double UnIn;
+    if (kind == kBcPressureIn) {
+        a.rhoB[wf] = p / R / a.TbM[wf];
+        UnIn = Un + (p - rhoi * R * Ti) / rhoi / ai;
+    } else {
+        a.rhoB[wf] = rhoi + (p - rhoi * R * Ti) / ai / ai;
+        a.TbM[wf] = p / (R * rhoi);
+        UnIn = Un + (rhoi * R * Ti - p) / rhoi / ai;
+    }
+    for (int k = 0; k < 3; ++k) a.UbM[3 * wf + k] = UnIn * n[k] + (Ui[k] - Un * n[k]);
+}
+
+// Initial face values of mixed patches (rho fixedValue): the Maxwellian of the
+// patch rho, U, T for every DV (discreteVelocity::initBoundaryField,
+// discreteVelocity.C:302-345, equilibriumMaxwell :1046-1061).
+__global__ void k_mixed_init(StepArgs a, double* __restrict__ gS, double* __restrict__ hS) {
+    const int wf = blockIdx.x;
+    if (a.bKind[wf] != kBcFixedValue) return;
+    const long long fb = (long long)(a.nI + wf) * a.Vp;
+    const double rho = a.rhoB[wf], T = a.TbM[wf], R = a.R;
+    const double* U = a.UbM + 3 * wf;
+    const double s = sqrt(2.0 * kPi * R * T);
+    const double pw = (a.D == 2) ? s * s : (a.D == 3 ? s * s * s : s);
+    for (int v = threadIdx.x; v < a.nV; v += blockDim.x) {
+        const double c0 = U[0] - a.xi[v], c1 = U[1] - a.xi[a.Vp + v], c2 = U[2] - a.xi[2 * a.Vp + v];
+        const double g = rho / pw * exp(-(c0 * c0 + c1 * c1 + c2 * c2) / (2.0 * R * T));
+        gS[fb + v] = g;
+        if (a.hasH) hS[fb + v] = (a.K + 3 - a.D) * R * T * g;
+    }
+}
+
 int grid_for(long long n, int threads, int sms) {
     long long b = (n + threads - 1) / threads;
     long long cap = (long long)sms * 32;
@@ -342,6 +462,10 @@ int grid_for(long long n, int threads, int sms) {
 }
 
 }  // namespace
+
+void launch_ref_mixed_init(const StepArgs& a, const RefBuffers& b, cudaStream_t s) {
+    if (a.nW > 0 && (a.bcMask & (1 << kBcFixedValue))) k_mixed_init<<<a.nW, kRedThreads, 0, s>>>(a, b.gS, b.hS);
+}
 
 const char* const kRefKernelNames[kRefKernels] = {"k_barp", "k_grad", "k_recon", "k_wall",
                                                   "k_face_mom", "k_relax", "k_cell", "k_cell_mom"};
@@ -352,11 +476,21 @@ void launch_ref_pass(int pass, const StepArgs& a, const RefBuffers& b, int sms, 
         case 0: k_barp<<<grid_for(nCV, kThreads, sms), kThreads, 0, s>>>(a, b.gT, b.hT, b.gB, b.hB); break;
         case 1: k_grad<<<grid_for(nCV, kThreads, sms), kThreads, 0, s>>>(a, b.gB, b.hB, b.gG, b.hG, b.Gbg, b.Gbh); break;
         case 2: k_recon<<<grid_for(nAV, kThreads, sms), kThreads, 0, s>>>(a, b.gB, b.hB, b.gG, b.hG, b.gS, b.hS); break;
-        case 3: if (a.nW > 0) k_wall<<<a.nW, kRedThreads, 0, s>>>(a, b.gS, b.hS); break;
+        case 3:
+            if (a.nW > 0 && (a.bcMask & (1 << kBcMaxwell))) k_wall<<<a.nW, kRedThreads, 0, s>>>(a, b.gS, b.hS);
+            if (a.bcMask & ((1 << kBcSymmetryMod) | (1 << kBcSymmetryPlane))) {
+                k_sym_snap<<<a.nW, kRedThreads, 0, s>>>(a, b.gS, b.hS, b.gSym, b.hSym);
+                k_sym_in<<<a.nW, kRedThreads, 0, s>>>(a, b.gS, b.hS, b.gSym, b.hSym);
+            }
+            break;
         case 4: k_face_mom<<<a.nA, kRedThreads, 0, s>>>(a, b.gS, b.hS); break;
         case 5: k_relax<<<grid_for(nAV, kThreads, sms), kThreads, 0, s>>>(a, b.gS, b.hS); break;
         case 6: k_cell<<<grid_for(nCV, kThreads, sms), kThreads, 0, s>>>(a, b.gT, b.hT, b.gB, b.hB, b.gS, b.hS); break;
-        case 7: k_cell_mom<<<a.nC, kRedThreads, 0, s>>>(a, b.gT, b.hT); break;
+        case 7:
+            k_cell_mom<<<a.nC, kRedThreads, 0, s>>>(a, b.gT, b.hT);
+            if (a.bcMask & ((1 << kBcPressureIn) | (1 << kBcPressureOut)))
+                k_pressure<<<(a.nW + 127) / 128, 128, 0, s>>>(a);
+            break;
         default: break;
     }
 }

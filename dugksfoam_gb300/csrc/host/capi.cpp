@@ -1,6 +1,7 @@
 // extern "C" entry points of libdugks (include/dugks/dugks.h).
 #include <cstring>
 #include <exception>
+#include <cstdio>
 #include <filesystem>
 #include <memory>
 #include <string>
@@ -20,6 +21,7 @@ struct dugks_handle {
     std::vector<std::string> patchNames;
     std::vector<int32_t> patchStart, patchSize, patchKind;
     std::vector<double> wallU, wallT;  // per boundary face
+    std::vector<double> patchPressure; // per patch (pressureIn / pressureOut)
 };
 
 namespace {
@@ -55,7 +57,7 @@ int dugks_create(const dugks_case_desc* desc, dugks_handle** out) {
         int code = DUGKS_OK;
         auto s = dugks::Solver::create(*desc, err, code);
         if (!s) { g_err = err; return code; }
-        auto* h = new dugks_handle{std::move(s), std::string(), {}, {}, {}, {}, {}, {}};
+        auto* h = new dugks_handle{std::move(s), std::string(), {}, {}, {}, {}, {}, {}, {}};
         const int nB = desc->n_faces - desc->n_internal_faces;
         for (int p = 0; p < desc->n_patches; ++p) {
             h->patchNames.push_back("patch" + std::to_string(p));
@@ -65,6 +67,7 @@ int dugks_create(const dugks_case_desc* desc, dugks_handle** out) {
         }
         if (desc->wall_U) h->wallU.assign(desc->wall_U, desc->wall_U + 3 * (size_t)nB);
         if (desc->wall_T) h->wallT.assign(desc->wall_T, desc->wall_T + nB);
+        if (desc->patch_pressure) h->patchPressure.assign(desc->patch_pressure, desc->patch_pressure + desc->n_patches);
         *out = h;
         return DUGKS_OK;
     } catch (const std::exception& e) {
@@ -91,6 +94,7 @@ int dugks_create_from_case_dir(const char* dir, int32_t precision, dugks_handle*
     d.n_patches = (int32_t)c.patchNames.size();
     d.patch_start = c.patchStart.data(); d.patch_size = c.patchSize.data(); d.patch_kind = c.patchKind.data();
     d.wall_U = c.wallU.data(); d.wall_T = c.wallT.data();
+    d.bnd_rho = c.bndRho.data(); d.patch_pressure = c.patchPressure.data();
     d.n_xi_per_dim = c.nDV; d.xis = c.xis.data(); d.weights = c.weights.data(); d.xi_max = c.xiMax;
     d.R = c.R; d.omega = c.omega; d.Tref = c.Tref; d.muRef = c.muRef; d.Pr = c.Pr; d.KInner = c.KInner;
     d.rho0 = c.rho0.data(); d.U0 = c.U0.data(); d.T0 = c.T0.data();
@@ -115,8 +119,10 @@ int dugks_inspect_case_dir(const char* dir, dugks_case_summary* out) {
     r.n_points = (int32_t)(c.points.size() / 3);
     r.n_cells = c.nCells; r.n_faces = c.nFaces; r.n_internal_faces = c.nInternal;
     r.n_patches = (int32_t)c.patchNames.size();
-    for (size_t p = 0; p < c.patchNames.size(); ++p)
-        (c.patchKind[p] == DUGKS_PATCH_MAXWELL ? r.n_wall_faces : r.n_empty_faces) += c.patchSize[p];
+    for (size_t p = 0; p < c.patchNames.size(); ++p) {
+        if (c.patchKind[p] == DUGKS_PATCH_MAXWELL) r.n_wall_faces += c.patchSize[p];
+        if (c.patchKind[p] == DUGKS_PATCH_EMPTY) r.n_empty_faces += c.patchSize[p];
+    }
     r.n_xi_per_dim = c.nDV; r.KInner = c.KInner;
     r.xi_max = c.xiMax; r.R = c.R; r.omega = c.omega; r.Tref = c.Tref; r.muRef = c.muRef; r.Pr = c.Pr;
     r.delta_t = c.deltaT;
@@ -136,33 +142,46 @@ int dugks_write_time(dugks_handle* h, const char* case_dir, const char* time_nam
         std::vector<double> qF(3 * (size_t)(m.nI + m.nW));
         if (int e = s.faceMacros(nullptr, nullptr, nullptr, qF.data(), nullptr)) return e;
         // per patch outputs, in patch face order
+        static const char* const kRhoType[] = {"empty", "calculatedMaxwell", "zeroGradient", "fixedValue", "farField",
+                                               "pressureIn", "pressureOut", "symmetryMod", "symmetryPlane"};
         std::vector<dugks::PatchOut> pr(nP), pu(nP), pt(nP), pq(nP), pqs(nP), pst(nP);
         for (int p = 0; p < nP; ++p) {
-            const bool wall = h->patchKind[p] == DUGKS_PATCH_MAXWELL;
-            pr[p] = {h->patchNames[p], wall ? "calculatedMaxwell" : "empty", {}};
-            pu[p] = {h->patchNames[p], wall ? "fixedValue" : "empty", {}};
+            const int kind = h->patchKind[p];
+            const bool wall = kind == DUGKS_PATCH_MAXWELL, empty = kind == DUGKS_PATCH_EMPTY;
+            const bool plane = kind == DUGKS_PATCH_SYMMETRY_PLANE;
+            const char* uT = empty ? "empty" : (plane ? "symmetryPlane" : "fixedValue");
+            const char* calc = empty ? "empty" : (plane ? "symmetryPlane" : "calculated");
+            pr[p] = {h->patchNames[p], kRhoType[kind], {}, {}};
+            pu[p] = {h->patchNames[p], uT, {}, {}};
             pt[p] = pu[p];
-            pq[p] = {h->patchNames[p], wall ? "calculated" : "empty", {}};
+            pq[p] = {h->patchNames[p], calc, {}, {}};
             pqs[p] = pq[p];
             pst[p] = pq[p];
-            if (!wall) continue;
+            if (empty || plane) continue;
             const int n = h->patchSize[p];
-            std::vector<double> rw(n), qw(3 * (size_t)n), sw(9 * (size_t)n);
-            if (int e = s.wall(p, rw.data(), qw.data(), sw.data())) return e;
-            pr[p].values = rw;
+            if (kind == DUGKS_PATCH_PRESSURE_IN || kind == DUGKS_PATCH_PRESSURE_OUT) {
+                char buf[64];
+                std::snprintf(buf, sizeof buf, "%.17g", h->patchPressure.empty() ? 0.0 : h->patchPressure[p]);
+                pr[p].extra = std::string(kRhoType[kind]) + " " + buf;
+            }
+            std::vector<double> rb(n), ub(3 * (size_t)n), tb(n), qw(3 * (size_t)n, 0.0), sw(9 * (size_t)n, 0.0);
+            if (int e = s.boundary(p, rb.data(), ub.data(), tb.data())) return e;
+            if (wall && (s.wall(p, nullptr, qw.data(), sw.data()) != DUGKS_OK)) return DUGKS_ERR_CUDA;
+            if (kind == DUGKS_PATCH_ZERO_GRADIENT || kind == DUGKS_PATCH_SYMMETRY_MOD)
+                for (int i = 0; i < n; ++i) rb[i] = rho[m.owner[h->patchStart[p] + i]];
+            pr[p].values = rb;
+            pu[p].values = ub;
+            pt[p].values = tb;
             pqs[p].values = qw;
             pst[p].values = sw;
-            const int b0 = h->patchStart[p] - nI;  // boundary-face offset of the patch
-            for (int i = 0; i < n; ++i) {
-                for (int k = 0; k < 3; ++k) pu[p].values.push_back(h->wallU.empty() ? 0.0 : h->wallU[3 * (size_t)(b0 + i) + k]);
-                pt[p].values.push_back(h->wallT.empty() ? 0.0 : h->wallT[b0 + i]);
-            }
         }
-        // face heat flux of the wall faces, by wall index -> patch position
+        // face heat flux of the active boundary faces, by boundary index -> patch position
         for (int p = 0; p < nP; ++p)
-            if (h->patchKind[p] == DUGKS_PATCH_MAXWELL) pq[p].values.assign(3 * (size_t)h->patchSize[p], 0.0);
+            if (h->patchKind[p] != DUGKS_PATCH_EMPTY && h->patchKind[p] != DUGKS_PATCH_SYMMETRY_PLANE)
+                pq[p].values.assign(3 * (size_t)h->patchSize[p], 0.0);
         for (int w = 0; w < m.nW; ++w) {
             const int p = m.wallPatch[w], i = m.wallFace[w] - h->patchStart[p];
+            if (pq[p].values.empty()) continue;
             for (int k = 0; k < 3; ++k) pq[p].values[3 * (size_t)i + k] = qF[3 * (size_t)(nI + w) + k];
         }
         const std::string dir = std::string(case_dir) + "/" + time_name;
@@ -239,6 +258,10 @@ int dugks_get_face_macros(dugks_handle* h, double* rho, double* U, double* T, do
 
 int dugks_get_wall(dugks_handle* h, int32_t patch, double* rho_w, double* q_wall, double* stress_wall) {
     return call(h, [&](dugks::Solver& s) -> int { return s.wall(patch, rho_w, q_wall, stress_wall); });
+}
+
+int dugks_get_boundary(dugks_handle* h, int32_t patch, double* rho, double* U, double* T) {
+    return call(h, [&](dugks::Solver& s) -> int { return s.boundary(patch, rho, U, T); });
 }
 
 int dugks_get_residual(dugks_handle* h, double res[3]) {

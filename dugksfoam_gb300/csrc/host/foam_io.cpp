@@ -345,8 +345,17 @@ bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err) {
     if (!brho || !bU || !bT) { err = "0/{rho,U,T}: missing boundaryField"; return false; }
     c.wallU.assign(3 * (size_t)nB, 0.0);
     c.wallT.assign(nB, 0.0);
+    c.bndRho.assign(nB, 0.0);
+    c.patchPressure.assign(nP, 0.0);
     c.rhoBC.clear();
     c.patchKind.clear();
+    // rho boundary type -> kind (discreteVelocity::setBCtype, discreteVelocity.C:250-300)
+    static const std::pair<const char*, int> kKinds[] = {
+        {"calculatedMaxwell", DUGKS_PATCH_MAXWELL}, {"empty", DUGKS_PATCH_EMPTY},
+        {"zeroGradient", DUGKS_PATCH_ZERO_GRADIENT}, {"fixedValue", DUGKS_PATCH_FIXED_VALUE},
+        {"farField", DUGKS_PATCH_FAR_FIELD}, {"pressureIn", DUGKS_PATCH_PRESSURE_IN},
+        {"pressureOut", DUGKS_PATCH_PRESSURE_OUT}, {"symmetryMod", DUGKS_PATCH_SYMMETRY_MOD},
+        {"symmetryPlane", DUGKS_PATCH_SYMMETRY_PLANE}};
     for (int p = 0; p < nP; ++p) {
         const Dict* pr = brho->sub(c.patchNames[p]);
         const Entry* ty = pr ? pr->find("type") : nullptr;
@@ -359,26 +368,48 @@ bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err) {
         }
         std::string type = (ty && !ty->toks.empty()) ? ty->toks[0].s : std::string("empty");
         c.rhoBC.push_back(type);
-        if (type == "calculatedMaxwell") {
-            c.patchKind.push_back(DUGKS_PATCH_MAXWELL);
-        } else if (type == "empty") {
-            c.patchKind.push_back(DUGKS_PATCH_EMPTY);
-            continue;
-        } else {
+        int kind = -1;
+        for (const auto& k : kKinds)
+            if (type == k.first) kind = k.second;
+        if (kind < 0) {
             err = "unsupported rho boundary type '" + type + "' on patch " + c.patchNames[p] +
-                  " (supported: calculatedMaxwell, empty)";
+                  " (supported: calculatedMaxwell, zeroGradient, fixedValue, farField, pressureIn, pressureOut, "
+                  "symmetryMod, symmetryPlane, empty)";
             return false;
         }
+        c.patchKind.push_back(kind);
+        if (kind == DUGKS_PATCH_EMPTY) continue;
+        const int s = c.patchStart[p] - c.nInternal, n = c.patchSize[p];
+        if (kind == DUGKS_PATCH_FIXED_VALUE || kind == DUGKS_PATCH_FAR_FIELD) {
+            std::vector<double> rv;
+            if (!fieldValues(pr->find("value"), n, 1, rv, err)) { err = "0/rho " + c.patchNames[p] + ": " + err; return false; }
+            for (int i = 0; i < n; ++i) c.bndRho[s + i] = rv[i];
+        }
+        if (kind == DUGKS_PATCH_PRESSURE_IN || kind == DUGKS_PATCH_PRESSURE_OUT) {
+            const char* key = kind == DUGKS_PATCH_PRESSURE_IN ? "pressureIn" : "pressureOut";
+            if (!lastNumber(pr->find(key), c.patchPressure[p])) {
+                err = std::string("0/rho ") + c.patchNames[p] + ": missing " + key;
+                return false;
+            }
+        }
+        // U and T patch values: the "value" entry, else the owner cells' initial
+        // values (zeroGradient-like entries without a value)
         const Dict* pu = bU->sub(c.patchNames[p]);
         const Dict* pt = bT->sub(c.patchNames[p]);
         if (!pu || !pt) { err = "0/U or 0/T: no boundary entry for patch " + c.patchNames[p]; return false; }
         std::vector<double> uv, tv;
-        if (!fieldValues(pu->find("value"), c.patchSize[p], 3, uv, err)) { err = "0/U " + c.patchNames[p] + ": " + err; return false; }
-        if (!fieldValues(pt->find("value"), c.patchSize[p], 1, tv, err)) { err = "0/T " + c.patchNames[p] + ": " + err; return false; }
-        int s = c.patchStart[p] - c.nInternal;
-        for (int i = 0; i < c.patchSize[p]; ++i) {
-            for (int k = 0; k < 3; ++k) c.wallU[3 * (size_t)(s + i) + k] = uv[3 * (size_t)i + k];
-            c.wallT[s + i] = tv[i];
+        const bool needValues = kind == DUGKS_PATCH_MAXWELL;
+        if (pu->find("value") || needValues) {
+            if (!fieldValues(pu->find("value"), n, 3, uv, err)) { err = "0/U " + c.patchNames[p] + ": " + err; return false; }
+        }
+        if (pt->find("value") || needValues) {
+            if (!fieldValues(pt->find("value"), n, 1, tv, err)) { err = "0/T " + c.patchNames[p] + ": " + err; return false; }
+        }
+        for (int i = 0; i < n; ++i) {
+            const int own = c.owner[c.patchStart[p] + i];
+            for (int k = 0; k < 3; ++k)
+                c.wallU[3 * (size_t)(s + i) + k] = uv.empty() ? c.U0[3 * (size_t)own + k] : uv[3 * (size_t)i + k];
+            c.wallT[s + i] = tv.empty() ? c.T0[own] : tv[i];
         }
     }
     // DVMProperties
@@ -456,7 +487,12 @@ bool write_vol_field(const std::string& path, const std::string& name, const std
     o << "boundaryField\n{\n";
     for (const PatchOut& p : patches) {
         o << "    " << p.name << "\n    {\n        type            " << p.type << ";\n";
-        if (p.type != "empty") {
+        if (!p.extra.empty()) {
+            const size_t sp = p.extra.find(' ');
+            o << "        " << p.extra.substr(0, sp) << std::string(sp < 16 ? 16 - sp : 1, ' ') << p.extra.substr(sp + 1)
+              << ";\n";
+        }
+        if (p.type != "empty" && p.type != "symmetryPlane") {
             const size_t m = p.values.size() / ncomp;
             o << "        value           nonuniform List<" << lst << "> " << m << "(";
             for (size_t i = 0; i < m; ++i) { o << (i ? " " : ""); item(p.values.data() + ncomp * i); }

@@ -25,7 +25,9 @@ struct FoamCase {
     std::vector<int32_t> patchKind;                     // dugks_patch_kind
     // fields
     std::vector<double> rho0, U0, T0;                   // internal
-    std::vector<double> wallU, wallT;                   // per boundary face
+    std::vector<double> wallU, wallT;                   // U, T patch values per boundary face
+    std::vector<double> bndRho;                         // rho patch values per boundary face
+    std::vector<double> patchPressure;                  // pressureIn / pressureOut per patch
     // DVMProperties
     int nDV = 0;
     double xiMax = 0, xiMin = 0;
@@ -44,6 +46,7 @@ bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err);
 struct PatchOut {
     std::string name, type;
     std::vector<double> values;  // ncomp per face
+    std::string extra;           // one more "keyword value" entry (e.g. "pressureIn 1e5"), or empty
 };
 
 // Write a vol field in OpenFOAM ASCII (volScalarField / volVectorField /

@@ -101,8 +101,8 @@ bool build_mesh(const MeshInput& in, Mesh& m, std::string& err) {
         int s = in.patchStart[p] - nI, e = s + in.patchSize[p];
         if (s < 0 || e > nB) { err = "mesh: patch range outside boundary faces"; return false; }
         int kind = in.patchKind[p];
-        if (kind != DUGKS_PATCH_EMPTY && kind != DUGKS_PATCH_MAXWELL) {
-            err = "mesh: unsupported patch kind (supported: empty, calculatedMaxwell)";
+        if (kind < DUGKS_PATCH_EMPTY || kind > DUGKS_PATCH_SYMMETRY_PLANE) {
+            err = "mesh: unsupported patch kind";
             return false;
         }
         for (int b = s; b < e; ++b) { m.bKind[b] = kind; m.bPatch[b] = p; }
@@ -171,13 +171,14 @@ bool build_mesh(const MeshInput& in, Mesh& m, std::string& err) {
 
     // ---- wall (active boundary) faces
     m.globalToWall.assign(nB, -1);
-    m.wallFace.clear(); m.wallCell.clear(); m.wallPatch.clear();
+    m.wallFace.clear(); m.wallCell.clear(); m.wallPatch.clear(); m.wallKind.clear();
     for (int b = 0; b < nB; ++b) {
         if (m.bKind[b] == DUGKS_PATCH_EMPTY) continue;
         m.globalToWall[b] = (int)m.wallFace.size();
         m.wallFace.push_back(nI + b);
         m.wallCell.push_back(m.owner[nI + b]);
         m.wallPatch.push_back(m.bPatch[b]);
+        m.wallKind.push_back(m.bKind[b]);
     }
     m.nW = (int)m.wallFace.size();
 

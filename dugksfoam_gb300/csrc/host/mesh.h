@@ -36,11 +36,13 @@ struct Mesh {
     std::vector<int32_t> owner, neighbour;
     std::vector<int32_t> bKind;    // per boundary face
     std::vector<int32_t> bPatch;   // per boundary face
-    // Active faces = internal faces followed by non-empty boundary faces.
-    int nW = 0;                    // active boundary (wall) faces
+    // Active faces = internal faces followed by non-empty boundary faces
+    // ("wall" faces below: every non-empty boundary face, whatever its kind).
+    int nW = 0;                    // active boundary faces
     std::vector<int32_t> wallFace; // global face index of wall face w
     std::vector<int32_t> wallCell;
     std::vector<int32_t> wallPatch;
+    std::vector<int32_t> wallKind; // dugks_patch_kind of boundary face w
     std::vector<int32_t> globalToWall; // boundary face b -> w or -1
     std::vector<double> dcI;       // internal deltaCoeffs [nI]
     std::vector<double> pVec, nVec;// internal LS vectors [nI][3]

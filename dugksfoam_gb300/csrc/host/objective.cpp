@@ -114,6 +114,9 @@ int check(Solver& s, const Objective& o) {
         return s.fail(DUGKS_ERR_ARG, "objective: need 0 <= avg_first < n_steps");
     if (o.ckptEvery < 1) return s.fail(DUGKS_ERR_ARG, "objective: checkpoint_every must be >= 1");
     if (!(s.dt() > 0)) return s.fail(DUGKS_ERR_ARG, "objective: set dt first");
+    for (int32_t k : s.mesh().wallKind)
+        if (k != DUGKS_PATCH_MAXWELL)
+            return s.fail(DUGKS_ERR_UNSUPPORTED, "objective: the differentiated step takes diffuse walls only");
     return s.synchronize();
 }
 

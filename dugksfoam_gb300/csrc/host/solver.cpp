@@ -123,12 +123,40 @@ int Solver::init(const dugks_case_desc& d) {
     const int K = d.KInner;
     hasH_ = (K + 3 - D) != 0 ? 1 : 0;  // K=0, D=3: h equilibrium is identically 0
 
-    // ---- wall data and inComingByRho (fvDVM::setCalculatedMaxwellRhoBC, fvDVM.C:263-309)
-    std::vector<double> Uw(3 * (size_t)nW), Tw(nW), incAbs(nW);
+    // ---- boundary kinds other than diffuse walls: plain FP64 pipeline only
+    int bcMask = 0;
+    for (int wf = 0; wf < nW; ++wf) bcMask |= 1 << m.wallKind[wf];
+    if ((bcMask & ~(1 << DUGKS_PATCH_MAXWELL)) && pipeline_ != DUGKS_PIPE_REFERENCE)
+        return fail(DUGKS_ERR_UNSUPPORTED, "boundary types other than calculatedMaxwell walls need the plain FP64 "
+                                           "pipeline (DUGKS_FP64 with DUGKS_PIPE_REFERENCE or DUGKS_PIPE_AUTO)");
+    const bool pressureBc = bcMask & ((1 << DUGKS_PATCH_PRESSURE_IN) | (1 << DUGKS_PATCH_PRESSURE_OUT));
+    if (pressureBc && !d.patch_pressure) return fail(DUGKS_ERR_ARG, "pressureIn/pressureOut patches need patch_pressure");
+    if ((bcMask & ((1 << DUGKS_PATCH_FIXED_VALUE) | (1 << DUGKS_PATCH_FAR_FIELD))) && !d.bnd_rho)
+        return fail(DUGKS_ERR_ARG, "fixedValue/farField patches need bnd_rho");
+
+    // ---- boundary data and inComingByRho (fvDVM::setCalculatedMaxwellRhoBC, fvDVM.C:263-309)
+    std::vector<double> Uw(3 * (size_t)nW), Tw(nW), incAbs(nW, 1.0), rhoB(nW, 0.0), pB(nW, 0.0), bS0(3 * (size_t)nW);
     for (int wf = 0; wf < nW; ++wf) {
         int b = m.wallFace[wf] - nI;
+        const int kind = m.wallKind[wf], p = m.wallPatch[wf];
         for (int k = 0; k < 3; ++k) Uw[3 * wf + k] = d.wall_U[3 * b + k];
+        for (int k = 0; k < 3; ++k) bS0[3 * wf + k] = m.Sf[3 * (size_t)d.patch_start[p] + k];
         Tw[wf] = d.wall_T[b];
+        if (d.bnd_rho) rhoB[wf] = d.bnd_rho[b];
+        if (kind == DUGKS_PATCH_PRESSURE_IN || kind == DUGKS_PATCH_PRESSURE_OUT) {
+            // pressureIn/Out ctor: value 1 until the first update (pressureInFvPatchField.C:62-76)
+            rhoB[wf] = 1.0;
+            pB[wf] = d.patch_pressure[p];
+            if (!(pB[wf] > 0)) return fail(DUGKS_ERR_ARG, "patch pressure must be positive");
+        }
+        if ((kind == DUGKS_PATCH_FIXED_VALUE || kind == DUGKS_PATCH_FAR_FIELD) && !(rhoB[wf] > 0))
+            return fail(DUGKS_ERR_ARG, "fixedValue/farField rho patch values must be positive");
+        if (kind != DUGKS_PATCH_MAXWELL) {
+            const bool needT = kind == DUGKS_PATCH_FIXED_VALUE || kind == DUGKS_PATCH_FAR_FIELD ||
+                               kind == DUGKS_PATCH_PRESSURE_IN || kind == DUGKS_PATCH_PRESSURE_OUT;
+            if (needT && !(Tw[wf] > 0)) return fail(DUGKS_ERR_ARG, "boundary temperature must be positive");
+            continue;
+        }
         if (!(Tw[wf] > 0)) return fail(DUGKS_ERR_ARG, "wall temperature must be positive");
         const double* S = &m.Sf[3 * (size_t)m.wallFace[wf]];
         double acc = 0.0;
@@ -144,6 +172,40 @@ int Solver::init(const dugks_case_desc& d) {
         }
         incAbs[wf] = std::fabs(acc);
         if (!(incAbs[wf] > 0)) return fail(DUGKS_ERR_ARG, "wall face with no incoming discrete velocity");
+    }
+    // ---- symmetry patches: mirror velocity of every velocity, round(|n . (symX, symY, symZ)|)
+    // with n the patch's first-face normal (fvDVM.C:140-221, discreteVelocity.C:733-817)
+    std::vector<int32_t> symOff(nW, -1), symTab;
+    {
+        std::vector<int> patchRow(d.n_patches, -1);
+        for (int wf = 0; wf < nW; ++wf) {
+            const int kind = m.wallKind[wf], p = m.wallPatch[wf];
+            if (kind != DUGKS_PATCH_SYMMETRY_MOD && kind != DUGKS_PATCH_SYMMETRY_PLANE) continue;
+            if (patchRow[p] < 0) {
+                patchRow[p] = (int)(symTab.size() / nV_);
+                const double* S0 = &bS0[3 * wf];
+                const double mS = std::sqrt(S0[0] * S0[0] + S0[1] * S0[1] + S0[2] * S0[2]);
+                const double n[3] = {S0[0] / mS, S0[1] / mS, S0[2] / mS};
+                for (int v = 0; v < nV_; ++v) {
+                    int ix = v % M, iy = D == 3 ? (v / M) % M : v / M, iz = D == 3 ? v / (M * M) : 0;
+                    double sx, sy, sz;
+                    if (D == 3) {
+                        sx = iz * M * M + iy * M + (M - ix - 1);
+                        sy = iz * M * M + (M - iy - 1) * M + ix;
+                        sz = (M - iz - 1) * M * M + iy * M + ix;
+                    } else {
+                        sx = iy * M + (M - ix - 1);
+                        sy = (M - iy - 1) * M + ix;
+                        sz = 0;
+                    }
+                    const long t = std::lround(std::fabs(n[0] * sx + n[1] * sy + n[2] * sz));
+                    if (t < 0 || t >= nV_)
+                        return fail(DUGKS_ERR_UNSUPPORTED, "symmetry patch is not normal to a coordinate axis");
+                    symTab.push_back((int32_t)t);
+                }
+            }
+            symOff[wf] = patchRow[p];
+        }
     }
     patchFirstWall_.assign(d.n_patches, -1);
     patchNWall_.assign(d.n_patches, 0);
@@ -220,6 +282,17 @@ int Solver::init(const dugks_case_desc& d) {
     a.Sf = dSf; a.dO = ddO; a.dN = ddN; a.own = down; a.nei = dnei; a.pVec = dpV; a.nVec = dnV; a.bVec = dbV;
     a.dcW = ddcW; a.nHatW = dnH; a.vol = dvol; a.cellOff = dcO; a.cellFace = dcF; a.xi = dxi; a.w = dw;
     a.Uw = dUw; a.Tw = dTw; a.incAbs = dinc;
+    a.bcMask = bcMask;
+    a.TbM = dTw; a.UbM = dUw;
+    {
+        int* dk = dalloc<int>(nW);
+        double *drB = dalloc<double>(nW), *dpB = dalloc<double>(nW), *dS0 = dalloc<double>(bS0.size());
+        int *dsO = dalloc<int>(nW), *dsT = dalloc<int>(std::max<size_t>(symTab.size(), 1));
+        if (oom_) return fail(DUGKS_ERR_OOM, "device allocation failed");
+        chk(up(dk, m.wallKind)); chk(up(drB, rhoB)); chk(up(dpB, pB)); chk(up(dS0, bS0)); chk(up(dsO, symOff));
+        if (!symTab.empty()) chk(up(dsT, symTab));
+        a.bKind = dk; a.rhoB = drB; a.pB = dpB; a.bS0 = dS0; a.symOff = dsO; a.symTab = dsT;
+    }
 
     // initial macros; face velocity = linear interpolation (fvDVM.C:1074) for the first CFL
     std::vector<double> UF(3 * (size_t)nA, 0.0), one(nW, 1.0);
@@ -256,8 +329,13 @@ int Solver::init(const dugks_case_desc& d) {
             b.hT = dalloc<double>(nCV); b.hB = dalloc<double>(nCV); b.hG = dalloc<double>(nCV * D);
             b.Gbh = dalloc<double>((size_t)nW * Vp); b.hS = dalloc<double>((size_t)nA * Vp);
         }
+        if (bcMask & ((1 << DUGKS_PATCH_SYMMETRY_MOD) | (1 << DUGKS_PATCH_SYMMETRY_PLANE))) {
+            b.gSym = dalloc<double>((size_t)nW * Vp);
+            if (hasH_) b.hSym = dalloc<double>((size_t)nW * Vp);
+        }
         if (oom_) return fail(DUGKS_ERR_OOM, "device allocation failed (distribution buffers)");
         launch_init_state<double>(a, b.gT, b.hT, 1.0, sms_, stream_);
+        launch_ref_mixed_init(a, b, stream_);
     } else {
         std::string ferr;
         fused_ = make_fused_pipeline(*this, a, precision_, ferr);
@@ -381,6 +459,19 @@ int Solver::wall(int patch, double* rhoW, double* qWall, double* stressWall) {
     if (stressWall && ce == cudaSuccess)
         ce = cudaMemcpy(stressWall, base_.stressWall + 9 * s, 9 * n * sizeof(double), cudaMemcpyDeviceToHost);
     return checkCuda(ce, "get wall");
+}
+
+int Solver::boundary(int patch, double* rho, double* U, double* T) {
+    if (patch < 0 || patch >= (int)patchFirstWall_.size()) return fail(DUGKS_ERR_ARG, "patch index out of range");
+    if (patchNWall_[patch] == 0) return fail(DUGKS_ERR_ARG, "patch has no active faces");
+    if (int e = synchronize()) return e;
+    const size_t s = patchFirstWall_[patch], n = patchNWall_[patch];
+    const bool wall = mesh_.wallKind[s] == DUGKS_PATCH_MAXWELL;
+    cudaError_t ce = cudaSuccess;
+    if (rho) ce = cudaMemcpy(rho, (wall ? base_.rhoW : base_.rhoB) + s, n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (U && ce == cudaSuccess) ce = cudaMemcpy(U, base_.Uw + 3 * s, 3 * n * sizeof(double), cudaMemcpyDeviceToHost);
+    if (T && ce == cudaSuccess) ce = cudaMemcpy(T, base_.Tw + s, n * sizeof(double), cudaMemcpyDeviceToHost);
+    return checkCuda(ce, "get boundary");
 }
 
 int Solver::residual(double res[3]) {

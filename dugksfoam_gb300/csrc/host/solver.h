@@ -32,6 +32,8 @@ public:
     int macros(double* rho, double* U, double* T, double* q, double* tau);
     int faceMacros(double* rho, double* U, double* T, double* q, double* tau);
     int wall(int patch, double* rhoW, double* qWall, double* stressWall);
+    // rho, U, T patch values of a non-empty patch (rho: Maxwell-wall density on walls)
+    int boundary(int patch, double* rho, double* U, double* T);
     int residual(double res[3]);
     int getDist(double* g, double* h);
     int setDist(const double* g, const double* h);

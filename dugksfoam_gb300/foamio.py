@@ -49,12 +49,15 @@ def _vector_list(v):
 
 
 def _field(path, cls, obj, dims, internal, patches, vector):
-    """internal: array; patches: list of (name, type, values or None)."""
+    """internal: array; patches: list of (name, type, values or None[, extra "key value" entry])."""
     kind = "vector" if vector else "scalar"
     lst = _vector_list(internal) if vector else _scalar_list(internal)
     body = f"dimensions      {dims};\n\ninternalField   nonuniform List<{kind}>\n{lst};\n\nboundaryField\n{{\n"
-    for name, typ, val in patches:
+    for name, typ, val, *extra in patches:
         body += f"    {name}\n    {{\n        type            {typ};\n"
+        for e in extra:
+            key, v = e.split(" ", 1)
+            body += f"        {key:<16}{v};\n"
         if val is not None:
             body += f"        value           nonuniform List<{kind}>\n"
             body += (_vector_list(val) if vector else _scalar_list(val)) + ";\n"
@@ -89,15 +92,22 @@ def write_case(case, path, delta_t=None, end_time=None):
     nI = len(nei)
     Ub, Tb = np.asarray(case["Ub"]), np.asarray(case["Tb"])
     prho, pU, pT = [], [], []
+    rhob = np.asarray(case.get("rhob", np.zeros(len(Tb))))
     for p in m["patches"]:
         s, e = p["startFace"] - nI, p["startFace"] - nI + p["nFaces"]
-        if p["type"] == "wall":
+        bc = p.get("bc", {"wall": "calculatedMaxwell"}.get(p["type"], p["type"]))
+        if bc == "calculatedMaxwell":
             prho.append((p["name"], "calculatedMaxwell", np.ones(p["nFaces"])))
             pU.append((p["name"], "fixedValue", Ub[s:e]))
             pT.append((p["name"], "fixedValue", Tb[s:e]))
-        else:
+        elif bc in ("empty", "symmetryPlane"):
             for lst in (prho, pU, pT):
-                lst.append((p["name"], "empty", None))
+                lst.append((p["name"], bc, None))
+        else:  # zeroGradient, fixedValue, farField, pressureIn, pressureOut, symmetryMod
+            extra = [f"{bc} {_f(p['pressure'])}"] if bc in ("pressureIn", "pressureOut") else []
+            prho.append((p["name"], bc, rhob[s:e], *extra))
+            pU.append((p["name"], "fixedValue", Ub[s:e]))
+            pT.append((p["name"], "fixedValue", Tb[s:e]))
     z = os.path.join(path, "0")
     _field(os.path.join(z, "rho"), "volScalarField", "rho", "[1 -3 0 0 0 0 0]", case["rho0"], prho, False)
     _field(os.path.join(z, "U"), "volVectorField", "U", "[0 1 -1 0 0 0 0]", case["U0"], pU, True)

@@ -20,6 +20,9 @@ FP64 = 0
 FP32_FP64MOM = 1
 PIPE_AUTO, PIPE_REFERENCE, PIPE_FUSED = 0, 1, 2
 PATCH_EMPTY, PATCH_MAXWELL = 0, 1
+# dugks_patch_kind by rho boundary-condition type (include/dugks/dugks.h)
+BC_KINDS = {"empty": 0, "calculatedMaxwell": 1, "zeroGradient": 2, "fixedValue": 3, "farField": 4,
+            "pressureIn": 5, "pressureOut": 6, "symmetryMod": 7, "symmetryPlane": 8}
 
 ERRORS = {0: "OK", 1: "DUGKS_ERR_ARG", 2: "DUGKS_ERR_IO", 3: "DUGKS_ERR_UNSUPPORTED", 4: "DUGKS_ERR_CUDA",
           5: "DUGKS_ERR_NUMERIC", 6: "DUGKS_ERR_TIMEOUT", 7: "DUGKS_ERR_OOM"}
@@ -28,7 +31,7 @@ ERRORS = {0: "OK", 1: "DUGKS_ERR_ARG", 2: "DUGKS_ERR_IO", 3: "DUGKS_ERR_UNSUPPOR
 EXPORTS = [
     "dugks_create", "dugks_create_from_case_dir", "dugks_destroy", "dugks_last_error", "dugks_global_error",
     "dugks_get_info", "dugks_set_dt", "dugks_get_dt", "dugks_set_stream", "dugks_step", "dugks_synchronize",
-    "dugks_get_conum", "dugks_get_macros", "dugks_get_face_macros", "dugks_get_wall", "dugks_get_residual",
+    "dugks_get_conum", "dugks_get_macros", "dugks_get_face_macros", "dugks_get_wall", "dugks_get_boundary", "dugks_get_residual",
     "dugks_get_dist", "dugks_set_dist", "dugks_checkpoint_size", "dugks_checkpoint_save",
     "dugks_checkpoint_load", "dugks_profile_step", "dugks_launches_per_step", "dugks_macros_noalloc",
     "dugks_inspect_case_dir", "dugks_write_time",
@@ -54,7 +57,7 @@ class CaseDesc(C.Structure):
         ("n_cells", C.c_int32), ("n_faces", C.c_int32), ("n_internal_faces", C.c_int32),
         ("face_offsets", _ip), ("face_verts", _ip), ("owner", _ip), ("neighbour", _ip),
         ("n_patches", C.c_int32), ("patch_start", _ip), ("patch_size", _ip), ("patch_kind", _ip),
-        ("wall_U", _dp), ("wall_T", _dp),
+        ("wall_U", _dp), ("wall_T", _dp), ("bnd_rho", _dp), ("patch_pressure", _dp),
         ("n_xi_per_dim", C.c_int32), ("xis", _dp), ("weights", _dp), ("xi_max", C.c_double),
         ("R", C.c_double), ("omega", C.c_double), ("Tref", C.c_double), ("muRef", C.c_double),
         ("Pr", C.c_double), ("KInner", C.c_int32),
@@ -125,6 +128,7 @@ def load_library(path: str | None = None):
     lib.dugks_get_macros.argtypes = [vp] + [_dp] * 5
     lib.dugks_get_face_macros.argtypes = [vp] + [_dp] * 5
     lib.dugks_get_wall.argtypes = [vp, C.c_int32, _dp, _dp, _dp]
+    lib.dugks_get_boundary.argtypes = [vp, C.c_int32, _dp, _dp, _dp]
     lib.dugks_get_residual.argtypes = [vp, _dp]
     lib.dugks_get_dist.argtypes = [vp, _dp, _dp]
     lib.dugks_set_dist.argtypes = [vp, _dp, _dp]
@@ -171,11 +175,15 @@ def _i(a):
     return a.ctypes.data_as(_ip)
 
 
+def patch_bc(p):
+    """rho boundary-condition type of a case patch: its "bc" entry, else from the mesh patch type."""
+    if "bc" in p:
+        return p["bc"]
+    return {"empty": "empty", "wall": "calculatedMaxwell", "symmetryPlane": "symmetryPlane"}[p["type"]]
+
+
 def _kinds(mesh):
-    out = []
-    for p in mesh["patches"]:
-        out.append(PATCH_EMPTY if p["type"] == "empty" else PATCH_MAXWELL)
-    return np.array(out, np.int32)
+    return np.array([BC_KINDS[patch_bc(p)] for p in mesh["patches"]], np.int32)
 
 
 def case_desc(case, precision=FP64, pipeline=PIPE_AUTO, device=0):
@@ -193,6 +201,8 @@ def case_desc(case, precision=FP64, pipeline=PIPE_AUTO, device=0):
         pk=_kinds(m),
         Ub=np.ascontiguousarray(case["Ub"], np.float64),
         Tb=np.ascontiguousarray(case["Tb"], np.float64),
+        rhob=np.ascontiguousarray(case.get("rhob", np.zeros(len(case["Tb"]))), np.float64),
+        pp=np.ascontiguousarray([p.get("pressure", 0.0) for p in m["patches"]], np.float64),
         xis=np.ascontiguousarray(case["xis"], np.float64),
         w=np.ascontiguousarray(case["weights"], np.float64),
         rho0=np.ascontiguousarray(case["rho0"], np.float64),
@@ -205,6 +215,7 @@ def case_desc(case, precision=FP64, pipeline=PIPE_AUTO, device=0):
         face_verts=_i(keep["fv"]), owner=_i(keep["own"]), neighbour=_i(keep["nei"]),
         n_patches=len(keep["ps"]), patch_start=_i(keep["ps"]), patch_size=_i(keep["pn"]),
         patch_kind=_i(keep["pk"]), wall_U=_d(keep["Ub"]), wall_T=_d(keep["Tb"]),
+        bnd_rho=_d(keep["rhob"]), patch_pressure=_d(keep["pp"]),
         n_xi_per_dim=len(keep["xis"]), xis=_d(keep["xis"]), weights=_d(keep["w"]),
         xi_max=float(case["xi_max"]), R=g["R"], omega=g["omega"], Tref=g["Tref"], muRef=g["muRef"],
         Pr=g["Pr"], KInner=int(g["KInner"]), rho0=_d(keep["rho0"]), U0=_d(keep["U0"]), T0=_d(keep["T0"]),
@@ -328,6 +339,12 @@ class FvDVM:
         out = dict(rhoW=np.empty(n_faces), qWall=np.empty((n_faces, 3)), stressWall=np.empty((n_faces, 9)))
         self._check(self._lib.dugks_get_wall(self._h, int(patch), _d(out["rhoW"]), _d(out["qWall"]),
                                              _d(out["stressWall"])))
+        return out
+
+    def boundary(self, patch, n_faces):
+        """rho, U, T patch values of one non-empty patch (rho_w on walls)."""
+        out = dict(rho=np.empty(n_faces), U=np.empty((n_faces, 3)), T=np.empty(n_faces))
+        self._check(self._lib.dugks_get_boundary(self._h, int(patch), _d(out["rho"]), _d(out["U"]), _d(out["T"])))
         return out
 
     def residual(self):

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define DUGKS_ABI_VERSION 1
+#define DUGKS_ABI_VERSION 2
 
 typedef struct dugks_handle dugks_handle;
 
@@ -48,10 +48,25 @@ enum dugks_precision {
 };
 
 /* Patch kinds: the rho boundary-condition type of 0/rho
- * (discreteVelocity.C:274-281 maps it to the g/h surface patch type). */
+ * (discreteVelocity::setBCtype, discreteVelocity.C:250-300, maps it to the
+ * g/h surface patch type given in brackets).  Kinds 2..8 run on the plain FP64
+ * pipeline (DUGKS_FP64 with DUGKS_PIPE_REFERENCE or AUTO); the FP32 pipeline
+ * and the gradient harness take diffuse walls and empty patches only. */
 enum dugks_patch_kind {
-    DUGKS_PATCH_EMPTY = 0,      /* "empty" (2D front/back)                        */
-    DUGKS_PATCH_MAXWELL = 1     /* "calculatedMaxwell" diffuse wall (maxwellWall) */
+    DUGKS_PATCH_EMPTY = 0,          /* "empty" (2D front/back)                            */
+    DUGKS_PATCH_MAXWELL = 1,        /* "calculatedMaxwell" [maxwellWall] diffuse wall     */
+    DUGKS_PATCH_ZERO_GRADIENT = 2,  /* "zeroGradient" [zeroGradient]: face = owner cell   */
+    DUGKS_PATCH_FIXED_VALUE = 3,    /* "fixedValue" [mixed]: incoming DFs stay at the
+                                       Maxwellian of the initial patch rho, U, T          */
+    DUGKS_PATCH_FAR_FIELD = 4,      /* "farField" [farField]: incoming DFs
+                                       rho_b M(U of the owner cell, T_b)                  */
+    DUGKS_PATCH_PRESSURE_IN = 5,    /* "pressureIn" [farField]; rho_b = p/(R T_b) after
+                                       each step (fvDVM::updatePressureInOutBC)           */
+    DUGKS_PATCH_PRESSURE_OUT = 6,   /* "pressureOut" [farField]; rho_b, T_b from p and
+                                       the owner cell after each step                     */
+    DUGKS_PATCH_SYMMETRY_MOD = 7,   /* "symmetryMod" [DVMsymmetry]: incoming DFs mirror
+                                       the outgoing ones                                  */
+    DUGKS_PATCH_SYMMETRY_PLANE = 8  /* constraint "symmetryPlane": mirrored incoming DFs  */
 };
 
 /* Kernel pipeline selection (both produce the same step). */
@@ -78,8 +93,12 @@ typedef struct dugks_case_desc {
     const int32_t* patch_start;      /* [n_patches] global face index        */
     const int32_t* patch_size;
     const int32_t* patch_kind;       /* dugks_patch_kind                     */
-    const double* wall_U;            /* [n_faces-n_internal_faces][3]        */
-    const double* wall_T;            /* [n_faces-n_internal_faces]           */
+    const double* wall_U;            /* [n_faces-n_internal_faces][3] U patch values */
+    const double* wall_T;            /* [n_faces-n_internal_faces]    T patch values */
+    const double* bnd_rho;           /* [n_faces-n_internal_faces] rho patch values
+                                        (fixedValue, farField); NULL if unused       */
+    const double* patch_pressure;    /* [n_patches] pressureIn / pressureOut values;
+                                        NULL if unused                               */
     int32_t n_xi_per_dim;            /* fvDVMparas.nDV                       */
     const double* xis;               /* [n_xi_per_dim] constant/Xis          */
     const double* weights;           /* [n_xi_per_dim] constant/weights      */
@@ -149,6 +168,13 @@ int dugks_get_face_macros(dugks_handle* h, double* rho, double* U, double* T, do
  * density rho_w (calculatedMaxwellFvPatchField value), qWall[3] and
  * stressWall[9] per face (fvDVM.C:539-581).  Any pointer may be NULL. */
 int dugks_get_wall(dugks_handle* h, int32_t patch, double* rho_w, double* q_wall, double* stress_wall);
+
+/* Patch values of the volume fields rhoVol(), Uvol(), Tvol() on one non-empty
+ * patch (fvDVMI.H:26-60 boundaryField()): rho is the Maxwell-wall density on
+ * walls and the rho patch value elsewhere (pressureIn / pressureOut patches
+ * change rho, U and T after each step, fvDVM.C:730-806).  rho[n], U[n][3],
+ * T[n] for the patch's n faces; any pointer may be NULL. */
+int dugks_get_boundary(dugks_handle* h, int32_t patch, double* rho, double* U, double* T);
 
 /* Steady-state residuals of dugksFoam.C:88-107: sum|U-Uold|/sum|U|,
  * sum|T-Told|/sum T, sum|rho-rhoOld|/sum rho against the fields saved by the

@@ -48,7 +48,7 @@
 static const double O_PI = 3.14159265358979323846;
 
 typedef struct oracle_t {
-    int nC, nF, nI, nB, nV, D, K;
+    int nC, nF, nI, nB, nV, D, K, M;
     int* owner;        /* [nF] */
     int* neighbour;    /* [nI] */
     int* bKind;        /* [nB] */
@@ -63,7 +63,9 @@ typedef struct oracle_t {
     int *cellOff, *cellFaces; /* active faces per cell, increasing face id */
     double *xi, *w;    /* [nV][3], [nV] */
     double xiMax, R, omega, Tref, muRef, Pr;
-    double *Ub, *Tb;   /* [nB][3], [nB] */
+    double *Ub, *Tb;   /* [nB][3], [nB]  U, T patch values */
+    double *rhob, *pB; /* [nB] rho patch values; pressureIn/Out pressure of the face's patch */
+    double* bS0;       /* [nB][3] Sf of the first face of the face's patch (symmetry patches) */
     double *inByRho, *outGoing, *rhoW; /* [nB] */
     double *qWall, *stressWall;        /* [nB][3], [nB][9] */
     double *rho, *U, *T, *q, *tau;     /* cells */
@@ -184,6 +186,41 @@ static inline void shakhov(const oracle_t* o, double rho, const double* U, doubl
 static inline double maxwell_by_rho(const oracle_t* o, const double* U, double T, const double* xi) {
     double umx[3] = {U[0] - xi[0], U[1] - xi[1], U[2] - xi[2]};
     return 1.0 / pow(sqrt(2.0 * O_PI * o->R * T), (double)o->D) * exp(-magsqr3(umx) / (2.0 * o->R * T));
+}
+
+/* discreteVelocity::equilibriumMaxwell for patch fields, discreteVelocity.C:1046-1061 */
+static inline void maxwell_patch(const oracle_t* o, double rho, const double* U, double T, const double* xi,
+                                 double* geq, double* heq) {
+    double umx[3] = {U[0] - xi[0], U[1] - xi[1], U[2] - xi[2]};
+    *geq = rho / pow(sqrt(2.0 * O_PI * o->R * T), (double)o->D) * exp(-magsqr3(umx) / (2.0 * o->R * T));
+    *heq = (o->K + 3 - o->D) * o->R * T * *geq;
+}
+
+/* DV mirrored across a symmetry patch: fvDVM::initialiseDV builds the x, y, z
+   mirror ids (fvDVM.C:140-221); the patch picks
+   round(|n . (symX, symY, symZ)|) with n its first face's unit normal
+   (discreteVelocity.C:733-817). */
+static int sym_target(const oracle_t* o, int v, const double* S0) {
+    const int M = o->M, D = o->D;
+    int ix, iy = 0, iz = 0;
+    if (D == 3) { ix = v % M; iy = (v / M) % M; iz = v / (M * M); }
+    else if (D == 2) { ix = v % M; iy = v / M; }
+    else ix = v;
+    double sx, sy, sz;
+    if (D == 3) {
+        sx = iz * M * M + iy * M + (M - ix - 1);
+        sy = iz * M * M + (M - iy - 1) * M + ix;
+        sz = (M - iz - 1) * M * M + iy * M + ix;
+    } else if (D == 2) {
+        sx = iy * M + (M - ix - 1);
+        sy = (M - iy - 1) * M + ix;
+        sz = 0;
+    } else {
+        sx = M - ix - 1; sy = 0; sz = 0;
+    }
+    const double m = sqrt(magsqr3(S0));
+    const double n[3] = {S0[0] / m, S0[1] / m, S0[2] / m};
+    return (int)round(fabs(n[0] * sx + n[1] * sy + n[2] * sz));
 }
 
 /* fvDVM::updateTau, fvDVM.C:808-817 */
@@ -383,6 +420,7 @@ void* oracle_create(const oracle_case* c) {
     const int M = c->nXiPerDim;
     int nV = (D == 3) ? M * M * M : (D == 2 ? M * M : M);
     o->nV = nV;
+    o->M = M;
     o->xi = (double*)xcalloc(3 * (size_t)nV, sizeof(double));
     o->w = (double*)xcalloc(nV, sizeof(double));
     {
@@ -413,6 +451,21 @@ void* oracle_create(const oracle_case* c) {
     o->Tb = (double*)xcalloc(nB, sizeof(double));
     memcpy(o->Ub, c->Ub, sizeof(double) * 3 * nB);
     memcpy(o->Tb, c->Tb, sizeof(double) * nB);
+    o->rhob = (double*)xcalloc(nB, sizeof(double));
+    o->pB = (double*)xcalloc(nB, sizeof(double));
+    o->bS0 = (double*)xcalloc(3 * (size_t)nB, sizeof(double));
+    if (c->rhob) memcpy(o->rhob, c->rhob, sizeof(double) * nB);
+    for (int p = 0; p < c->nPatches; ++p) {
+        const int k = c->patchKind[p];
+        for (int i = 0; i < c->patchSize[p]; ++i) {
+            const int b = c->patchStart[p] + i - nI;
+            /* pressureIn/Out ctor: value = 1 until the first updatePressureInOutBC
+               (pressureInFvPatchField.C:62-76, pressureOutFvPatchField.C:62-76) */
+            if (k == ORACLE_PATCH_PRESSURE_IN || k == ORACLE_PATCH_PRESSURE_OUT) o->rhob[b] = 1.0;
+            if (c->patchPressure) o->pB[b] = c->patchPressure[p];
+            for (int d = 0; d < 3; ++d) o->bS0[3 * b + d] = o->Sf[3 * (size_t)c->patchStart[p] + d];
+        }
+    }
     o->inByRho = (double*)xcalloc(nB, sizeof(double));
     o->outGoing = (double*)xcalloc(nB, sizeof(double));
     o->rhoW = (double*)xcalloc(nB, sizeof(double));
@@ -453,6 +506,17 @@ void* oracle_create(const oracle_case* c) {
             shakhov(o, o->rho[i], o->U + 3 * i, o->T[i], q0, o->xi + 3 * v,
                     o->gT + (size_t)v * nC + i, o->hT + (size_t)v * nC + i);
 
+    /* discreteVelocity::initBoundaryField (discreteVelocity.C:302-345): the
+       mixed patches (rho fixedValue) start at the Maxwellian of the patch values;
+       their incoming DFs are never written again. */
+    for (int b = 0; b < nB; ++b) {
+        if (o->bKind[b] != ORACLE_PATCH_FIXED_VALUE) continue;
+        const int f = nI + b;
+        for (int v = 0; v < nV; ++v)
+            maxwell_patch(o, o->rhob[b], o->Ub + 3 * b, o->Tb[b], o->xi + 3 * v, o->gS + (size_t)v * nF + f,
+                          o->hS + (size_t)v * nF + f);
+    }
+
     /* fvDVM::setCalculatedMaxwellRhoBC, fvDVM.C:263-309 (computed once) */
     for (int b = 0; b < nB; ++b) {
         if (o->bKind[b] != ORACLE_PATCH_MAXWELL) continue;
@@ -488,6 +552,7 @@ void oracle_destroy(void* h) {
     void* ptrs[] = {o->owner, o->neighbour, o->bKind, o->bCell, o->C, o->V, o->Cf, o->Sf, o->pVec, o->nVec,
                     o->bVec, o->dcI, o->dcB, o->nHatB, o->cellOff, o->cellFaces, o->xi, o->w, o->Ub, o->Tb,
                     o->inByRho, o->outGoing, o->rhoW, o->qWall, o->stressWall, o->rho, o->U, o->T, o->q,
+                    o->rhob, o->pB, o->bS0,
                     o->tau, o->rhoF, o->UF, o->TF, o->qF, o->tauF, o->gT, o->hT, o->gB, o->hB, o->Gg, o->Gh,
                     o->gS, o->hS};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
@@ -537,8 +602,15 @@ static void dv_bar_and_surf(oracle_t* o, int v, double* grad /* [nC][3] */, doub
                 }
             } else {
                 int b = f - nI;
-                double gbv = gB[i] + Gg[b] / o->dcB[b];  /* fixedGradient evaluate */
-                double hbv = hB[i] + Gh[b] / o->dcB[b];
+                double gbv, hbv;
+                if (o->bKind[b] == ORACLE_PATCH_SYMMETRY_PLANE) {
+                    /* constraint patch of gBarPvol: scalar symmetryPlane value = internal value */
+                    gbv = gB[i];
+                    hbv = hB[i];
+                } else {
+                    gbv = gB[i] + Gg[b] / o->dcB[b];  /* fixedGradient evaluate */
+                    hbv = hB[i] + Gh[b] / o->dcB[b];
+                }
                 double dg = gbv - gB[i], dh = hbv - hB[i];
                 for (int k = 0; k < 3; ++k) { gg[k] += o->bVec[3 * b + k] * dg; hg[k] += o->bVec[3 * b + k] * dh; }
             }
@@ -572,15 +644,33 @@ static void dv_bar_and_surf(oracle_t* o, int v, double* grad /* [nC][3] */, doub
             hS[f] = 0.5 * (hB[ne] + dot3(grh + 3 * ne, rN) + hB[ow] + dot3(grh + 3 * ow, rO));
         }
     }
-    /* P3: maxwellWall outgoing faces (xi.S > 0) */
+    /* P3: boundary faces by surface patch type (discreteVelocity.C:530-689) */
     for (int b = 0; b < nB; ++b) {
-        if (o->bKind[b] != ORACLE_PATCH_MAXWELL) continue;
+        const int kind = o->bKind[b];
+        if (kind == ORACLE_PATCH_EMPTY) continue;
         int f = nI + b, P = o->bCell[b];
-        if (dot3(xi, o->Sf + 3 * f) > 0) {
+        const double xs = dot3(xi, o->Sf + 3 * f);
+        int outgoing;
+        if (kind == ORACLE_PATCH_ZERO_GRADIENT) {
+            /* gSurf == gBarPvol patchInternalField, every DV */
+            gS[f] = gB[P];
+            hS[f] = hB[P];
+            continue;
+        } else if (kind == ORACLE_PATCH_SYMMETRY_MOD || kind == ORACLE_PATCH_SYMMETRY_PLANE) {
+            outgoing = xs > -O_VSMALL;  /* outgoing and tangential */
+        } else {
+            outgoing = xs > 0;
+        }
+        if (outgoing) {
             double r[3];
             for (int k = 0; k < 3; ++k) r[k] = o->Cf[3 * f + k] - o->C[3 * P + k] - 0.5 * xi[k] * dt;
             gS[f] = gB[P] + dot3(grad + 3 * P, r);
             hS[f] = hB[P] + dot3(grh + 3 * P, r);
+        } else if (kind == ORACLE_PATCH_FAR_FIELD || kind == ORACLE_PATCH_PRESSURE_IN ||
+                   kind == ORACLE_PATCH_PRESSURE_OUT) {
+            /* incoming: rho_b M(U of the owner cell, T_b) */
+            gS[f] = o->rhob[b] * maxwell_by_rho(o, o->U + 3 * P, o->Tb[b], xi);
+            hS[f] = gS[f] * (o->R * o->Tb[b]) * (o->K + 3 - o->D);
         }
     }
 }
@@ -620,15 +710,23 @@ static void dv_surf_and_tilde(oracle_t* o, int v) {
         gS[f] = (1.0 - b) * gS[f] + b * ge;
         hS[f] = (1.0 - b) * hS[f] + b * he;
     }
-    /* maxwellWall patch: field assignment is a no-op (maxwellWallFvsPatchField.H:163-181);
-       only outgoing DVs are relaxed explicitly. */
+    /* Boundary patches.  The field assignment is a no-op on the project's own
+       surface patch types (maxwellWall, mixed, farField, zeroGradient,
+       DVMsymmetry: e.g. maxwellWallFvsPatchField.H:163-181) and a plain
+       assignment on the constraint type symmetryPlane; then every outgoing DV
+       (xi.S > 0) is relaxed explicitly (discreteVelocity.C:887-931), so
+       symmetryPlane relaxes its outgoing DVs twice. */
     for (int bb = 0; bb < nB; ++bb) {
-        if (o->bKind[bb] != ORACLE_PATCH_MAXWELL) continue;
+        const int kind = o->bKind[bb];
+        if (kind == ORACLE_PATCH_EMPTY) continue;
         int f = nI + bb;
-        if (dot3(xi, o->Sf + 3 * f) > 0) {
-            double b = hh / (2 * o->tauF[f] + hh);
-            double ge, he;
-            shakhov(o, o->rhoF[f], o->UF + 3 * f, o->TF[f], o->qF + 3 * f, xi, &ge, &he);
+        const int out = dot3(xi, o->Sf + 3 * f) > 0;
+        const int times = (kind == ORACLE_PATCH_SYMMETRY_PLANE) + out;
+        if (times == 0) continue;
+        double b = hh / (2 * o->tauF[f] + hh);
+        double ge, he;
+        shakhov(o, o->rhoF[f], o->UF + 3 * f, o->TF[f], o->qF + 3 * f, xi, &ge, &he);
+        for (int t = 0; t < times; ++t) {
             gS[f] = (1.0 - b) * gS[f] + b * ge;
             hS[f] = (1.0 - b) * hS[f] + b * he;
         }
@@ -792,6 +890,69 @@ static void cell_macros(oracle_t* o) {
     }
 }
 
+/* fvDVM::updateGHbarSurfSymmetryIn (fvDVM.C:375-454, discreteVelocity.C:733-817):
+   incoming DVs (xi.S0 <= 0, S0 the patch's first face) of a symmetry patch
+   take the face value of their mirror DV.  DVMsymmetry copies from a snapshot
+   of all DVs taken before the pass; symmetryPlane copies DV by DV in DV order. */
+static void symmetry_in(oracle_t* o) {
+    const int nI = o->nI, nB = o->nB, nF = o->nF, nV = o->nV;
+#pragma omp parallel
+    {
+        double* snap = (double*)malloc(sizeof(double) * 2 * (size_t)nV);
+#pragma omp for schedule(dynamic, 4)
+        for (int b = 0; b < nB; ++b) {
+            const int kind = o->bKind[b];
+            if (kind != ORACLE_PATCH_SYMMETRY_MOD && kind != ORACLE_PATCH_SYMMETRY_PLANE) continue;
+            const int f = nI + b;
+            const double* S0 = o->bS0 + 3 * b;
+            for (int v = 0; v < nV; ++v) {
+                snap[v] = o->gS[(size_t)v * nF + f];
+                snap[nV + v] = o->hS[(size_t)v * nF + f];
+            }
+            for (int v = 0; v < nV; ++v) {
+                if (!(dot3(o->xi + 3 * v, S0) <= 0)) continue;
+                const int t = sym_target(o, v, S0);
+                if (kind == ORACLE_PATCH_SYMMETRY_MOD) {
+                    o->gS[(size_t)v * nF + f] = snap[t];
+                    o->hS[(size_t)v * nF + f] = snap[nV + t];
+                } else {
+                    o->gS[(size_t)v * nF + f] = o->gS[(size_t)t * nF + f];
+                    o->hS[(size_t)v * nF + f] = o->hS[(size_t)t * nF + f];
+                }
+            }
+        }
+        free(snap);
+    }
+}
+
+/* fvDVM::updatePressureInOutBC (fvDVM.C:730-806), after the cell macros. */
+static void pressure_bc(oracle_t* o) {
+    const int nI = o->nI, nB = o->nB;
+    const double R = o->R;
+    for (int b = 0; b < nB; ++b) {
+        const int kind = o->bKind[b];
+        if (kind != ORACLE_PATCH_PRESSURE_IN && kind != ORACLE_PATCH_PRESSURE_OUT) continue;
+        const int f = nI + b, P = o->bCell[b];
+        const double* Sf = o->Sf + 3 * f;
+        const double magSf = sqrt(magsqr3(Sf));
+        const double n[3] = {Sf[0] / magSf, Sf[1] / magSf, Sf[2] / magSf};
+        const double* Ui = o->U + 3 * P;
+        const double Ti = o->T[P], rhoi = o->rho[P];
+        const double ai = sqrt(R * Ti * (o->K + 5) / (o->K + 3));
+        const double Un = dot3(Ui, n);
+        double UnIn;
+        if (kind == ORACLE_PATCH_PRESSURE_IN) {
+            o->rhob[b] = o->pB[b] / R / o->Tb[b];
+            UnIn = Un + (o->pB[b] - rhoi * R * Ti) / rhoi / ai;
+        } else {
+            o->rhob[b] = rhoi + (o->pB[b] - rhoi * R * Ti) / ai / ai;
+            o->Tb[b] = o->pB[b] / (R * rhoi);
+            UnIn = Un + (rhoi * R * Ti - o->pB[b]) / rhoi / ai;
+        }
+        for (int k = 0; k < 3; ++k) o->Ub[3 * b + k] = UnIn * n[k] + (Ui[k] - Un * n[k]);
+    }
+}
+
 /* fvDVM::evolution, fvDVM.C:1086-1108 */
 static void evolution(oracle_t* o) {
     const int nV = o->nV, nC = o->nC, nB = o->nB, nI = o->nI, nF = o->nF;
@@ -822,10 +983,12 @@ static void evolution(oracle_t* o) {
     }
 #pragma omp parallel for schedule(dynamic, 4)
     for (int v = 0; v < nV; ++v) dv_wall_in(o, v);
+    symmetry_in(o);
     face_macros(o);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int v = 0; v < nV; ++v) dv_surf_and_tilde(o, v);
     cell_macros(o);
+    pressure_bc(o);
 }
 
 void oracle_step(void* h, double dt, int nsteps) {
@@ -860,6 +1023,14 @@ void oracle_get_wall(void* h, double* rhoW, double* qWall, double* stressWall) {
     if (rhoW) memcpy(rhoW, o->rhoW, sizeof(double) * n);
     if (qWall) memcpy(qWall, o->qWall, sizeof(double) * 3 * n);
     if (stressWall) memcpy(stressWall, o->stressWall, sizeof(double) * 9 * n);
+}
+
+void oracle_get_boundary(void* h, double* rhob, double* Ub, double* Tb) {
+    oracle_t* o = (oracle_t*)h;
+    int n = o->nB;
+    if (rhob) memcpy(rhob, o->rhob, sizeof(double) * n);
+    if (Ub) memcpy(Ub, o->Ub, sizeof(double) * 3 * n);
+    if (Tb) memcpy(Tb, o->Tb, sizeof(double) * n);
 }
 
 void oracle_get_dist(void* h, double* g, double* hh) {

@@ -20,10 +20,19 @@
 extern "C" {
 #endif
 
-/* Patch kinds understood by the oracle (rho boundary-condition types). */
+/* Patch kinds understood by the oracle: the rho boundary-condition type,
+   which discreteVelocity::setBCtype (discreteVelocity.C:250-300) maps to the
+   g/h surface patch type given in brackets. */
 enum {
-    ORACLE_PATCH_EMPTY = 0,              /* OpenFOAM "empty" (2D front/back) */
-    ORACLE_PATCH_MAXWELL = 1             /* rho "calculatedMaxwell" diffuse wall */
+    ORACLE_PATCH_EMPTY = 0,              /* "empty" (2D front/back) */
+    ORACLE_PATCH_MAXWELL = 1,            /* "calculatedMaxwell" [maxwellWall] diffuse wall */
+    ORACLE_PATCH_ZERO_GRADIENT = 2,      /* "zeroGradient" [zeroGradient] */
+    ORACLE_PATCH_FIXED_VALUE = 3,        /* "fixedValue" [mixed]: incoming DFs frozen at the initial Maxwellian */
+    ORACLE_PATCH_FAR_FIELD = 4,          /* "farField" [farField]: incoming DFs rho_b M(U_owner, T_b) */
+    ORACLE_PATCH_PRESSURE_IN = 5,        /* "pressureIn" [farField] + fvDVM::updatePressureInOutBC */
+    ORACLE_PATCH_PRESSURE_OUT = 6,       /* "pressureOut" [farField] + fvDVM::updatePressureInOutBC */
+    ORACLE_PATCH_SYMMETRY_MOD = 7,       /* "symmetryMod" [DVMsymmetry]: mirrored DFs */
+    ORACLE_PATCH_SYMMETRY_PLANE = 8      /* constraint "symmetryPlane": mirrored DFs */
 };
 
 typedef struct oracle_case {
@@ -38,8 +47,10 @@ typedef struct oracle_case {
     const int* patchStart;               /* [nPatches] global face index */
     const int* patchSize;
     const int* patchKind;                /* ORACLE_PATCH_* */
-    const double* Ub;                    /* [nFaces-nInternalFaces][3] wall U */
-    const double* Tb;                    /* [nFaces-nInternalFaces]    wall T */
+    const double* Ub;                    /* [nFaces-nInternalFaces][3] U patch values */
+    const double* Tb;                    /* [nFaces-nInternalFaces]    T patch values */
+    const double* rhob;                  /* [nFaces-nInternalFaces]    rho patch values (may be NULL) */
+    const double* patchPressure;         /* [nPatches] pressureIn / pressureOut (may be NULL) */
     int nXiPerDim;
     const double* xis;                   /* [nXiPerDim] 1-D nodes  (constant/Xis) */
     const double* weights;               /* [nXiPerDim] 1-D weights (constant/weights) */
@@ -63,6 +74,8 @@ void  oracle_get_cell(void* h, double* rho, double* U, double* T, double* q, dou
 void  oracle_get_face(void* h, double* rho, double* U, double* T, double* q, double* tau);
 /* Per boundary face: rho boundary value (Maxwell-wall density), qWall, stressWall[9]. */
 void  oracle_get_wall(void* h, double* rhoW, double* qWall, double* stressWall);
+/* Per boundary face: rho, U, T patch values (farField / pressure patches change them). */
+void  oracle_get_boundary(void* h, double* rhob, double* Ub, double* Tb);
 /* g~, h~ in DV-outer layout [nDV][nCells]. */
 void  oracle_get_dist(void* h, double* g, double* hh);
 void  oracle_set_dist(void* h, const double* g, const double* hh);

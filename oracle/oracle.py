@@ -24,6 +24,10 @@ LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 PATCH_EMPTY = 0
 PATCH_MAXWELL = 1
+# rho boundary-condition type -> patch kind (dugks_oracle.h; the same numbering
+# as the engine's dugks_patch_kind)
+BC_KINDS = {"empty": 0, "calculatedMaxwell": 1, "zeroGradient": 2, "fixedValue": 3, "farField": 4,
+            "pressureIn": 5, "pressureOut": 6, "symmetryMod": 7, "symmetryPlane": 8}
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
@@ -35,7 +39,7 @@ class _Case(C.Structure):
         ("nCells", C.c_int), ("nFaces", C.c_int), ("nInternalFaces", C.c_int),
         ("faceOffsets", _ip), ("faceVerts", _ip), ("owner", _ip), ("neighbour", _ip),
         ("nPatches", C.c_int), ("patchStart", _ip), ("patchSize", _ip), ("patchKind", _ip),
-        ("Ub", _dp), ("Tb", _dp),
+        ("Ub", _dp), ("Tb", _dp), ("rhob", _dp), ("patchPressure", _dp),
         ("nXiPerDim", C.c_int), ("xis", _dp), ("weights", _dp), ("xiMax", C.c_double),
         ("R", C.c_double), ("omega", C.c_double), ("Tref", C.c_double), ("muRef", C.c_double),
         ("Pr", C.c_double), ("KInner", C.c_int),
@@ -68,6 +72,7 @@ def _load():
         for name in ("oracle_get_cell", "oracle_get_face"):
             getattr(lib, name).argtypes = [C.c_void_p] + [_dp] * 5
         lib.oracle_get_wall.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        lib.oracle_get_boundary.argtypes = [C.c_void_p, _dp, _dp, _dp]
         lib.oracle_get_dist.argtypes = [C.c_void_p, _dp, _dp]
         lib.oracle_set_dist.argtypes = [C.c_void_p, _dp, _dp]
         lib.oracle_get_geometry.argtypes = [C.c_void_p] + [_dp] * 8
@@ -85,16 +90,15 @@ def _i(a):
     return a.ctypes.data_as(_ip)
 
 
+def patch_bc(p):
+    """rho boundary-condition type of a case patch (explicit "bc", else from the mesh type)."""
+    if "bc" in p:
+        return p["bc"]
+    return {"empty": "empty", "wall": "calculatedMaxwell", "symmetryPlane": "symmetryPlane"}[p["type"]]
+
+
 def patch_kinds(mesh):
-    kinds = []
-    for p in mesh["patches"]:
-        if p["type"] == "empty":
-            kinds.append(PATCH_EMPTY)
-        elif p["type"] == "wall":
-            kinds.append(PATCH_MAXWELL)
-        else:
-            raise ValueError("oracle supports empty and calculatedMaxwell wall patches only")
-    return np.array(kinds, np.int32)
+    return np.array([BC_KINDS[patch_bc(p)] for p in mesh["patches"]], np.int32)
 
 
 class Oracle:
@@ -117,6 +121,8 @@ class Oracle:
             pk=patch_kinds(m),
             Ub=np.ascontiguousarray(case["Ub"], np.float64),
             Tb=np.ascontiguousarray(case["Tb"], np.float64),
+            rhob=np.ascontiguousarray(case.get("rhob", np.zeros(len(case["Tb"]))), np.float64),
+            pp=np.ascontiguousarray([p.get("pressure", 0.0) for p in m["patches"]], np.float64),
             xis=np.ascontiguousarray(case["xis"], np.float64),
             w=np.ascontiguousarray(case["weights"], np.float64),
             rho0=np.ascontiguousarray(case["rho0"], np.float64),
@@ -129,6 +135,7 @@ class Oracle:
             faceOffsets=_i(keep["off"]), faceVerts=_i(keep["fv"]), owner=_i(keep["own"]),
             neighbour=_i(keep["nei"]), nPatches=len(keep["ps"]), patchStart=_i(keep["ps"]),
             patchSize=_i(keep["pn"]), patchKind=_i(keep["pk"]), Ub=_d(keep["Ub"]), Tb=_d(keep["Tb"]),
+            rhob=_d(keep["rhob"]), patchPressure=_d(keep["pp"]),
             nXiPerDim=len(keep["xis"]), xis=_d(keep["xis"]), weights=_d(keep["w"]),
             xiMax=float(case["xi_max"]), R=g["R"], omega=g["omega"], Tref=g["Tref"],
             muRef=g["muRef"], Pr=g["Pr"], KInner=int(g["KInner"]),
@@ -174,6 +181,12 @@ class Oracle:
         r, q, s = np.zeros(n), np.zeros((n, 3)), np.zeros((n, 9))
         self._lib.oracle_get_wall(self._h, _d(r), _d(q), _d(s))
         return dict(rhoW=r, qWall=q, stressWall=s)
+
+    def boundary(self):
+        n = self.nB
+        r, U, T = np.zeros(n), np.zeros((n, 3)), np.zeros(n)
+        self._lib.oracle_get_boundary(self._h, _d(r), _d(U), _d(T))
+        return dict(rho=r, U=U, T=T)
 
     def dist(self):
         g = np.zeros((self.nV, self.nC))

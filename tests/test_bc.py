@@ -1,0 +1,107 @@
+"""Boundary types other than diffuse walls on the CPU: the oracle's restatement
+of zeroGradient, mixed (rho fixedValue), farField, pressureIn / pressureOut
+(discreteVelocity.C:530-689, fvDVM.C:730-806) and the two symmetry types
+(discreteVelocity.C:733-817), the case writer and reader for them, and the
+reference's own symmetry demo case read in place when the tree is present."""
+import os
+
+import numpy as np
+import pytest
+
+REF_SYM = "/root/reference/demo/testSymmetry/symmetry"
+
+
+def _cases():
+    from dugksfoam_gb300 import cases
+
+    return {
+        "channel": cases.channel2d(16, 8, nxi=8),
+        "open_box": cases.open_box2d(10, nxi=8),
+        "half_plane": cases.half_cavity2d(6, 12, nxi=8),
+        "half_mod": cases.half_cavity2d(6, 12, nxi=8, sym="symmetryMod"),
+    }
+
+
+@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod"])
+def test_oracle_runs_every_boundary_type(oracle_lib, name):
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import Oracle
+
+    case = _cases()[name]
+    o = Oracle(case)
+    o.step(cases.stable_dt(case), 40)
+    c = o.cell()
+    assert all(np.isfinite(c[k]).all() for k in ("rho", "U", "T", "q"))
+    assert c["rho"].min() > 0 and c["T"].min() > 0
+
+
+def test_pressure_patches_follow_the_characteristic_update(oracle_lib):
+    """After a step: inlet rho_b = p_in / (R T_in); outlet T_b = p_out / (R rho_owner)
+    and rho_b = rho_i + (p_out - rho_i R T_i) / a_i^2 with the owner's new macros."""
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import Oracle
+
+    case = _cases()["channel"]
+    o = Oracle(case)
+    o.step(cases.stable_dt(case), 30)
+    m = case["mesh"]
+    nI = len(m["neighbour"])
+    b, c = o.boundary(), o.cell()
+    R, K = case["gas"]["R"], case["gas"]["KInner"]
+    inlet, outlet = (next(p for p in m["patches"] if p["name"] == n) for n in ("inlet", "outlet"))
+    si = slice(inlet["startFace"] - nI, inlet["startFace"] - nI + inlet["nFaces"])
+    assert np.array_equal(b["rho"][si], inlet["pressure"] / R / b["T"][si])
+    so = slice(outlet["startFace"] - nI, outlet["startFace"] - nI + outlet["nFaces"])
+    own = np.asarray(m["owner"])[outlet["startFace"]:outlet["startFace"] + outlet["nFaces"]]
+    rho_i, T_i = c["rho"][own], c["T"][own]
+    a2 = R * T_i * (K + 5) / (K + 3)
+    np.testing.assert_allclose(b["T"][so], outlet["pressure"] / (R * rho_i), rtol=1e-15)
+    np.testing.assert_allclose(b["rho"][so], rho_i + (outlet["pressure"] - rho_i * R * T_i) / a2, rtol=1e-14)
+    # the pressure difference drives the gas from the inlet to the outlet
+    assert c["U"][:, 0].mean() > 0
+
+
+def test_mixed_patch_keeps_its_incoming_maxwellian(oracle_lib):
+    """rho fixedValue -> mixed surface patch: the face macros there stay close to
+    the patch's Maxwellian half (its incoming DFs are frozen), while a
+    zeroGradient face copies its owner cell."""
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import Oracle
+
+    case = _cases()["open_box"]
+    o = Oracle(case)
+    o.step(cases.stable_dt(case), 20)
+    f = o.face()
+    m = case["mesh"]
+    top = next(p for p in m["patches"] if p["name"] == "top")
+    sl = slice(top["startFace"], top["startFace"] + top["nFaces"])
+    # the top patch drives the gas in +x
+    assert f["U"][sl, 0].min() > 0
+
+
+def test_written_cases_read_back(built_lib, tmp_path):
+    from dugksfoam_gb300 import foamio, solver
+
+    for name, case in _cases().items():
+        d = tmp_path / name
+        foamio.write_case(case, d)
+        s = solver.inspect_case_dir(d)
+        m = case["mesh"]
+        assert s["n_cells"] == m["n_cells"] and s["n_patches"] == len(m["patches"])
+        walls = sum(p["nFaces"] for p in m["patches"] if solver.patch_bc(p) == "calculatedMaxwell")
+        empties = sum(p["nFaces"] for p in m["patches"] if p["type"] == "empty")
+        assert s["n_wall_faces"] == walls and s["n_empty_faces"] == empties
+        rho, prho = foamio.read_vol_field(d / "0" / "rho")
+        for p in m["patches"]:
+            assert prho[p["name"]][0] == solver.patch_bc(p)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_SYM), reason="reference demo case not present")
+def test_reference_symmetry_demo_case(built_lib):
+    """demo/testSymmetry/symmetry: the left half (30 x 60 quads) of the cavity
+    with a symmetryMod (DVMsymmetry) patch of 60 faces at x = 0.5."""
+    from dugksfoam_gb300 import solver
+
+    s = solver.inspect_case_dir(REF_SYM)
+    assert (s["n_cells"], s["n_wall_faces"], s["n_empty_faces"]) == (1800, 120, 3600)
+    assert s["n_patches"] == 4

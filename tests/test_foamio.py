@@ -69,7 +69,7 @@ def test_missing_field_and_unsupported_bc_are_errors(built_lib, tmp_path):
         solver.inspect_case_dir(tmp_path)
     assert e.value.code == 2  # DUGKS_ERR_IO
     foamio.write_case(_case(), tmp_path)
-    t = (tmp_path / "0" / "rho").read_text().replace("calculatedMaxwell", "farField", 1)
+    t = (tmp_path / "0" / "rho").read_text().replace("calculatedMaxwell", "totalPressure", 1)
     (tmp_path / "0" / "rho").write_text(t)
     with pytest.raises(solver.DugksError) as e:
         solver.inspect_case_dir(tmp_path)
