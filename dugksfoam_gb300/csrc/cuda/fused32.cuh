@@ -507,6 +507,45 @@ __device__ __forceinline__ void finalize_face32(const FusedArgs<float>& A, int a
         }
 }
 
+// Face values of an open boundary face (deviation form) once the owner side is
+// reconstructed: zeroGradient takes the owner's gbar+ for every velocity
+// (discreteVelocity.C:551-555); farField / pressureIn / pressureOut replace
+// the incoming velocities (xi.S <= 0) by rho_b M(U of the owner cell, T_b)
+// (:570-600) and fixedValue (mixed) by the Maxwellian of its patch rho, U, T,
+// which stays what it was at the start (:302-345).
+template <int D, bool H, int NPL>
+__device__ __forceinline__ void open_face_values(const FusedArgs<float>& A, int kind, int w, int a,
+                                                 const Lane32<D, NPL>& L, const float2 (&xs)[NPL / 2],
+                                                 const float* ownG, const float* ownH, float2 (&gf)[NPL / 2],
+                                                 float2 (&hf)[NPL / 2]) {
+    constexpr int NP = NPL / 2;
+    const StepArgs& b = A.b;
+    if (kind == kBcZeroGradient) {
+        ldp<NP>(gf, ownG);
+        if (H) ldp<NP>(hf, ownH);
+        return;
+    }
+    const double Tb = b.TbM[w], RT = b.R * Tb;
+    const double* U = kind == kBcFixedValue ? b.Uw + 3 * w : b.U + 3 * b.own[a];
+    const double s = sqrt(2.0 * kPi * RT);
+    const float ng = (float)(A.gscale * b.rhoB[w] / (D == 2 ? s * s : s * s * s));
+    const float i2 = (float)(-0.5 / RT), hw = (float)(RT * (b.K + 3 - D));
+    const float ux = (float)U[0], uy = (float)U[1], uz = (float)U[2];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float2 cx = sub2(L.x[p], f2(ux)), cy = sub2(L.y[p], f2(uy));
+        float2 cc = fma2(cy, cy, mul2(cx, cx));
+        if (D == 3) {
+            const float2 cz = sub2(L.z[p], f2(uz));
+            cc = fma2(cz, cz, cc);
+        }
+        const float2 m = make_float2(ng * expf(i2 * cc.x), ng * expf(i2 * cc.y));
+        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
+        gf[p] = sel2(o0, o1, gf[p], sub2(m, L.mr[p]));
+        if (H) hf[p] = sel2(o0, o1, hf[p], sub2(mul2(m, f2(hw)), mul2(L.mr[p], f2(A.hrefFac))));
+    }
+}
+
 // ---------------------------------------------------------------- sweep A, face sides
 // One-sided upwind reconstruction from cell u (local row lu, stencil entries
 // [e0,e1) of u, d = Cf - C_u): val = gbar+_u + sum_e L_e.(d - xi dt/2) (gbar+_e - gbar+_u).
@@ -694,7 +733,8 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
             const size_t fi = (size_t)F.r.a * Vp + v0 + col;
             const float dO[3] = {F.dOx, F.dOy, F.dOz}, dN[3] = {F.dNx, F.dNy, F.dNz};
             if (F.r.w >= 0) {
-                if (GR) {  // wall: owner side; gw = the owner's gradient (for grad . n)
+                const int kind = b.bKind[F.r.w];
+                if (GR) {  // boundary: owner side; gw = the owner's gradient (for grad . n)
                     side_value_g<D, H, NPL>(L, cg, chh, gbuf, F.r.ownL, dO, A.dt, col, gf, hf);
 #pragma unroll
                     for (int k = 0; k < D; ++k) {
@@ -718,11 +758,17 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
                     const float2 fx = mul2(mul2(mul2(L.w[p], xs[p]), gf[p]), use[p]);
                     fl += fx.x + fx.y;
                 }
-                m[SL::FLUX] = fl;
                 const size_t wi = (size_t)F.r.w * Vp + v0 + col;
                 stp<NP>(A.Gbgn + wi, gn);
                 if (H) stp<NP>(A.Gbhn + wi, hn);
-                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
+                if (kind == kBcMaxwell) {
+                    m[SL::FLUX] = fl;
+                    mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
+                } else {
+                    open_face_values<D, H, NPL>(A, kind, F.r.w, F.r.a, L, xs, cg + F.r.ownL * KC + col,
+                                                chh + F.r.ownL * KC + col, gf, hf);
+                    mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
+                }
                 stp<NP>(A.gF + fi, gf);
                 if (H) stp<NP>(A.hF + fi, hf);
             } else if (F.r.ownL < hd.nT && F.r.neiL < hd.nT) {  // both sides in T: complete
@@ -818,7 +864,8 @@ __device__ __forceinline__ void face_macros_one(const FusedArgs<float>& A, int a
     const double* src = A.faceMom + (size_t)a * 2 * NS;
     double M[NS];
     for (int s = 0; s < NS; ++s) M[s] = src[s] + src[NS + s];
-    finalize_face32<D, H>(A, a, a >= A.b.nI ? a - A.b.nI : -1, A.uref4[a], M);
+    const int w = a >= A.b.nI && A.b.bKind[a - A.b.nI] == kBcMaxwell ? a - A.b.nI : -1;
+    finalize_face32<D, H>(A, a, w, A.uref4[a], M);
 }
 
 template <int D, bool H>
@@ -965,7 +1012,16 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
                 xs[p] = fma2(L.y[p], f2(ent.y), mul2(L.x[p], f2(ent.x)));
                 if (D == 3) xs[p] = fma2(L.z[p], f2(ent.z), xs[p]);
             }
-            if (a >= b.nI) {  // wall: the cell is the owner; outgoing where xi.S > 0
+            if (a >= b.nI && b.bKind[a - b.nI] != kBcMaxwell) {  // open boundary: incoming stored, unrelaxed
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    float2 go = gf[p], ho = hf[p];
+                    eq.relax(L, p, go, ho);
+                    const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
+                    gf[p] = sel2(o0, o1, go, gf[p]);
+                    if (H) hf[p] = sel2(o0, o1, ho, hf[p]);
+                }
+            } else if (a >= b.nI) {  // wall: the cell is the owner; outgoing where xi.S > 0
                 const int w = a - b.nI;
                 const float rws = A.rhoWs[w], hwf = A.wall4[w].x;
                 float2 mw[NP];

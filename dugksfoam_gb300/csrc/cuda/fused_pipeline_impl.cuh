@@ -29,6 +29,7 @@ public:
     bool init(Solver& solver, const StepArgs& a, std::string& err) {
         const Mesh& m = solver.mesh();
         D_ = a.D;
+        bcMask_ = a.bcMask;
         H_ = a.hasH != 0;
         if (D_ != 2 && D_ != 3) { err = "fused pipeline supports 2D and 3D meshes"; return false; }
         npl_ = fused_npl(sizeof(S) == 4 ? DUGKS_FP32_FP64MOM : DUGKS_FP64);
@@ -283,7 +284,7 @@ public:
         return A;
     }
 
-    bool batchable() const override { return fp32_; }
+    bool batchable() const override { return fp32_ && (bcMask_ & ~(1 << kBcMaxwell)) == 0; }
     void batchArgs(const StepArgs& a, int parity, void* out) const override {
         const FusedArgs<S> A = stepArgs(a, parity);
         std::memcpy(out, &A, sizeof(A));
@@ -305,9 +306,15 @@ public:
         if (k == 0) kFace_<<<plan_.nTiles, kWarps * 32, smemA_, s>>>(A);
         else if (!fp32_) kCell_<<<plan_.nTiles, kWarps * 32, smemB_, s>>>(A);
         else if (k == 1) kMacros_<<<std::max(1, (a.nA + 127) / 128), 128, 0, s>>>(A);  // one face per thread
-        else
+        else {
             kGather_<<<std::min((a.nC + kGatherWarps - 1) / kGatherWarps, gatherBlocks_), kGatherWarps * 32, gatherSmem_,
                        s>>>(A, gatherMF_);
+            if (a.bcMask & ((1 << kBcPressureIn) | (1 << kBcPressureOut))) {
+                StepArgs n = A.b;  // P10 from the macros this step wrote
+                n.rho = A.rhoN; n.U = A.UN; n.T = A.TN;
+                launch_pressure_bc(n, s);
+            }
+        }
     }
 
     void endStep(StepArgs& base) override {
@@ -413,6 +420,7 @@ private:
 
     int D_ = 2, npl_ = 1;
     bool fp32_ = false, grad_ = false;
+    int bcMask_ = 1 << kBcMaxwell;
     KernelFn kMacros_ = nullptr;
     int gatherMF_ = 0, gatherBlocks_ = 1;
     size_t gatherSmem_ = 0;

@@ -23,6 +23,8 @@ struct RefBuffers {
 // Launch pass `pass` (0..kRefKernels-1) of one reference-pipeline step.
 // Pass 3 also runs the symmetry-patch copy, pass 7 the pressure-patch update.
 void launch_ref_pass(int pass, const StepArgs& a, const RefBuffers& b, int sms, cudaStream_t s);
+// P10 update of pressureIn / pressureOut patch values from the cell macros in a.
+void launch_pressure_bc(const StepArgs& a, cudaStream_t s);
 // Initial face values of mixed (rho fixedValue) patches; once, at creation.
 void launch_ref_mixed_init(const StepArgs& a, const RefBuffers& b, cudaStream_t s);
 

@@ -463,6 +463,10 @@ int grid_for(long long n, int threads, int sms) {
 
 }  // namespace
 
+void launch_pressure_bc(const StepArgs& a, cudaStream_t s) {
+    if (a.nW > 0) k_pressure<<<(a.nW + 127) / 128, 128, 0, s>>>(a);
+}
+
 void launch_ref_mixed_init(const StepArgs& a, const RefBuffers& b, cudaStream_t s) {
     if (a.nW > 0 && (a.bcMask & (1 << kBcFixedValue))) k_mixed_init<<<a.nW, kRedThreads, 0, s>>>(a, b.gS, b.hS);
 }

@@ -126,9 +126,16 @@ int Solver::init(const dugks_case_desc& d) {
     // ---- boundary kinds other than diffuse walls: plain FP64 pipeline only
     int bcMask = 0;
     for (int wf = 0; wf < nW; ++wf) bcMask |= 1 << m.wallKind[wf];
-    if ((bcMask & ~(1 << DUGKS_PATCH_MAXWELL)) && pipeline_ != DUGKS_PIPE_REFERENCE)
-        return fail(DUGKS_ERR_UNSUPPORTED, "boundary types other than calculatedMaxwell walls need the plain FP64 "
-                                           "pipeline (DUGKS_FP64 with DUGKS_PIPE_REFERENCE or DUGKS_PIPE_AUTO)");
+    // the FP32 pipeline takes walls and the open types; the symmetry types and
+    // the fused FP64 sweeps run on the plain FP64 pipeline only
+    const int fp32Kinds = (1 << DUGKS_PATCH_MAXWELL) | (1 << DUGKS_PATCH_ZERO_GRADIENT) |
+                          (1 << DUGKS_PATCH_FIXED_VALUE) | (1 << DUGKS_PATCH_FAR_FIELD) |
+                          (1 << DUGKS_PATCH_PRESSURE_IN) | (1 << DUGKS_PATCH_PRESSURE_OUT);
+    if (pipeline_ != DUGKS_PIPE_REFERENCE && (bcMask & ~(precision_ == DUGKS_FP32_FP64MOM ? fp32Kinds : 1 << DUGKS_PATCH_MAXWELL)))
+        return fail(DUGKS_ERR_UNSUPPORTED, precision_ == DUGKS_FP32_FP64MOM
+                                               ? "symmetry patches need the plain FP64 pipeline (DUGKS_FP64)"
+                                               : "boundary types other than calculatedMaxwell walls need the plain FP64 "
+                                                 "pipeline (DUGKS_PIPE_REFERENCE or DUGKS_PIPE_AUTO)");
     const bool pressureBc = bcMask & ((1 << DUGKS_PATCH_PRESSURE_IN) | (1 << DUGKS_PATCH_PRESSURE_OUT));
     if (pressureBc && !d.patch_pressure) return fail(DUGKS_ERR_ARG, "pressureIn/pressureOut patches need patch_pressure");
     if ((bcMask & ((1 << DUGKS_PATCH_FIXED_VALUE) | (1 << DUGKS_PATCH_FAR_FIELD))) && !d.bnd_rho)

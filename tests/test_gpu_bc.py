@@ -67,11 +67,32 @@ def test_fp64_boundary_types_match_oracle(built_lib, oracle_lib, name):
     s.close()
 
 
-def test_fp32_path_refuses_open_boundaries(built_lib):
+@pytest.mark.parametrize("name", ["channel", "open_box"])
+def test_fp32_open_boundaries_match_oracle(built_lib, oracle_lib, name):
+    """FP32 bulk / FP64 moments with zeroGradient, fixedValue, farField and the
+    pressure patches: within 1e-5 of the FP64 oracle (the FP32 path's bound)."""
+    from dugksfoam_gb300 import cases, solver
+    from oracle.oracle import Oracle
+
+    case = _cases()[name]
+    dt = cases.stable_dt(case)
+    ref = Oracle(case)
+    ref.step(dt, STEPS)
+    s = solver.FvDVM(case, precision=solver.FP32_FP64MOM)
+    s.set_dt(dt)
+    s.evolution(STEPS)
+    got, want = s.macros(), ref.cell()
+    for k in ("rho", "U", "T", "q"):
+        einf, el2 = rel_err(got[k], want[k])
+        assert einf <= 1e-5 and el2 <= 1e-5, (name, k, einf, el2)
+    s.close()
+
+
+def test_fp32_path_refuses_symmetry_patches(built_lib):
     from dugksfoam_gb300 import solver
 
     with pytest.raises(solver.DugksError) as e:
-        solver.FvDVM(_cases()["channel"], precision=solver.FP32_FP64MOM)
+        solver.FvDVM(_cases()["half_plane"], precision=solver.FP32_FP64MOM)
     assert e.value.code == 3  # DUGKS_ERR_UNSUPPORTED
 
 
