@@ -507,45 +507,6 @@ __device__ __forceinline__ void finalize_face32(const FusedArgs<float>& A, int a
         }
 }
 
-// Face values of an open boundary face (deviation form) once the owner side is
-// reconstructed: zeroGradient takes the owner's gbar+ for every velocity
-// (discreteVelocity.C:551-555); farField / pressureIn / pressureOut replace
-// the incoming velocities (xi.S <= 0) by rho_b M(U of the owner cell, T_b)
-// (:570-600) and fixedValue (mixed) by the Maxwellian of its patch rho, U, T,
-// which stays what it was at the start (:302-345).
-template <int D, bool H, int NPL>
-__device__ __forceinline__ void open_face_values(const FusedArgs<float>& A, int kind, int w, int a,
-                                                 const Lane32<D, NPL>& L, const float2 (&xs)[NPL / 2],
-                                                 const float* ownG, const float* ownH, float2 (&gf)[NPL / 2],
-                                                 float2 (&hf)[NPL / 2]) {
-    constexpr int NP = NPL / 2;
-    const StepArgs& b = A.b;
-    if (kind == kBcZeroGradient) {
-        ldp<NP>(gf, ownG);
-        if (H) ldp<NP>(hf, ownH);
-        return;
-    }
-    const double Tb = b.TbM[w], RT = b.R * Tb;
-    const double* U = kind == kBcFixedValue ? b.Uw + 3 * w : b.U + 3 * b.own[a];
-    const double s = sqrt(2.0 * kPi * RT);
-    const float ng = (float)(A.gscale * b.rhoB[w] / (D == 2 ? s * s : s * s * s));
-    const float i2 = (float)(-0.5 / RT), hw = (float)(RT * (b.K + 3 - D));
-    const float ux = (float)U[0], uy = (float)U[1], uz = (float)U[2];
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
-        const float2 cx = sub2(L.x[p], f2(ux)), cy = sub2(L.y[p], f2(uy));
-        float2 cc = fma2(cy, cy, mul2(cx, cx));
-        if (D == 3) {
-            const float2 cz = sub2(L.z[p], f2(uz));
-            cc = fma2(cz, cz, cc);
-        }
-        const float2 m = make_float2(ng * expf(i2 * cc.x), ng * expf(i2 * cc.y));
-        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
-        gf[p] = sel2(o0, o1, gf[p], sub2(m, L.mr[p]));
-        if (H) hf[p] = sel2(o0, o1, hf[p], sub2(mul2(m, f2(hw)), mul2(L.mr[p], f2(A.hrefFac))));
-    }
-}
-
 // ---------------------------------------------------------------- sweep A, face sides
 // One-sided upwind reconstruction from cell u (local row lu, stencil entries
 // [e0,e1) of u, d = Cf - C_u): val = gbar+_u + sum_e L_e.(d - xi dt/2) (gbar+_e - gbar+_u).
@@ -733,7 +694,6 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
             const size_t fi = (size_t)F.r.a * Vp + v0 + col;
             const float dO[3] = {F.dOx, F.dOy, F.dOz}, dN[3] = {F.dNx, F.dNy, F.dNz};
             if (F.r.w >= 0) {
-                const int kind = b.bKind[F.r.w];
                 if (GR) {  // boundary: owner side; gw = the owner's gradient (for grad . n)
                     side_value_g<D, H, NPL>(L, cg, chh, gbuf, F.r.ownL, dO, A.dt, col, gf, hf);
 #pragma unroll
@@ -758,17 +718,11 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
                     const float2 fx = mul2(mul2(mul2(L.w[p], xs[p]), gf[p]), use[p]);
                     fl += fx.x + fx.y;
                 }
+                m[SL::FLUX] = fl;
                 const size_t wi = (size_t)F.r.w * Vp + v0 + col;
                 stp<NP>(A.Gbgn + wi, gn);
                 if (H) stp<NP>(A.Gbhn + wi, hn);
-                if (kind == kBcMaxwell) {
-                    m[SL::FLUX] = fl;
-                    mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
-                } else {
-                    open_face_values<D, H, NPL>(A, kind, F.r.w, F.r.a, L, xs, cg + F.r.ownL * KC + col,
-                                                chh + F.r.ownL * KC + col, gf, hf);
-                    mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
-                }
+                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
                 stp<NP>(A.gF + fi, gf);
                 if (H) stp<NP>(A.hF + fi, hf);
             } else if (F.r.ownL < hd.nT && F.r.neiL < hd.nT) {  // both sides in T: complete
@@ -857,6 +811,98 @@ __global__ void __launch_bounds__(NW * 32, 1) k_face_sides32_batch(const FusedAr
     face_sides_body<D, H, NPL, NW, false>(sA, w.y, smem);
 }
 
+// Open boundary faces (zeroGradient, fixedValue -> mixed, farField, pressureIn,
+// pressureOut), one warp per face, after sweep A stored their owner-side
+// reconstruction for every velocity: the complete face values (deviation
+// form) and their moments over all velocities, so that the face macros take
+// the internal-face path.  zeroGradient: every velocity takes the owner's
+// gbar+ (discreteVelocity.C:551-555); the others keep the outgoing
+// reconstruction and set the incoming velocities (xi.S <= 0) to
+// rho_b M(U of the owner cell, T_b) (:570-600) -- fixedValue to the
+// Maxwellian of its patch rho, U, T, which stays as it was at the start
+// (:302-345).  A separate kernel keeps the sweep's code unchanged.
+template <int D, bool H, int NPL>
+__global__ void k_open_faces32(FusedArgs<float> A) {
+    using SL = Slots<D, H>;
+    constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2;
+    const StepArgs& b = A.b;
+    const int lane = threadIdx.x & 31, Vp = b.Vp, col = lane * NPL;
+    const int myslot = slot_of<NS>(lane);
+    const bool writer = NS == 16 ? (lane & 1) == 0 : true;
+    for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < b.nW; w += gridDim.x * (blockDim.x >> 5)) {
+        const int kind = b.bKind[w];
+        if (kind == kBcMaxwell) continue;  // warp-uniform
+        const int a = b.nI + w, own = b.own[a];
+        const float sx = (float)b.Sf[3 * a], sy = (float)b.Sf[3 * a + 1], sz = (float)b.Sf[3 * a + 2];
+        const float4 u4 = A.uref4[a];
+        const float ur[3] = {u4.x, u4.y, u4.z};
+        Eq32<D, H> ec;
+        float ng = 0.f, i2 = 0.f, hw = 0.f, ux = 0.f, uy = 0.f, uz = 0.f;
+        if (kind == kBcZeroGradient) {
+            const float* cblk = A.cc + (size_t)own * kNCoef;
+            float4 q[3];
+            eq_table(q, cblk, cell_weight(A.dt, cblk));
+            ec.load(q, b.K, A.hrefFac);
+        } else {
+            const double Tb = b.TbM[w], RT = b.R * Tb;
+            const double* U = kind == kBcFixedValue ? b.Uw + 3 * w : b.U + 3 * own;
+            const double sq = sqrt(2.0 * kPi * RT);
+            ng = (float)(A.gscale * b.rhoB[w] / (D == 2 ? sq * sq : sq * sq * sq));
+            i2 = (float)(-0.5 / RT);
+            hw = (float)(RT * (b.K + 3 - D));
+            ux = (float)U[0]; uy = (float)U[1]; uz = (float)U[2];
+        }
+        Acc<float> acc;
+        acc.zero();
+        for (int v0 = 0; v0 < Vp; v0 += KC) {
+            Lane32<D, NPL> L;
+            L.load(A, v0, lane);
+            const size_t fi = (size_t)a * Vp + v0 + col;
+            float2 gf[NP], hf[NP];
+            if (kind == kBcZeroGradient) {
+                const size_t ci = (size_t)own * Vp + v0 + col;
+                ldp<NP>(gf, A.gT + ci);
+                if (H) ldp<NP>(hf, A.hT + ci);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    if (!H) hf[p] = f2(0.f);
+                    ec.relax(L, p, gf[p], hf[p]);
+                }
+            } else {
+                ldp<NP>(gf, A.gF + fi);
+                if (H) ldp<NP>(hf, A.hF + fi);
+#pragma unroll
+                for (int p = 0; p < NP; ++p) {
+                    float2 xs = fma2(L.y[p], f2(sy), mul2(L.x[p], f2(sx)));
+                    if (D == 3) xs = fma2(L.z[p], f2(sz), xs);
+                    const float2 cx = sub2(L.x[p], f2(ux)), cy = sub2(L.y[p], f2(uy));
+                    float2 cc = fma2(cy, cy, mul2(cx, cx));
+                    if (D == 3) {
+                        const float2 cz = sub2(L.z[p], f2(uz));
+                        cc = fma2(cz, cz, cc);
+                    }
+                    const float2 m = make_float2(ng * expf(i2 * cc.x), ng * expf(i2 * cc.y));
+                    const bool o0 = xs.x > 0.f, o1 = xs.y > 0.f;
+                    gf[p] = sel2(o0, o1, gf[p], sub2(m, L.mr[p]));
+                    if (H) hf[p] = sel2(o0, o1, hf[p], sub2(mul2(m, f2(hw)), mul2(L.mr[p], f2(A.hrefFac))));
+                }
+            }
+            stp<NP>(A.gF + fi, gf);
+            if (H) stp<NP>(A.hF + fi, hf);
+            float m[NS];
+#pragma unroll
+            for (int s2 = 0; s2 < NS; ++s2) m[s2] = 0.0f;
+            mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
+            acc.add(reduce_scatter<NS, float>(m, lane));
+        }
+        double* dst = A.faceMom + (size_t)a * 2 * NS;
+        if (writer && myslot < NS) {
+            dst[myslot] = myslot < SL::FLUX ? acc.value() : 0.0;
+            dst[NS + myslot] = 0.0;
+        }
+    }
+}
+
 // Face macros of every active face from the two per-side moment totals.
 template <int D, bool H>
 __device__ __forceinline__ void face_macros_one(const FusedArgs<float>& A, int a) {
@@ -931,7 +977,9 @@ constexpr int kGatherBatch = 32;
 // One cell of the gather sweep, all DV chunks; returns this lane's slot total
 // of the new cell moments (slot slot_of(lane)).  wb: the warp's two stages,
 // offset by the lane's column.
-template <int D, bool H, int NPL>
+// OPEN: the case has open boundary faces (instantiated apart so that
+// wall-only cases run the same code as before those existed).
+template <int D, bool H, int NPL, bool OPEN = false>
 __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, int MF, float* wb, int lane) {
     using SL = Slots<D, H>;
     constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2, NR = H ? 2 : 1;
@@ -1012,28 +1060,31 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
                 xs[p] = fma2(L.y[p], f2(ent.y), mul2(L.x[p], f2(ent.x)));
                 if (D == 3) xs[p] = fma2(L.z[p], f2(ent.z), xs[p]);
             }
-            if (a >= b.nI && b.bKind[a - b.nI] != kBcMaxwell) {  // open boundary: incoming stored, unrelaxed
-#pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    float2 go = gf[p], ho = hf[p];
-                    eq.relax(L, p, go, ho);
-                    const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
-                    gf[p] = sel2(o0, o1, go, gf[p]);
-                    if (H) hf[p] = sel2(o0, o1, ho, hf[p]);
-                }
-            } else if (a >= b.nI) {  // wall: the cell is the owner; outgoing where xi.S > 0
+            if (a >= b.nI) {  // boundary: the cell is the owner; outgoing where xi.S > 0
                 const int w = a - b.nI;
-                const float rws = A.rhoWs[w], hwf = A.wall4[w].x;
-                float2 mw[NP];
-                ldp<NP>(mw, A.Mw + (size_t)w * Vp + v0 + col);
+                const float4 w4 = A.wall4[w];
+                if (OPEN && w4.z != 0.f) {  // open boundary: incoming stored, unrelaxed
 #pragma unroll
-                for (int p = 0; p < NP; ++p) {
-                    float2 go = gf[p], ho = hf[p];
-                    eq.relax(L, p, go, ho);
-                    const float2 gw = mul2(f2(rws), mw[p]);
-                    const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
-                    gf[p] = sel2(o0, o1, go, sub2(gw, L.mr[p]));
-                    if (H) hf[p] = sel2(o0, o1, ho, sub2(mul2(gw, f2(hwf)), mul2(L.mr[p], f2(A.hrefFac))));
+                    for (int p = 0; p < NP; ++p) {
+                        float2 go = gf[p], ho = hf[p];
+                        eq.relax(L, p, go, ho);
+                        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
+                        gf[p] = sel2(o0, o1, go, gf[p]);
+                        if (H) hf[p] = sel2(o0, o1, ho, hf[p]);
+                    }
+                } else {  // diffuse wall: incoming rho_w Mw
+                    const float rws = A.rhoWs[w], hwf = w4.x;
+                    float2 mw[NP];
+                    ldp<NP>(mw, A.Mw + (size_t)w * Vp + v0 + col);
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) {
+                        float2 go = gf[p], ho = hf[p];
+                        eq.relax(L, p, go, ho);
+                        const float2 gw = mul2(f2(rws), mw[p]);
+                        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;
+                        gf[p] = sel2(o0, o1, go, sub2(gw, L.mr[p]));
+                        if (H) hf[p] = sel2(o0, o1, ho, sub2(mul2(gw, f2(hwf)), mul2(L.mr[p], f2(A.hrefFac))));
+                    }
                 }
             } else {
 #pragma unroll
@@ -1067,7 +1118,7 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
 // tiles or block barriers.  The rows of chunk k+1 are copied into the warp's
 // other stage while chunk k is computed; the FP64 macros of a batch of cells
 // are finished together, one lane per cell.
-template <int D, bool H, int NPL, int NW>
+template <int D, bool H, int NPL, int NW, bool OPEN = false>
 __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A, int MF) {
     constexpr int NS = Slots<D, H>::NS, KC = 32 * NPL, NR = H ? 2 : 1;
     __shared__ double sM[NW][kGatherBatch][NS];
@@ -1080,7 +1131,7 @@ __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A
     const int TW = gridDim.x * NW, nC = A.b.nC;
     int nb = 0;
     for (int c = blockIdx.x * NW + warp; c < nC; c += TW) {
-        const double tot = gather_cell<D, H, NPL>(A, c, MF, wb, lane);
+        const double tot = gather_cell<D, H, NPL, OPEN>(A, c, MF, wb, lane);
         if (writer) sM[warp][nb][myslot] = tot;
         if (lane == 0) sC[warp][nb] = c;
         ++nb;

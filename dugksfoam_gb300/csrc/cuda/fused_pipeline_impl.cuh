@@ -36,12 +36,12 @@ public:
         fp32_ = sizeof(S) == 4;
         const int KC = 32 * npl_;
         if (a.Vp % KC != 0) { err = "padded DV count is not a multiple of the DV chunk"; return false; }
-        pick();
         // ---- tile plan, sized to the shared-memory budget
         int dev = 0;
         cudaGetDevice(&dev);
         int maxSmem = 0;
         cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        pick();
         const size_t budget = (size_t)maxSmem - 2048;
         const char* envT = std::getenv("DUGKS_TILE_CELLS");
         const int maxCells = fused_tile_cap() > 0 ? fused_tile_cap() : (envT ? std::max(1, std::atoi(envT)) : 4096);
@@ -171,7 +171,8 @@ public:
             std::vector<double> Tw(a.nW);
             if (a.nW) cudaMemcpy(Tw.data(), a.Tw, a.nW * 8, cudaMemcpyDeviceToHost);
             for (int w = 0; w < a.nW; ++w)
-                w4[w] = make_float4((float)((a.R * Tw[w]) * (a.K + 3 - a.D)), (float)(1.0 / m.dcW[w]), 0.f, 0.f);
+                w4[w] = make_float4((float)((a.R * Tw[w]) * (a.K + 3 - a.D)), (float)(1.0 / m.dcW[w]),
+                                    m.wallKind[w] == DUGKS_PATCH_MAXWELL ? 0.f : 1.f, 0.f);  // .z: open boundary
             args_.wall4 = upload(w4);
             args_.rhoWs = alloc<float>(std::max(a.nW, 1));
             args_.uref4 = alloc<float4>(a.nA);
@@ -303,7 +304,10 @@ public:
 
     void launchArgs(int k, const FusedArgs<S>& A, const StepArgs& a, int sms, cudaStream_t s) {
         (void)sms;
-        if (k == 0) kFace_<<<plan_.nTiles, kWarps * 32, smemA_, s>>>(A);
+        if (k == 0) {
+            kFace_<<<plan_.nTiles, kWarps * 32, smemA_, s>>>(A);
+            if (kOpen_) kOpen_<<<std::max(1, std::min((a.nW + 3) / 4, sms * 8)), 128, 0, s>>>(A);
+        }
         else if (!fp32_) kCell_<<<plan_.nTiles, kWarps * 32, smemB_, s>>>(A);
         else if (k == 1) kMacros_<<<std::max(1, (a.nA + 127) / 128), 128, 0, s>>>(A);  // one face per thread
         else {
@@ -387,7 +391,9 @@ private:
             grad_ = D == 3 || fused_face_grad();
             kFace_ = grad_ ? k_face_sides32<D, H, NPL, kWarps, true> : k_face_sides32<D, H, NPL, kWarps, false>;
             kMacros_ = k_face_macros32<D, H>;
-            kGather_ = k_cell_gather32<D, H, NPL, kGatherWarps>;
+            kOpen_ = (bcMask_ & ~(1 << kBcMaxwell)) ? k_open_faces32<D, H, NPL> : nullptr;
+            kGather_ = (bcMask_ & ~(1 << kBcMaxwell)) ? k_cell_gather32<D, H, NPL, kGatherWarps, true>
+                                                     : k_cell_gather32<D, H, NPL, kGatherWarps, false>;
             kRef_ = k_ref_tables<D, H>;
         } else {
             kFace_ = k_sweep_face<S, D, H, NPL, kWarps>;
@@ -422,6 +428,7 @@ private:
     bool fp32_ = false, grad_ = false;
     int bcMask_ = 1 << kBcMaxwell;
     KernelFn kMacros_ = nullptr;
+    KernelFn kOpen_ = nullptr;  // open boundary faces after sweep A (when the case has any)
     int gatherMF_ = 0, gatherBlocks_ = 1;
     size_t gatherSmem_ = 0;
     void (*kGather_)(FusedArgs<S>, int) = nullptr;
