@@ -820,7 +820,13 @@ __global__ void __launch_bounds__(NW * 32, 1) k_face_sides32_batch(const FusedAr
 // reconstruction and set the incoming velocities (xi.S <= 0) to
 // rho_b M(U of the owner cell, T_b) (:570-600) -- fixedValue to the
 // Maxwellian of its patch rho, U, T, which stays as it was at the start
-// (:302-345).  A separate kernel keeps the sweep's code unchanged.
+// (:302-345).  Symmetry faces (symmetryMod, symmetryPlane): the incoming
+// velocities (xi.S0 <= 0, S0 the patch's first face) take their mirror
+// velocity's value (discreteVelocity.C:733-817), read from a snapshot of the
+// face row; symmetryPlane assigns in index order, so a mirror that is itself
+// an earlier incoming velocity passes its own mirror's value on (the chain
+// ends after one step on grids symmetric about 0).  A separate kernel keeps
+// the sweep's code unchanged.
 template <int D, bool H, int NPL>
 __global__ void k_open_faces32(FusedArgs<float> A) {
     using SL = Slots<D, H>;
@@ -838,7 +844,19 @@ __global__ void k_open_faces32(FusedArgs<float> A) {
         const float ur[3] = {u4.x, u4.y, u4.z};
         Eq32<D, H> ec;
         float ng = 0.f, i2 = 0.f, hw = 0.f, ux = 0.f, uy = 0.f, uz = 0.f;
-        if (kind == kBcZeroGradient) {
+        const bool sym = kind == kBcSymmetryMod || kind == kBcSymmetryPlane;
+        const double* S0 = b.bS0 + 3 * w;
+        auto incoming = [&](int u) {
+            return b.xi[u] * S0[0] + b.xi[Vp + u] * S0[1] + b.xi[2 * Vp + u] * S0[2] <= 0;
+        };
+        if (sym) {  // snapshot of the row
+            const size_t fb = (size_t)a * Vp, wb = (size_t)w * Vp;
+            for (int v = lane; v < Vp; v += 32) {
+                A.symG[wb + v] = A.gF[fb + v];
+                if (H) A.symH[wb + v] = A.hF[fb + v];
+            }
+            __syncwarp();
+        } else if (kind == kBcZeroGradient) {
             const float* cblk = A.cc + (size_t)own * kNCoef;
             float4 q[3];
             eq_table(q, cblk, cell_weight(A.dt, cblk));
@@ -859,7 +877,31 @@ __global__ void k_open_faces32(FusedArgs<float> A) {
             L.load(A, v0, lane);
             const size_t fi = (size_t)a * Vp + v0 + col;
             float2 gf[NP], hf[NP];
-            if (kind == kBcZeroGradient) {
+            if (sym) {
+                ldp<NP>(gf, A.gF + fi);
+                if (H) ldp<NP>(hf, A.hF + fi);
+                float* gs = reinterpret_cast<float*>(gf);
+                float* hs = reinterpret_cast<float*>(hf);
+                const int* tab = b.symTab + (size_t)b.symOff[w] * b.nV;
+                const float* snG = A.symG + (size_t)w * Vp;
+                const float* snH = H ? A.symH + (size_t)w * Vp : nullptr;
+#pragma unroll
+                for (int j = 0; j < NPL; ++j) {
+                    const int v = v0 + col + j;
+                    if (v >= b.nV || !incoming(v)) continue;
+                    int cur = v, u = tab[v];
+                    if (kind == kBcSymmetryPlane)
+                        for (int guard = 0; guard < b.nV && u < cur && incoming(u); ++guard) {
+                            cur = u;
+                            u = tab[u];
+                        }
+                    gs[j] = snG[u];
+                    if (H) hs[j] = snH[u];
+                }
+                if (!H)
+#pragma unroll
+                    for (int p = 0; p < NP; ++p) hf[p] = f2(0.f);
+            } else if (kind == kBcZeroGradient) {
                 const size_t ci = (size_t)own * Vp + v0 + col;
                 ldp<NP>(gf, A.gT + ci);
                 if (H) ldp<NP>(hf, A.hT + ci);
@@ -1064,8 +1106,10 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
                 const int w = a - b.nI;
                 const float4 w4 = A.wall4[w];
                 if (OPEN && w4.z != 0.f) {  // open boundary: incoming stored, unrelaxed
+                    const bool plane = w4.z == 2.f;  // symmetryPlane: every DV once, outgoing twice
 #pragma unroll
                     for (int p = 0; p < NP; ++p) {
+                        if (plane) eq.relax(L, p, gf[p], hf[p]);
                         float2 go = gf[p], ho = hf[p];
                         eq.relax(L, p, go, ho);
                         const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f;

@@ -76,7 +76,9 @@ struct FusedArgs {
     const S* Mw;                // [nW][Vp] wall Maxwellian / rho
     const double* Min;          // [nW][NS] incoming moments of Mw about Uw
     // FP32 side data
-    const float4* wall4;        // [nW] {R Tw (K+3-D), 1/deltaCoeff, open boundary ? 1 : 0, 0}
+    const float4* wall4;        // [nW] {R Tw (K+3-D), 1/deltaCoeff (0: symmetryPlane), kind: 0 wall,
+                                //       1 open or symmetryMod, 2 symmetryPlane, 0}
+    float *symG, *symH;         // [nW][Vp] snapshot of symmetry faces' values (when present)
     float* rhoWs;               // [nW] scaled rho_w (written by sweep A)
     float4* uref4;              // [nA] face reference velocity (walls: U_w)
     const float* cc;            // [nC][kNCoef] current cell equilibrium block

@@ -170,10 +170,20 @@ public:
             std::vector<float4> w4(std::max(a.nW, 1), make_float4(0, 0, 0, 0));
             std::vector<double> Tw(a.nW);
             if (a.nW) cudaMemcpy(Tw.data(), a.Tw, a.nW * 8, cudaMemcpyDeviceToHost);
-            for (int w = 0; w < a.nW; ++w)
-                w4[w] = make_float4((float)((a.R * Tw[w]) * (a.K + 3 - a.D)), (float)(1.0 / m.dcW[w]),
-                                    m.wallKind[w] == DUGKS_PATCH_MAXWELL ? 0.f : 1.f, 0.f);  // .z: open boundary
+            for (int w = 0; w < a.nW; ++w) {
+                // .y: 1/deltaCoeff of the lagged-gradient boundary value; 0 on
+                // symmetryPlane (a constraint patch of gbar+: value = internal value)
+                // .z: 0 wall, 1 open boundary, 2 symmetryPlane (relaxed twice outgoing)
+                const int kind = m.wallKind[w];
+                const bool plane = kind == DUGKS_PATCH_SYMMETRY_PLANE;
+                w4[w] = make_float4((float)((a.R * Tw[w]) * (a.K + 3 - a.D)), plane ? 0.f : (float)(1.0 / m.dcW[w]),
+                                    kind == DUGKS_PATCH_MAXWELL ? 0.f : (plane ? 2.f : 1.f), 0.f);
+            }
             args_.wall4 = upload(w4);
+            if (a.bcMask & ((1 << kBcSymmetryMod) | (1 << kBcSymmetryPlane))) {
+                args_.symG = alloc<float>((size_t)a.nW * a.Vp);
+                args_.symH = H_ ? alloc<float>((size_t)a.nW * a.Vp) : nullptr;
+            }
             args_.rhoWs = alloc<float>(std::max(a.nW, 1));
             args_.uref4 = alloc<float4>(a.nA);
         } else {

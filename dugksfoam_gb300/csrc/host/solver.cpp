@@ -126,11 +126,11 @@ int Solver::init(const dugks_case_desc& d) {
     // ---- boundary kinds other than diffuse walls: plain FP64 pipeline only
     int bcMask = 0;
     for (int wf = 0; wf < nW; ++wf) bcMask |= 1 << m.wallKind[wf];
-    // the FP32 pipeline takes walls and the open types; the symmetry types and
-    // the fused FP64 sweeps run on the plain FP64 pipeline only
+    // the FP32 pipeline takes every type; the fused FP64 sweeps take walls only
     const int fp32Kinds = (1 << DUGKS_PATCH_MAXWELL) | (1 << DUGKS_PATCH_ZERO_GRADIENT) |
                           (1 << DUGKS_PATCH_FIXED_VALUE) | (1 << DUGKS_PATCH_FAR_FIELD) |
-                          (1 << DUGKS_PATCH_PRESSURE_IN) | (1 << DUGKS_PATCH_PRESSURE_OUT);
+                          (1 << DUGKS_PATCH_PRESSURE_IN) | (1 << DUGKS_PATCH_PRESSURE_OUT) |
+                          (1 << DUGKS_PATCH_SYMMETRY_MOD) | (1 << DUGKS_PATCH_SYMMETRY_PLANE);
     if (pipeline_ != DUGKS_PIPE_REFERENCE && (bcMask & ~(precision_ == DUGKS_FP32_FP64MOM ? fp32Kinds : 1 << DUGKS_PATCH_MAXWELL)))
         return fail(DUGKS_ERR_UNSUPPORTED, precision_ == DUGKS_FP32_FP64MOM
                                                ? "symmetry patches need the plain FP64 pipeline (DUGKS_FP64)"

@@ -67,10 +67,11 @@ def test_fp64_boundary_types_match_oracle(built_lib, oracle_lib, name):
     s.close()
 
 
-@pytest.mark.parametrize("name", ["channel", "open_box"])
-def test_fp32_open_boundaries_match_oracle(built_lib, oracle_lib, name):
-    """FP32 bulk / FP64 moments with zeroGradient, fixedValue, farField and the
-    pressure patches: within 1e-5 of the FP64 oracle (the FP32 path's bound)."""
+@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod"])
+def test_fp32_boundary_types_match_oracle(built_lib, oracle_lib, name):
+    """FP32 bulk / FP64 moments with zeroGradient, fixedValue, farField, the
+    pressure and the symmetry patches: within 1e-5 of the FP64 oracle (the FP32
+    path's bound)."""
     from dugksfoam_gb300 import cases, solver
     from oracle.oracle import Oracle
 
@@ -88,11 +89,11 @@ def test_fp32_open_boundaries_match_oracle(built_lib, oracle_lib, name):
     s.close()
 
 
-def test_fp32_path_refuses_symmetry_patches(built_lib):
+def test_fused_fp64_sweeps_refuse_open_boundaries(built_lib):
     from dugksfoam_gb300 import solver
 
     with pytest.raises(solver.DugksError) as e:
-        solver.FvDVM(_cases()["half_plane"], precision=solver.FP32_FP64MOM)
+        solver.FvDVM(_cases()["half_plane"], precision=solver.FP64, pipeline=solver.PIPE_FUSED)
     assert e.value.code == 3  # DUGKS_ERR_UNSUPPORTED
 
 
