@@ -344,7 +344,7 @@ def stable_dt(case, cfl=0.5):
     C, _ = cell_centres_volumes(mesh)
     d = C[mesh["neighbour"]] - C[mesh["owner"][: len(mesh["neighbour"])]]
     dc = 1.0 / np.sqrt((d * d).sum(1))
-    D = 2 if case["two_d"] else 3
+    D = 1 if case.get("one_d") else (2 if case["two_d"] else 3)
     return cfl / (dc.max() * math.sqrt(D) * case["xi_max"])
 
 
@@ -448,6 +448,22 @@ def half_cavity2d(nx=15, ny=30, Kn=0.075, nxi=16, sym="symmetryPlane"):
         ("movingWall", "wall", ["y1"], None), ("fixedWalls", "wall", ["x0", "y0"], None),
         ("symmetryWall", mtype, ["x1"], sym)])
     return make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, bvals={"symmetryWall": dict(T=273.0)})
+
+
+def tube1d(nx=100, Kn=0.05, nxi=32, rho_ratio=4.0):
+    """1D closed shock tube [0,1] in reduced units (R = 1/2, T0 = 1): rho = 1
+    on the left half and 1/rho_ratio on the right, at rest, diffuse walls at
+    both ends; y and z faces are empty patches, so the case is 1D (M velocities)."""
+    gas, _ = gas_from_kn(Kn, R=0.5, T0=1.0)
+    gas["muRef"] = gas["muRef"] / _
+    xi_max = 5.0 * math.sqrt(2 * gas["R"] * 1.0)
+    mesh = structured_mesh(nx, 1, 1, lx=1.0, ly=1.0 / nx, lz=1.0 / nx, two_d=True, patch_defs=[
+        ("left", "wall", ["x0"], None), ("right", "wall", ["x1"], None), ("sides", "empty", ["y0", "y1"], None)])
+    case = make_case(mesh, gas, 1.0, nxi, xi_max, two_d=True, lid_u=0.0, T0=1.0, lid_patch="none")
+    xc = (np.arange(nx) + 0.5) / nx
+    case["rho0"] = np.where(xc < 0.5, 1.0, 1.0 / rho_ratio)
+    case["one_d"] = True
+    return case
 
 
 def batch_case(inst):

@@ -28,6 +28,7 @@ public:
 
     bool init(Solver& solver, const StepArgs& a, std::string& err) {
         const Mesh& m = solver.mesh();
+        if (a.D != 2 && a.D != 3) { err = "the fused pipelines need a 2D or 3D mesh (1D runs on the plain FP64 pipeline)"; return false; }
         D_ = a.D;
         bcMask_ = a.bcMask;
         H_ = a.hasH != 0;

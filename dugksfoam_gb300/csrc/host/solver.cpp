@@ -200,9 +200,13 @@ int Solver::init(const dugks_case_desc& d) {
                         sx = iz * M * M + iy * M + (M - ix - 1);
                         sy = iz * M * M + (M - iy - 1) * M + ix;
                         sz = (M - iz - 1) * M * M + iy * M + ix;
-                    } else {
+                    } else if (D == 2) {
                         sx = iy * M + (M - ix - 1);
                         sy = (M - iy - 1) * M + ix;
+                        sz = 0;
+                    } else {
+                        sx = M - ix - 1;
+                        sy = 0;
                         sz = 0;
                     }
                     const long t = std::lround(std::fabs(n[0] * sx + n[1] * sy + n[2] * sz));

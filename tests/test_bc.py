@@ -1,8 +1,9 @@
 """Boundary types other than diffuse walls on the CPU: the oracle's restatement
 of zeroGradient, mixed (rho fixedValue), farField, pressureIn / pressureOut
 (discreteVelocity.C:530-689, fvDVM.C:730-806) and the two symmetry types
-(discreteVelocity.C:733-817), the case writer and reader for them, and the
-reference's own symmetry demo case read in place when the tree is present."""
+(discreteVelocity.C:733-817), 1D meshes, the case writer and reader for them,
+and the reference's own symmetry demo case read in place when the tree is
+present."""
 import os
 
 import numpy as np
@@ -105,3 +106,20 @@ def test_reference_symmetry_demo_case(built_lib):
     s = solver.inspect_case_dir(REF_SYM)
     assert (s["n_cells"], s["n_wall_faces"], s["n_empty_faces"]) == (1800, 120, 3600)
     assert s["n_patches"] == 4
+
+
+def test_oracle_1d_tube(oracle_lib):
+    """A 1D mesh (y and z faces empty: M velocities, fvDVM.C:196-219) between
+    two diffuse walls: the expansion runs from the dense half into the thin one."""
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import Oracle
+
+    case = cases.tube1d(40, nxi=16)
+    o = Oracle(case)
+    assert o.D == 1 and o.nV == 16
+    o.step(cases.stable_dt(case), 100)
+    c = o.cell()
+    assert np.isfinite(c["q"]).all() and c["T"].min() > 0
+    mid = len(c["rho"]) // 2
+    assert c["U"][mid - 3:mid + 3, 0].min() > 0.05  # gas moves toward the thin side
+    assert c["rho"][:mid].mean() > c["rho"][mid:].mean()

@@ -123,3 +123,26 @@ def test_channel_writes_a_restartable_time_directory(built_lib, tmp_path):
     shutil.copytree(tmp_path / "10", tmp_path / "0")
     info = solver.inspect_case_dir(tmp_path)
     assert info["n_cells"] == m["n_cells"]
+
+
+def test_fp64_1d_tube_matches_oracle(built_lib, oracle_lib):
+    """1D mesh on the plain FP64 pipeline (the fused pipelines refuse it)."""
+    from dugksfoam_gb300 import cases, solver
+    from oracle.oracle import Oracle
+
+    case = cases.tube1d(60, nxi=16)
+    dt = cases.stable_dt(case)
+    ref = Oracle(case)
+    ref.step(dt, STEPS)
+    s = solver.FvDVM(case, precision=solver.FP64)
+    assert s.info()["n_solution_d"] == 1
+    s.set_dt(dt)
+    s.evolution(STEPS)
+    got, want = s.macros(), ref.cell()
+    for k in ("rho", "U", "T", "q"):
+        einf, el2 = rel_err(got[k], want[k])
+        assert einf <= TOL64 and el2 <= TOL64, ("1d", k, einf, el2)
+    s.close()
+    with pytest.raises(solver.DugksError) as e:
+        solver.FvDVM(case, precision=solver.FP32_FP64MOM)
+    assert e.value.code == 3  # DUGKS_ERR_UNSUPPORTED
