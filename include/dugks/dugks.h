@@ -244,7 +244,7 @@ int dugks_inspect_case_dir(const char* case_dir, dugks_case_summary* out);
  * those of the case directory, or patch<i> for handles made by dugks_create. */
 int dugks_write_time(dugks_handle* h, const char* case_dir, const char* time_name);
 
-/* ---- gradient harness (no counterpart in the reference; SURVEY config 4) ----
+/* ---- gradient harness (no counterpart in the reference) ----
  * Objective over a window of FP64 steps from the handle's initial state:
  *   J = 1/(n_steps-avg_first) * sum_{n=avg_first}^{n_steps-1}
  *       [ sum_{w in q_patch} S_w . qWall_w(n) + sum_{w in stress_patch} |S_w| stressWall_w,xy(n) ]
@@ -266,7 +266,7 @@ int dugks_objective_tangent(dugks_handle* h, const dugks_objective* o, const dou
 /* Adjoint gradient: dJ/dTw [n_wall_faces] and dJ/ds, with J. */
 int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J, double* dJ_dTw, double* dJ_ds);
 
-/* ---- batched cases (no counterpart in the reference; SURVEY config 3) ----
+/* ---- batched cases (no counterpart in the reference) ----
  * Independent 2D cases (uneven meshes and velocity grids) advanced together
  * with the FP32 pipeline: every pass of the step is one launch over all cases,
  * the cases are split into groups whose launch chains are independent
