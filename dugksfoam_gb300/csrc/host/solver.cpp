@@ -545,12 +545,14 @@ int Solver::setDist(const double* g, const double* h) {
 }
 
 // Exact-restart checkpoint layout: header, g~, h~ (storage type), lagged
-// boundary gradients, cell macros rho,U,T,q,tau, face velocity.
+// boundary gradients, cell macros rho,U,T,q,tau, face velocity, boundary patch
+// values rho_b, T_b, U_b (pressure patches change them every step).
 size_t Solver::checkpointSize() const {
     const size_t es = precision_ == DUGKS_FP64 ? 8 : 4;
     const size_t nCV = (size_t)mesh_.nC * Vp_, nWV = (size_t)mesh_.nW * Vp_;
     const size_t nd = hasH_ ? 2 : 1;
-    return sizeof(CkptHeader) + nd * (nCV + nWV) * es + (size_t)mesh_.nC * 9 * 8 + (size_t)base_.nA * 3 * 8;
+    return sizeof(CkptHeader) + nd * (nCV + nWV) * es + (size_t)mesh_.nC * 9 * 8 + (size_t)base_.nA * 3 * 8 +
+           (size_t)mesh_.nW * 5 * 8;
 }
 
 int Solver::checkpointSave(void* buf, size_t n) {
@@ -558,7 +560,7 @@ int Solver::checkpointSave(void* buf, size_t n) {
     if (int e = synchronize()) return e;
     char* p = static_cast<char*>(buf);
     CkptHeader hd{};
-    std::memcpy(hd.magic, "DUGKSCK1", 8);
+    std::memcpy(hd.magic, "DUGKSCK2", 8);
     hd.abi = DUGKS_ABI_VERSION; hd.precision = precision_; hd.nC = mesh_.nC; hd.nV = nV_; hd.Vp = Vp_;
     hd.nW = mesh_.nW; hd.hasH = hasH_; hd.dt = dt_; hd.steps = steps_;
     std::memcpy(p, &hd, sizeof(hd));
@@ -585,6 +587,8 @@ int Solver::checkpointSave(void* buf, size_t n) {
     const size_t nC = mesh_.nC;
     get(base_.rho, nC * 8); get(base_.U, 3 * nC * 8); get(base_.T, nC * 8); get(base_.q, 3 * nC * 8); get(base_.tau, nC * 8);
     get(base_.UF, (size_t)base_.nA * 3 * 8);
+    const size_t nW = mesh_.nW;
+    get(base_.rhoB, nW * 8); get(base_.TbM, nW * 8); get(base_.UbM, 3 * nW * 8);
     return checkCuda(ce, "checkpoint save");
 }
 
@@ -593,7 +597,7 @@ int Solver::checkpointLoad(const void* buf, size_t n) {
     const char* p = static_cast<const char*>(buf);
     CkptHeader hd;
     std::memcpy(&hd, p, sizeof(hd));
-    if (std::memcmp(hd.magic, "DUGKSCK1", 8) != 0) return fail(DUGKS_ERR_ARG, "not a DUGKS checkpoint");
+    if (std::memcmp(hd.magic, "DUGKSCK2", 8) != 0) return fail(DUGKS_ERR_ARG, "not a DUGKS checkpoint (or an older layout)");
     if (hd.precision != precision_ || hd.nC != mesh_.nC || hd.nV != nV_ || hd.Vp != Vp_ || hd.nW != mesh_.nW ||
         hd.hasH != hasH_)
         return fail(DUGKS_ERR_ARG, "checkpoint does not match this case/precision");
@@ -622,6 +626,8 @@ int Solver::checkpointLoad(const void* buf, size_t n) {
     const size_t nC = mesh_.nC;
     put(base_.rho, nC * 8); put(base_.U, 3 * nC * 8); put(base_.T, nC * 8); put(base_.q, 3 * nC * 8); put(base_.tau, nC * 8);
     put(base_.UF, (size_t)base_.nA * 3 * 8);
+    const size_t nW = mesh_.nW;
+    put(base_.rhoB, nW * 8); put(base_.TbM, nW * 8); put(base_.UbM, 3 * nW * 8);
     dt_ = hd.dt;
     steps_ = hd.steps;
     if (ce == cudaSuccess && fused_) fused_->refreshDerived(argsNow(), sms_, stream_);

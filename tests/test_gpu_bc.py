@@ -146,3 +146,27 @@ def test_fp64_1d_tube_matches_oracle(built_lib, oracle_lib):
     with pytest.raises(solver.DugksError) as e:
         solver.FvDVM(case, precision=solver.FP32_FP64MOM)
     assert e.value.code == 3  # DUGKS_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pressure_case_restarts_exactly(built_lib, precision):
+    """The checkpoint carries the pressure patches' rho_b, T_b, U_b: a restored
+    handle continues bit for bit (FP64 and FP32 pipelines)."""
+    from dugksfoam_gb300 import cases, solver
+
+    case = _cases()["channel"]
+    dt = cases.stable_dt(case)
+    a = solver.FvDVM(case, precision=precision)
+    a.set_dt(dt)
+    a.evolution(10)
+    ck = a.checkpoint()
+    a.evolution(10)
+    want = a.macros()
+    b = solver.FvDVM(case, precision=precision)
+    b.restore(ck)
+    b.evolution(10)
+    got = b.macros()
+    for k in ("rho", "U", "T", "q"):
+        assert np.array_equal(got[k], want[k]), k
+    a.close()
+    b.close()
