@@ -377,7 +377,9 @@ __global__ void k_cell_coef(StepArgs b, float* cc, double gs) {
 // Face reference velocities (FP32 path): current face velocity, wall velocity on walls.
 static __global__ void k_face_uref(StepArgs b, float4* uref4) {
     for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < b.nA; a += gridDim.x * blockDim.x) {
-        const double* u = a < b.nI ? b.UF + 3 * a : b.Uw + 3 * (a - b.nI);
+        // walls: moments about U_w; internal and open boundary faces: the face velocity
+        const bool wall = a >= b.nI && b.bKind[a - b.nI] == kBcMaxwell;
+        const double* u = wall ? b.Uw + 3 * (a - b.nI) : b.UF + 3 * a;
         uref4[a] = make_float4((float)u[0], (float)u[1], (float)u[2], 0.0f);
     }
 }
