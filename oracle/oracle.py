@@ -227,6 +227,9 @@ class NumpyOracle:
     Same algorithm as fvDVM::evolution (fvDVM.C:1086-1108) written as whole-
     array operations: it does not share code or summation order with the C
     oracle, so agreement to ~1e-13 cross-checks both.  Small meshes only.
+    Boundary types as the C oracle (every rho type of BC_KINDS); symmetry
+    patches copy from a snapshot, which equals symmetryPlane's index-order
+    assignment on grids symmetric about 0.
     """
 
     def __init__(self, case):
@@ -245,10 +248,16 @@ class NumpyOracle:
         self.own = np.asarray(m["owner"][:nI])
         self.nei = np.asarray(m["neighbour"])
         kinds = np.zeros(nF - nI, np.int32)
+        press = np.zeros(nF - nI)
+        first = np.zeros(nF - nI, np.int64)
         for p in m["patches"]:
-            kinds[p["startFace"] - nI:p["startFace"] - nI + p["nFaces"]] = (
-                PATCH_MAXWELL if p["type"] == "wall" else PATCH_EMPTY)
-        wall = np.nonzero(kinds == PATCH_MAXWELL)[0]
+            sl = slice(p["startFace"] - nI, p["startFace"] - nI + p["nFaces"])
+            kinds[sl] = BC_KINDS[patch_bc(p)]
+            press[sl] = p.get("pressure", 0.0)
+            first[sl] = p["startFace"]
+        wall = np.nonzero(kinds != PATCH_EMPTY)[0]  # every active boundary face
+        self.kind = kinds[wall]
+        self.pB = press[wall]
         self.wb = wall
         self.wf = nI + wall
         self.wc = np.asarray(m["owner"])[self.wf]
@@ -259,8 +268,13 @@ class NumpyOracle:
         self.dcB = geo["deltaCoeffs"][nI:][wall]
         Sw = self.Sf[self.wf]
         self.nHat = Sw / np.linalg.norm(Sw, axis=1)[:, None]
-        self.Uw = case["Ub"][wall]
-        self.Tw = case["Tb"][wall]
+        self.Uw = np.array(case["Ub"][wall], float)
+        self.Tw = np.array(case["Tb"][wall], float)
+        self.rhob = np.array(case.get("rhob", np.zeros(nF - nI))[wall], float)
+        self.rhob[(self.kind == 5) | (self.kind == 6)] = 1.0  # pressure patches start at 1
+        S0 = geo["Sf"][first[wall]]
+        self.mirror = self._mirrors(S0)  # [nb][nV] mirror DV (symmetry faces)
+        self.inS0 = (S0 @ self.xi.T) <= 0
         nC = m["n_cells"]
         self.rho = np.array(case["rho0"], float)
         self.U = np.array(case["U0"], float)
@@ -271,8 +285,32 @@ class NumpyOracle:
         self.Gg = np.zeros((len(wall), len(self.w)))
         self.Gh = np.zeros_like(self.Gg)
         xs_w = Sw @ self.xi.T
-        M = self._maxwell(self.Uw, self.Tw)
+        Tpos = np.where(self.Tw > 0, self.Tw, 1.0)
+        M = self._maxwell(self.Uw, Tpos)
         self.inc = np.where(xs_w < 0, -self.w[None, :] * xs_w * M, 0.0).sum(1)
+        # mixed (rho fixedValue): frozen Maxwellian of the initial patch values
+        self.mixG = self.rhob[:, None] * M
+        self.mixH = (self.K + 3 - self.D) * self.R * Tpos[:, None] * self.mixG
+
+    def _mirrors(self, S0):
+        """round(|n . (symX, symY, symZ)|) per face and DV (fvDVM.C:140-221)."""
+        nV, D = len(self.w), self.D
+        M = int(round(nV ** (1.0 / D)))
+        v = np.arange(nV)
+        ix = v % M
+        iy = (v // M) % M if D == 3 else (v // M if D == 2 else 0 * v)
+        iz = v // (M * M) if D == 3 else 0 * v
+        if D == 3:
+            sx = iz * M * M + iy * M + (M - ix - 1)
+            sy = iz * M * M + (M - iy - 1) * M + ix
+            sz = (M - iz - 1) * M * M + iy * M + ix
+        elif D == 2:
+            sx, sy, sz = iy * M + (M - ix - 1), (M - iy - 1) * M + ix, 0 * v
+        else:
+            sx, sy, sz = M - ix - 1, 0 * v, 0 * v
+        n = S0 / np.linalg.norm(S0, axis=1)[:, None]
+        t = np.rint(np.abs(n[:, 0:1] * sx + n[:, 1:2] * sy + n[:, 2:3] * sz)).astype(np.int64)
+        return np.clip(t, 0, nV - 1)
 
     def _shakhov(self, rho, U, T, q):
         R, Pr, D, K = self.R, self.Pr, self.D, self.K
@@ -327,6 +365,7 @@ class NumpyOracle:
             np.add.at(grad, own, self.pV[:, None, :] * d[:, :, None])
             np.add.at(grad, nei, -self.nV_[:, None, :] * d[:, :, None])
             phib = f[self.wc] + G / self.dcB[:, None]
+            phib = np.where((self.kind == 8)[:, None], f[self.wc], phib)  # symmetryPlane: internal value
             np.add.at(grad, self.wc, self.bV[:, None, :] * (phib - f[self.wc])[:, :, None])
             grads.append(grad)
             newG.append((grad[self.wc] * self.nHat[:, None, :]).sum(2))
@@ -349,14 +388,31 @@ class NumpyOracle:
         hWo = recon(hb, grads[1], self.wc, self.Cf[self.wf])
         out = np.where(xsW > 0, self.w[None] * xsW * gWo, 0.0).sum(1)
         rhoW = out / np.abs(self.inc)
-        Mw = rhoW[:, None] * self._maxwell(self.Uw, self.Tw)
-        gW = np.where(xsW > 0, gWo, Mw)
-        hW = np.where(xsW > 0, hWo, Mw * (self.R * self.Tw)[:, None] * (self.K + 3 - self.D))
+        k = self.kind[:, None]
+        Tpos = np.where(self.Tw > 0, self.Tw, 1.0)
+        hfac = (self.R * Tpos)[:, None] * (self.K + 3 - self.D)
+        Mw = rhoW[:, None] * self._maxwell(self.Uw, Tpos)
+        Mf = self.rhob[:, None] * self._maxwell(self.U[self.wc], Tpos)  # farField / pressure incoming
+        sym = (k == 7) | (k == 8)
+        out_ = np.where(sym, xsW > -1e-300, xsW > 0)
+        rows = np.arange(len(self.wc))[:, None]
+        gM, hM = gWo[rows, self.mirror], hWo[rows, self.mirror]
+        gIn = np.select([k == 1, k == 3, (k >= 4) & (k <= 6)], [Mw, self.mixG, Mf], gM)
+        hIn = np.select([k == 1, k == 3, (k >= 4) & (k <= 6)], [Mw * hfac, self.mixH, Mf * hfac], hM)
+        inc = np.where(sym, self.inS0, ~out_)
+        gW = np.where(inc, gIn, gWo)
+        hW = np.where(inc, hIn, hWo)
+        zg = k == 2
+        gW = np.where(zg, gb[self.wc], gW)
+        hW = np.where(zg, hb[self.wc], hW)
         gF = np.concatenate([gI, gW])
         hF = np.concatenate([hI, hW])
         rF, UF, TF, tF, qF = self._moments(gF, hF, 0.5 * dt)
         b = (0.5 * dt / (2 * tF + 0.5 * dt))[:, None]
         geF, heF = self._shakhov(rF, UF, TF, qF)
+        plane = np.concatenate([np.zeros_like(xsI, bool), np.broadcast_to(k == 8, xsW.shape)])
+        gF = np.where(plane, (1 - b) * gF + b * geF, gF)  # symmetryPlane takes the field assignment
+        hF = np.where(plane, (1 - b) * hF + b * heF, hF)
         relax = np.concatenate([np.ones_like(xsI, bool), xsW > 0])
         gF = np.where(relax, (1 - b) * gF + b * geF, gF)
         hF = np.where(relax, (1 - b) * hF + b * heF, hF)
@@ -372,6 +428,23 @@ class NumpyOracle:
         self.g, self.h = gt, ht
         self.rho, self.U, self.T, self.tau, self.q = self._moments(self.g, self.h, dt)
         self.faces = dict(rho=rF, U=UF, T=TF, q=qF, tau=tF, rhoW=rhoW)
+        # fvDVM::updatePressureInOutBC (fvDVM.C:730-806)
+        R, K = self.R, self.K
+        for i in np.nonzero((self.kind == 5) | (self.kind == 6))[0]:
+            c = self.wc[i]
+            S = self.Sf[self.wf[i]]
+            n = S / np.sqrt((S * S).sum())
+            Ui, Ti, ri, p = self.U[c], self.T[c], self.rho[c], self.pB[i]
+            ai = np.sqrt(R * Ti * (K + 5) / (K + 3))
+            Un = (Ui * n).sum()
+            if self.kind[i] == 5:
+                self.rhob[i] = p / R / self.Tw[i]
+                UnIn = Un + (p - ri * R * Ti) / ri / ai
+            else:
+                self.rhob[i] = ri + (p - ri * R * Ti) / ai / ai
+                self.Tw[i] = p / (R * ri)
+                UnIn = Un + (ri * R * Ti - p) / ri / ai
+            self.Uw[i] = UnIn * n + (Ui - Un * n)
 
     def cell(self):
         return dict(rho=self.rho.copy(), U=self.U.copy(), T=self.T.copy(), q=self.q.copy(),
