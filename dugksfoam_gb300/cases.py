@@ -408,9 +408,7 @@ def cavity3d(n=48, Kn=0.1, nxi=20):
 def channel2d(nx=40, ny=20, Kn=0.1, nxi=16, p_ratio=1.2):
     """2D channel [0,2]x[0,1] in reduced units (R = 1/2, T0 = 1, rho0 = 1, so
     2 R T0 = 1): pressureIn (x = 0) at p_ratio p0, pressureOut (x = 2) at
-    p0 = rho0 R T0, diffuse walls top and bottom.  Reduced units because the
-    pressure patches start at rho_b = 1 (their constructor's value) until the
-    first update (pressureInFvPatchField.C:62-76)."""
+    p0 = rho0 R T0, diffuse walls top and bottom."""
     gas, _ = gas_from_kn(Kn, R=0.5, T0=1.0)
     rho0 = 1.0
     gas["muRef"] = gas["muRef"] / _ * rho0  # mu = rho0 C L mu_bar with this rho0

@@ -151,8 +151,7 @@ int Solver::init(const dugks_case_desc& d) {
         Tw[wf] = d.wall_T[b];
         if (d.bnd_rho) rhoB[wf] = d.bnd_rho[b];
         if (kind == DUGKS_PATCH_PRESSURE_IN || kind == DUGKS_PATCH_PRESSURE_OUT) {
-            // pressureIn/Out ctor: value 1 until the first update (pressureInFvPatchField.C:62-76)
-            rhoB[wf] = 1.0;
+            // rho_b (and T_b, U_b) from the initial macros: launch_pressure_bc below
             pB[wf] = d.patch_pressure[p];
             if (!(pB[wf] > 0)) return fail(DUGKS_ERR_ARG, "patch pressure must be positive");
         }
@@ -329,6 +328,12 @@ int Solver::init(const dugks_case_desc& d) {
     chk(up(a.UF, UF));
     chk(up(a.rhoW, one));
     if (ce != cudaSuccess) return checkCuda(ce, "upload");
+    // the constructor ends with updatePressureInOutBC on the initial macros
+    // (fvDVM.C:1067-1071)
+    if (pressureBc) {
+        launch_pressure_bc(a, stream_);
+        if (int e = checkCuda(cudaStreamSynchronize(stream_), "initial pressure patches")) return e;
+    }
 
     // ---- distributions
     const size_t nCV = (size_t)nC * Vp;

@@ -60,10 +60,11 @@ enum dugks_patch_kind {
                                        Maxwellian of the initial patch rho, U, T          */
     DUGKS_PATCH_FAR_FIELD = 4,      /* "farField" [farField]: incoming DFs
                                        rho_b M(U of the owner cell, T_b)                  */
-    DUGKS_PATCH_PRESSURE_IN = 5,    /* "pressureIn" [farField]; rho_b = p/(R T_b) after
-                                       each step (fvDVM::updatePressureInOutBC)           */
+    DUGKS_PATCH_PRESSURE_IN = 5,    /* "pressureIn" [farField]; rho_b = p/(R T_b) at
+                                       creation and after each step
+                                       (fvDVM::updatePressureInOutBC)                     */
     DUGKS_PATCH_PRESSURE_OUT = 6,   /* "pressureOut" [farField]; rho_b, T_b from p and
-                                       the owner cell after each step                     */
+                                       the owner cell, at creation and after each step    */
     DUGKS_PATCH_SYMMETRY_MOD = 7,   /* "symmetryMod" [DVMsymmetry]: incoming DFs mirror
                                        the outgoing ones                                  */
     DUGKS_PATCH_SYMMETRY_PLANE = 8  /* constraint "symmetryPlane": mirrored incoming DFs  */

@@ -229,6 +229,8 @@ static inline double tau_of(const oracle_t* o, double T, double rho) {
 }
 
 /* -------------------------------------------------------------- set-up */
+static void pressure_bc(oracle_t* o);
+
 void* oracle_create(const oracle_case* c) {
     oracle_t* o = (oracle_t*)xcalloc(1, sizeof(oracle_t));
     const int nC = c->nCells, nF = c->nFaces, nI = c->nInternalFaces, nB = nF - nI;
@@ -456,12 +458,8 @@ void* oracle_create(const oracle_case* c) {
     o->bS0 = (double*)xcalloc(3 * (size_t)nB, sizeof(double));
     if (c->rhob) memcpy(o->rhob, c->rhob, sizeof(double) * nB);
     for (int p = 0; p < c->nPatches; ++p) {
-        const int k = c->patchKind[p];
         for (int i = 0; i < c->patchSize[p]; ++i) {
             const int b = c->patchStart[p] + i - nI;
-            /* pressureIn/Out ctor: value = 1 until the first updatePressureInOutBC
-               (pressureInFvPatchField.C:62-76, pressureOutFvPatchField.C:62-76) */
-            if (k == ORACLE_PATCH_PRESSURE_IN || k == ORACLE_PATCH_PRESSURE_OUT) o->rhob[b] = 1.0;
             if (c->patchPressure) o->pB[b] = c->patchPressure[p];
             for (int d = 0; d < 3; ++d) o->bS0[3 * b + d] = o->Sf[3 * (size_t)c->patchStart[p] + d];
         }
@@ -543,6 +541,9 @@ void* oracle_create(const oracle_case* c) {
     }
     for (int b = 0; b < nB; ++b)
         for (int k = 0; k < 3; ++k) o->UF[3 * (nI + b) + k] = o->Ub[3 * b + k];
+    /* the constructor ends with updatePressureInOutBC on the initial macros
+       (fvDVM.C:1067-1071: "set initial rho in pressureIn/Out BC") */
+    pressure_bc(o);
     return o;
 }
 

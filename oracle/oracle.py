@@ -271,7 +271,6 @@ class NumpyOracle:
         self.Uw = np.array(case["Ub"][wall], float)
         self.Tw = np.array(case["Tb"][wall], float)
         self.rhob = np.array(case.get("rhob", np.zeros(nF - nI))[wall], float)
-        self.rhob[(self.kind == 5) | (self.kind == 6)] = 1.0  # pressure patches start at 1
         S0 = geo["Sf"][first[wall]]
         self.mirror = self._mirrors(S0)  # [nb][nV] mirror DV (symmetry faces)
         self.inS0 = (S0 @ self.xi.T) <= 0
@@ -291,6 +290,7 @@ class NumpyOracle:
         # mixed (rho fixedValue): frozen Maxwellian of the initial patch values
         self.mixG = self.rhob[:, None] * M
         self.mixH = (self.K + 3 - self.D) * self.R * Tpos[:, None] * self.mixG
+        self._pressure_bc()  # the constructor's initial update (fvDVM.C:1067-1071)
 
     def _mirrors(self, S0):
         """round(|n . (symX, symY, symZ)|) per face and DV (fvDVM.C:140-221)."""
@@ -428,7 +428,10 @@ class NumpyOracle:
         self.g, self.h = gt, ht
         self.rho, self.U, self.T, self.tau, self.q = self._moments(self.g, self.h, dt)
         self.faces = dict(rho=rF, U=UF, T=TF, q=qF, tau=tF, rhoW=rhoW)
-        # fvDVM::updatePressureInOutBC (fvDVM.C:730-806)
+        self._pressure_bc()
+
+    def _pressure_bc(self):
+        """fvDVM::updatePressureInOutBC (fvDVM.C:730-806) from the current cell macros."""
         R, K = self.R, self.K
         for i in np.nonzero((self.kind == 5) | (self.kind == 6))[0]:
             c = self.wc[i]
@@ -445,6 +448,7 @@ class NumpyOracle:
                 self.Tw[i] = p / (R * ri)
                 UnIn = Un + (ri * R * Ti - p) / ri / ai
             self.Uw[i] = UnIn * n + (Ui - Un * n)
+
 
     def cell(self):
         return dict(rho=self.rho.copy(), U=self.U.copy(), T=self.T.copy(), q=self.q.copy(),
