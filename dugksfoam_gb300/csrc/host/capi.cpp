@@ -22,6 +22,7 @@ struct dugks_handle {
     std::vector<int32_t> patchStart, patchSize, patchKind;
     std::vector<double> wallU, wallT;  // per boundary face
     std::vector<double> patchPressure; // per patch (pressureIn / pressureOut)
+    std::vector<int32_t> dfCells;      // DFwriteCellList of the case directory
 };
 
 namespace {
@@ -57,7 +58,7 @@ int dugks_create(const dugks_case_desc* desc, dugks_handle** out) {
         int code = DUGKS_OK;
         auto s = dugks::Solver::create(*desc, err, code);
         if (!s) { g_err = err; return code; }
-        auto* h = new dugks_handle{std::move(s), std::string(), {}, {}, {}, {}, {}, {}, {}};
+        auto* h = new dugks_handle{std::move(s), std::string(), {}, {}, {}, {}, {}, {}, {}, {}};
         const int nB = desc->n_faces - desc->n_internal_faces;
         for (int p = 0; p < desc->n_patches; ++p) {
             h->patchNames.push_back("patch" + std::to_string(p));
@@ -103,6 +104,7 @@ int dugks_create_from_case_dir(const char* dir, int32_t precision, dugks_handle*
     d.device = 0;
     int rc = dugks_create(&d, out);
     if (rc == DUGKS_OK) (*out)->patchNames = c.patchNames;
+    if (rc == DUGKS_OK) (*out)->dfCells = c.dfCells;
     if (rc == DUGKS_OK && c.deltaT > 0) (*out)->solver->setDt(c.deltaT);
     return rc;
 }
@@ -119,6 +121,7 @@ int dugks_inspect_case_dir(const char* dir, dugks_case_summary* out) {
     r.n_points = (int32_t)(c.points.size() / 3);
     r.n_cells = c.nCells; r.n_faces = c.nFaces; r.n_internal_faces = c.nInternal;
     r.n_patches = (int32_t)c.patchNames.size();
+    r.n_df_cells = (int32_t)c.dfCells.size();
     for (size_t p = 0; p < c.patchNames.size(); ++p) {
         if (c.patchKind[p] == DUGKS_PATCH_MAXWELL) r.n_wall_faces += c.patchSize[p];
         if (c.patchKind[p] == DUGKS_PATCH_EMPTY) r.n_empty_faces += c.patchSize[p];
@@ -130,6 +133,33 @@ int dugks_inspect_case_dir(const char* dir, dugks_case_summary* out) {
     for (double v : c.T0) r.T_sum += v;
     *out = r;
     return DUGKS_OK;
+}
+
+int dugks_write_df_on_cells(dugks_handle* h, const char* case_dir, const int32_t* cells, int32_t n_cells) {
+    if (!h || !h->solver || !case_dir || (cells && n_cells < 0)) return DUGKS_ERR_ARG;
+    return call(h, [&](dugks::Solver& s) -> int {
+        std::vector<int32_t> ids = cells ? std::vector<int32_t>(cells, cells + n_cells) : h->dfCells;
+        if (ids.empty()) return DUGKS_OK;
+        const int nC = s.mesh().nC;
+        for (int32_t id : ids)
+            if (id < 0 || id >= nC) return s.fail(DUGKS_ERR_ARG, "write_df_on_cells: cell out of range");
+        dugks_info info{};
+        s.info(info);
+        const size_t nV = (size_t)info.n_dv;
+        std::vector<double> g((size_t)nC * nV);
+        if (int e = s.getDist(g.data(), nullptr)) return e;
+        const std::string dir = std::string(case_dir) + "/0";
+        std::error_code ec;
+        std::filesystem::create_directories(dir, ec);
+        if (ec) return s.fail(DUGKS_ERR_IO, "cannot create " + dir + ": " + ec.message());
+        for (int32_t id : ids) {
+            std::string err;
+            const std::string name = "DF" + std::to_string(id);
+            if (!dugks::write_scalar_list(dir + "/" + name, name, g.data() + (size_t)id * nV, (int)nV, err))
+                return s.fail(DUGKS_ERR_IO, err);
+        }
+        return DUGKS_OK;
+    });
 }
 
 int dugks_write_time(dugks_handle* h, const char* case_dir, const char* time_name) {

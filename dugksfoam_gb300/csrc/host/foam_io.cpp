@@ -433,6 +433,19 @@ bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err) {
         return false;
     }
     c.KInner = lastNumber(gp->find("KInner"), v) ? (int)v : 0;
+    // DFwriteCellList (labelList, top level of DVMProperties, fvDVM.C:1067):
+    // the labels inside the parentheses (a leading count is not a label)
+    c.dfCells.clear();
+    if (const Entry* dl = dvm.find("DFwriteCellList")) {
+        int depth = 0;
+        for (const Tok& t : dl->toks) {
+            if (t.p == '(') ++depth;
+            else if (t.p == ')') --depth;
+            else if (t.p == 0 && depth > 0 && toNum(t.s, v)) c.dfCells.push_back((int32_t)v);
+        }
+        for (int32_t id : c.dfCells)
+            if (id < 0 || id >= c.nCells) { err = "DVMProperties: DFwriteCellList holds a cell out of range"; return false; }
+    }
     if (!readListFile(dir + "/constant/Xis", t, pos, err) || !parseScalarList(t, pos, c.xis, err)) { err = "Xis: " + err; return false; }
     if (!readListFile(dir + "/constant/weights", t, pos, err) || !parseScalarList(t, pos, c.weights, err)) {
         err = "weights: " + err; return false;
@@ -457,6 +470,18 @@ void header(std::ostream& o, const char* cls, const std::string& obj) {
       << ";\n    object      " << obj << ";\n}\n\n";
 }
 }  // namespace
+
+bool write_scalar_list(const std::string& path, const std::string& object, const double* v, int n,
+                       std::string& err) {
+    std::ofstream o(path);
+    if (!o) { err = "cannot write " + path; return false; }
+    o.precision(17);
+    header(o, "scalarList", object);
+    o << n << "\n(\n";
+    for (int i = 0; i < n; ++i) o << v[i] << "\n";
+    o << ")\n";
+    return (bool)o;
+}
 
 bool write_vol_field(const std::string& path, const std::string& name, const std::string& dims, int ncomp,
                      const double* internal, int n, const std::vector<PatchOut>& patches, std::string& err) {

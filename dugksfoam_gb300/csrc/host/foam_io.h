@@ -35,12 +35,17 @@ struct FoamCase {
     int KInner = 0;
     std::string macroFlux = "no";
     std::vector<double> xis, weights;
+    std::vector<int32_t> dfCells;                       // DFwriteCellList
     // controlDict
     std::map<std::string, std::string> control;
     double deltaT = 0;
 };
 
 bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err);
+
+// An OpenFOAM scalarList file (class scalarList, 17 significant digits).
+bool write_scalar_list(const std::string& path, const std::string& object, const double* v, int n,
+                       std::string& err);
 
 // One patch of a written vol field: "empty" patches carry no value.
 struct PatchOut {

@@ -66,8 +66,9 @@ def _field(path, cls, obj, dims, internal, patches, vector):
     _write(path, cls, "0", obj, body)
 
 
-def write_case(case, path, delta_t=None, end_time=None):
-    """Write ``case`` (a ``cases.make_case`` dict) as an OpenFOAM case directory."""
+def write_case(case, path, delta_t=None, end_time=None, df_cells=None):
+    """Write ``case`` (a ``cases.make_case`` dict) as an OpenFOAM case directory
+    (``df_cells``: DFwriteCellList of DVMProperties, written as a counted list)."""
     m = case["mesh"]
     pm = os.path.join(path, "constant", "polyMesh")
     pts = np.asarray(m["points"], np.float64)
@@ -120,6 +121,8 @@ def write_case(case, path, delta_t=None, end_time=None):
             f"    omega           {_f(g['omega'])};\n    Tref            Tref [0 0 0 1 0 0 0] {_f(g['Tref'])};\n"
             f"    muRef           muRef [1 -1 -1 0 0 0 0] {_f(g['muRef'])};\n    Pr              {_f(g['Pr'])};\n"
             f"    KInner          {int(g['KInner'])};\n}}\n")
+    if df_cells is not None:
+        body += f"\nDFwriteCellList {len(df_cells)}(" + " ".join(str(int(c)) for c in df_cells) + ");\n"
     _write(os.path.join(path, "constant", "DVMProperties"), "dictionary", "constant", "DVMProperties", body)
     _write(os.path.join(path, "constant", "Xis"), "scalarList", "constant", "Xis", _scalar_list(case["xis"]))
     _write(os.path.join(path, "constant", "weights"), "scalarList", "constant", "weights",

@@ -34,7 +34,7 @@ EXPORTS = [
     "dugks_get_conum", "dugks_get_macros", "dugks_get_face_macros", "dugks_get_wall", "dugks_get_boundary", "dugks_get_residual",
     "dugks_get_dist", "dugks_set_dist", "dugks_checkpoint_size", "dugks_checkpoint_save",
     "dugks_checkpoint_load", "dugks_profile_step", "dugks_launches_per_step", "dugks_macros_noalloc",
-    "dugks_inspect_case_dir", "dugks_write_time",
+    "dugks_inspect_case_dir", "dugks_write_time", "dugks_write_df_on_cells",
     "dugks_objective_value", "dugks_objective_tangent", "dugks_objective_adjoint",
     "dugks_batch_create", "dugks_batch_destroy", "dugks_batch_last_error", "dugks_batch_set_dt", "dugks_batch_step",
     "dugks_batch_synchronize", "dugks_batch_get_macros", "dugks_batch_get_info",
@@ -82,7 +82,7 @@ class CaseSummary(C.Structure):
         ("n_xi_per_dim", C.c_int32), ("KInner", C.c_int32),
         ("xi_max", C.c_double), ("R", C.c_double), ("omega", C.c_double), ("Tref", C.c_double),
         ("muRef", C.c_double), ("Pr", C.c_double), ("delta_t", C.c_double),
-        ("rho_sum", C.c_double), ("T_sum", C.c_double),
+        ("rho_sum", C.c_double), ("T_sum", C.c_double), ("n_df_cells", C.c_int32),
     ]
 
 
@@ -140,6 +140,7 @@ def load_library(path: str | None = None):
     lib.dugks_macros_noalloc.argtypes = [vp] + [vp] * 6
     lib.dugks_inspect_case_dir.argtypes = [C.c_char_p, C.POINTER(CaseSummary)]
     lib.dugks_write_time.argtypes = [vp, C.c_char_p, C.c_char_p]
+    lib.dugks_write_df_on_cells.argtypes = [vp, C.c_char_p, _ip, C.c_int32]
     op = C.POINTER(ObjectiveDesc)
     lib.dugks_objective_value.argtypes = [vp, op, _dp]
     lib.dugks_objective_tangent.argtypes = [vp, op, _dp, C.c_double, _dp, _dp]
@@ -362,6 +363,16 @@ class FvDVM:
         g = np.ascontiguousarray(g, np.float64)
         h = None if h is None else np.ascontiguousarray(h, np.float64)
         self._check(self._lib.dugks_set_dist(self._h, _d(g), _d(h)))
+
+    def writeDFonCells(self, case_dir, cells=None):
+        """fvDVM::writeDFonCells: case_dir/0/DF<id> with g~ of each cell (cells=None:
+        the case directory's DFwriteCellList)."""
+        if cells is None:
+            rc = self._lib.dugks_write_df_on_cells(self._h, str(case_dir).encode(), None, 0)
+        else:
+            ids = np.ascontiguousarray(cells, np.int32)
+            rc = self._lib.dugks_write_df_on_cells(self._h, str(case_dir).encode(), _i(ids), len(ids))
+        self._check(rc)
 
     def write(self, case_dir, time_name):
         """runTime.write(): rho, U, T, q, qSurf, stressSurf into case_dir/time_name (dugksFoam.C:81)."""

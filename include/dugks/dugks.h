@@ -231,8 +231,16 @@ typedef struct dugks_case_summary {
     int32_t n_xi_per_dim, KInner;
     double xi_max, R, omega, Tref, muRef, Pr, delta_t;
     double rho_sum, T_sum;          /* sums of the 0/rho and 0/T internal fields */
+    int32_t n_df_cells;             /* length of DVMProperties DFwriteCellList   */
 } dugks_case_summary;
 int dugks_inspect_case_dir(const char* case_dir, dugks_case_summary* out);
+
+/* fvDVM::writeDFonCells (fvDVM.C:820-882, called by dugksFoam.C:78 at output
+ * times): for each cell id, the file <case_dir>/0/DF<id> (an OpenFOAM
+ * scalarList of n_dv values) holding g~ of that cell over the velocity set.
+ * cells == NULL takes DFwriteCellList of the case directory the handle was
+ * created from (nothing to do when it has none). */
+int dugks_write_df_on_cells(dugks_handle* h, const char* case_dir, const int32_t* cells, int32_t n_cells);
 
 /* runTime.write() of dugksFoam.C:81: write the current fields into
  * <case_dir>/<time_name>/ in OpenFOAM ASCII (17 significant digits):

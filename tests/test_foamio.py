@@ -94,3 +94,20 @@ def test_reference_demo_case(built_lib):
     for k in ("R", "omega", "Tref", "muRef", "Pr"):
         v = float(re.search(rf"\n\s*{k}\s[^;]*?([-+0-9.eE]+)\s*;", dvm).group(1))
         assert s[k] == v, k
+
+
+def test_df_write_cell_list_is_read(built_lib, tmp_path):
+    """DFwriteCellList of DVMProperties (fvDVM.C:1067), counted or plain list;
+    a cell out of range is an error."""
+    from dugksfoam_gb300 import foamio, solver
+
+    case = _case()
+    foamio.write_case(case, tmp_path, df_cells=[0, 5, 17])
+    assert solver.inspect_case_dir(tmp_path)["n_df_cells"] == 3
+    dvm = tmp_path / "constant" / "DVMProperties"
+    dvm.write_text(dvm.read_text().replace("DFwriteCellList 3(0 5 17);", "DFwriteCellList (4 9);"))
+    assert solver.inspect_case_dir(tmp_path)["n_df_cells"] == 2
+    dvm.write_text(dvm.read_text().replace("DFwriteCellList (4 9);", "DFwriteCellList (4 100000);"))
+    with pytest.raises(solver.DugksError) as e:
+        solver.inspect_case_dir(tmp_path)
+    assert e.value.code == 2  # DUGKS_ERR_IO

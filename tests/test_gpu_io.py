@@ -75,3 +75,32 @@ def test_write_time_round_trip(built_lib, tmp_path):
     assert info["n_cells"] == s.nCells
     r.close()
     s.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_write_df_on_cells(built_lib, tmp_path, precision):
+    """fvDVM::writeDFonCells: 0/DF<id> holds g~ of the cell over the velocity
+    set, the case's DFwriteCellList by default or an explicit list."""
+    import re
+
+    from dugksfoam_gb300 import cases, foamio, solver
+
+    case = _case()
+    foamio.write_case(case, tmp_path, delta_t=cases.stable_dt(case), df_cells=[3, 42])
+    s = solver.FvDVM.from_case_dir(tmp_path, precision=precision)
+    s.evolution(4)
+    s.writeDFonCells(tmp_path)
+    s.writeDFonCells(tmp_path, cells=[7])
+    g, _ = s.dist()
+
+    def read(cid):
+        t = (tmp_path / "0" / f"DF{cid}").read_text()
+        body = t[t.index("}") + 1:]
+        n = int(re.search(r"\b(\d+)\s*\(", body).group(1))
+        vals = np.array([float(x) for x in body[body.index("(") + 1:body.rindex(")")].split()])
+        assert len(vals) == n == g.shape[1]
+        return vals
+
+    for cid in (3, 42, 7):
+        assert np.array_equal(read(cid), g[cid]), cid
+    s.close()
