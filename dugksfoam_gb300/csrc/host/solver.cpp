@@ -92,6 +92,7 @@ int Solver::init(const dugks_case_desc& d) {
 
     // ---- DV set, fvDVM::initialiseDV (fvDVM.C:140-221)
     const int M = d.n_xi_per_dim;
+    nXiPerDim_ = M;
     nV_ = D == 3 ? M * M * M : (D == 2 ? M * M : M);
     const int granule = pipeline_ == DUGKS_PIPE_FUSED ? fused_dv_granule(precision_) : 8;
     Vp_ = (nV_ + granule - 1) / granule * granule;
@@ -670,6 +671,9 @@ void Solver::info(dugks_info& o) const {
     o.n_dv = nV_; o.n_dv_padded = Vp_; o.n_solution_d = mesh_.D; o.has_h = hasH_;
     o.precision = precision_; o.pipeline = pipeline_; o.dt = dt_; o.step_count = steps_;
     o.device_bytes = bytes_ + (fused_ ? fused_->bytes() : 0);
+    o.n_xi_per_dim = nXiPerDim_; o.KInner = base_.K;
+    o.xi_max = xiMax_; o.R = base_.R; o.omega = base_.omega; o.Tref = base_.Tref; o.muRef = base_.muRef;
+    o.Pr = base_.Pr;
 }
 
 template double* Solver::dalloc<double>(size_t);

@@ -79,7 +79,7 @@ private:
     std::string err_;
     int device_ = 0, sms_ = 132;
     int precision_ = DUGKS_FP64, pipeline_ = DUGKS_PIPE_REFERENCE;
-    int nV_ = 0, Vp_ = 0, hasH_ = 1;
+    int nV_ = 0, Vp_ = 0, hasH_ = 1, nXiPerDim_ = 0;
     double dt_ = 0.0, xiMax_ = 0.0, gscale_ = 1.0;
     int64_t steps_ = 0;
     cudaStream_t ownStream_ = nullptr, stream_ = nullptr;

@@ -72,6 +72,8 @@ class Info(C.Structure):
         ("n_wall_faces", C.c_int32), ("n_dv", C.c_int32), ("n_dv_padded", C.c_int32),
         ("n_solution_d", C.c_int32), ("has_h", C.c_int32), ("precision", C.c_int32), ("pipeline", C.c_int32),
         ("dt", C.c_double), ("step_count", C.c_int64), ("device_bytes", C.c_size_t),
+        ("n_xi_per_dim", C.c_int32), ("KInner", C.c_int32), ("xi_max", C.c_double), ("R", C.c_double),
+        ("omega", C.c_double), ("Tref", C.c_double), ("muRef", C.c_double), ("Pr", C.c_double),
     ]
 
 

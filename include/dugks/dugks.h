@@ -115,12 +115,18 @@ typedef struct dugks_case_desc {
 } dugks_case_desc;
 
 typedef struct dugks_info {
+    /* n_wall_faces: every non-empty boundary face (walls and the other types);
+     * dugks_get_face_macros covers the internal faces followed by these */
     int32_t n_cells, n_faces, n_internal_faces, n_wall_faces;
     int32_t n_dv, n_dv_padded, n_solution_d, has_h;
     int32_t precision, pipeline;
     double dt;
     int64_t step_count;
     size_t device_bytes;             /* device memory held by the handle     */
+    /* fvDVM accessors nXiPerDim(), KInner(), xiMax(), R(), omega(), Tref(),
+     * muRef(), Pr() (fvDVMI.H:97-155) */
+    int32_t n_xi_per_dim, KInner;
+    double xi_max, R, omega, Tref, muRef, Pr;
 } dugks_info;
 
 /* fvDVM::fvDVM (fvDVM.C:886-1075): build the engine from an in-memory case.

@@ -104,3 +104,27 @@ def test_write_df_on_cells(built_lib, tmp_path, precision):
     for cid in (3, 42, 7):
         assert np.array_equal(read(cid), g[cid]), cid
     s.close()
+
+
+def test_cpp_mirror_drives_the_engine(built_lib, tmp_path):
+    """A dugksFoam-shaped C++ driver over include/dugks/fvdvm.hpp gives the same
+    fields as the Python binding on the same case directory."""
+    import re
+    import subprocess
+
+    from test_cpp_mirror import build_driver
+
+    from dugksfoam_gb300 import cases, foamio, solver
+
+    case = _case()
+    foamio.write_case(case, tmp_path / "case", delta_t=cases.stable_dt(case))
+    exe = build_driver(built_lib, tmp_path)
+    r = subprocess.run([str(exe), str(tmp_path / "case"), "5"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    m = re.search(r"nXi (\d+) R (\S+) rho0 (\S+) Ux0 (\S+)", r.stdout)
+    s = solver.FvDVM.from_case_dir(tmp_path / "case", precision=0)
+    s.evolution(5)
+    mac = s.macros()
+    assert int(m.group(1)) == s.nDV and float(m.group(2)) == case["gas"]["R"]
+    assert float(m.group(3)) == mac["rho"][0] and float(m.group(4)) == mac["U"][0, 0]
+    s.close()
