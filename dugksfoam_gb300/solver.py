@@ -332,6 +332,50 @@ class FvDVM:
     def tauVol(self):
         return self.macros()["tau"]
 
+    # fvDVMI.H:67-155: face fields (internal faces, then non-empty boundary faces)
+    # and parameters
+    def rhoSurf(self):
+        return self.face_macros()["rho"]
+
+    def Usurf(self):
+        return self.face_macros()["U"]
+
+    def Tsurf(self):
+        return self.face_macros()["T"]
+
+    def qSurf(self):
+        return self.face_macros()["q"]
+
+    def tauSurf(self):
+        return self.face_macros()["tau"]
+
+    def nXi(self):
+        return self.info()["n_dv"]
+
+    def nXiPerDim(self):
+        return self.info()["n_xi_per_dim"]
+
+    def xiMax(self):
+        return self.info()["xi_max"]
+
+    def R(self):
+        return self.info()["R"]
+
+    def omega(self):
+        return self.info()["omega"]
+
+    def Tref(self):
+        return self.info()["Tref"]
+
+    def muRef(self):
+        return self.info()["muRef"]
+
+    def Pr(self):
+        return self.info()["Pr"]
+
+    def KInner(self):
+        return self.info()["KInner"]
+
     def face_macros(self):
         n = self.nFaceMacros
         out = dict(rho=np.empty(n), U=np.empty((n, 3)), T=np.empty(n), q=np.empty((n, 3)), tau=np.empty(n))

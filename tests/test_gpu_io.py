@@ -126,5 +126,7 @@ def test_cpp_mirror_drives_the_engine(built_lib, tmp_path):
     s.evolution(5)
     mac = s.macros()
     assert int(m.group(1)) == s.nDV and float(m.group(2)) == case["gas"]["R"]
+    assert (s.nXi(), s.R(), s.Pr(), s.KInner(), s.nXiPerDim()) == (
+        s.nDV, case["gas"]["R"], case["gas"]["Pr"], 0, len(case["xis"]))
     assert float(m.group(3)) == mac["rho"][0] and float(m.group(4)) == mac["U"][0, 0]
     s.close()
