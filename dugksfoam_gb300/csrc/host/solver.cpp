@@ -211,7 +211,8 @@ int Solver::init(const dugks_case_desc& d) {
                     }
                     const long t = std::lround(std::fabs(n[0] * sx + n[1] * sy + n[2] * sz));
                     if (t < 0 || t >= nV_)
-                        return fail(DUGKS_ERR_UNSUPPORTED, "symmetry patch is not normal to a coordinate axis");
+                        return fail(DUGKS_ERR_UNSUPPORTED, "symmetry patch: mirror velocity index outside the "
+                                                           "velocity set (the patch is not normal to a coordinate axis)");
                     symTab.push_back((int32_t)t);
                 }
             }

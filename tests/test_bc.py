@@ -142,3 +142,43 @@ def test_two_independent_restatements_agree(oracle_lib, name):
     for k in ("rho", "U", "T", "q"):
         einf, el2 = rel_err(cb[k], ca[k])
         assert einf <= 1e-12 and el2 <= 1e-12, (name, k, einf, el2)
+
+
+def _create_rc(desc):
+    import ctypes as C
+
+    from dugksfoam_gb300 import solver
+
+    lib = solver.load_library()
+    h = C.c_void_p()
+    rc = lib.dugks_create(C.byref(desc), C.byref(h))
+    if rc == 0:
+        lib.dugks_destroy(h)
+    return rc, lib.dugks_global_error().decode()
+
+
+def test_boundary_descriptions_are_checked_before_device_use(built_lib):
+    """Host-side checks of the boundary data, before any device call (so they
+    hold without a GPU): pressure patches need patch_pressure, fixedValue and
+    farField need positive rho values, and the fused FP64 sweeps refuse open
+    types."""
+    import numpy as np
+
+    from dugksfoam_gb300 import cases, solver
+
+    d, keep = solver.case_desc(cases.channel2d(8, 4, nxi=8))
+    d.patch_pressure = None
+    rc, msg = _create_rc(d)
+    assert rc == 1 and "patch_pressure" in msg
+
+    box = cases.open_box2d(6, nxi=8)
+    box["rhob"] = np.zeros_like(box["rhob"])
+    d, keep = solver.case_desc(box)
+    rc, msg = _create_rc(d)
+    assert rc == 1 and "rho patch values" in msg
+
+    d, keep = solver.case_desc(cases.half_cavity2d(4, 8, nxi=8), precision=solver.FP64,
+                               pipeline=solver.PIPE_FUSED)
+    rc, msg = _create_rc(d)
+    assert rc == 3 and "plain FP64" in msg
+
