@@ -125,15 +125,30 @@ def test_oracle_1d_tube(oracle_lib):
     assert c["rho"][:mid].mean() > c["rho"][mid:].mean()
 
 
-@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod", "tube"])
+def _box3d():
+    """4^3 hexes, 6^3 velocities: farField (x = 0), symmetryPlane (x = 1),
+    zeroGradient (z = 1), diffuse walls elsewhere."""
+    import math
+
+    from dugksfoam_gb300 import cases
+
+    gas, rho0 = cases.gas_from_kn(0.1)
+    mesh = cases.structured_mesh(4, 4, 4, lz=1.0, two_d=False, patch_defs=[
+        ("ff", "patch", ["x0"], "farField"), ("sym", "symmetryPlane", ["x1"], "symmetryPlane"),
+        ("zg", "patch", ["z1"], "zeroGradient"), ("walls", "wall", ["y0", "y1", "z0"], None)])
+    return cases.make_case(mesh, gas, rho0, 6, 4.0 * math.sqrt(2 * gas["R"] * 273.0), two_d=False, lid_u=0.0,
+                           bvals={"ff": dict(rho=rho0, T=300.0, U=(30.0, 0.0, 0.0)), "zg": dict(T=273.0)})
+
+
+@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod", "tube", "box3d"])
 def test_two_independent_restatements_agree(oracle_lib, name):
     """The C oracle and the vectorised numpy restatement (separate code, separate
-    summation order) of every boundary type and of 1D agree to ~1e-13."""
+    summation order) of every boundary type, in 1D, 2D and 3D, agree to ~1e-13."""
     from conftest import rel_err
     from dugksfoam_gb300 import cases
     from oracle.oracle import NumpyOracle, Oracle
 
-    case = cases.tube1d(30, nxi=12) if name == "tube" else _cases()[name]
+    case = {"tube": lambda: cases.tube1d(30, nxi=12), "box3d": _box3d}.get(name, lambda: _cases()[name])()
     dt = cases.stable_dt(case)
     a, b = Oracle(case), NumpyOracle(case)
     a.step(dt, 20)
