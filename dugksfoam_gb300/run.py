@@ -89,9 +89,10 @@ class OutputClock:
         return False
 
 
-def run(case_dir, precision, max_steps=None, out=sys.stdout):
+def run(case_dir, precision, max_steps=None, out=None):
     from . import solver
 
+    out = out if out is not None else sys.stdout
     cd = read_control_dict(case_dir)
     c = time_controls(cd)
     dvm = solver.FvDVM.from_case_dir(case_dir, precision=precision)
