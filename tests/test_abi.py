@@ -3,7 +3,6 @@ header declares, and fails loudly (no CPU fallback) without a GPU."""
 import os
 import re
 
-import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
