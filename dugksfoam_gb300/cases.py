@@ -405,10 +405,13 @@ def cavity3d(n=48, Kn=0.1, nxi=20):
     return make_case(mesh, gas, rho0, nxi, xi_max, two_d=False)
 
 
-def channel2d(nx=40, ny=20, Kn=0.1, nxi=16, p_ratio=1.2):
+def channel2d(nx=40, ny=20, Kn=0.1, nxi=24, p_ratio=1.2):
     """2D channel [0,2]x[0,1] in reduced units (R = 1/2, T0 = 1, rho0 = 1, so
     2 R T0 = 1): pressureIn (x = 0) at p_ratio p0, pressureOut (x = 2) at
-    p0 = rho0 R T0, diffuse walls top and bottom."""
+    p0 = rho0 R T0, diffuse walls top and bottom.  Long runs need >= 24
+    velocities per direction on [-4, 4]: on 16 the pressureOut feedback
+    (rho_b, T_b from the owner cell's macros) drifts and the run blows up
+    within a few hundred steps (in the oracle and the engine alike)."""
     gas, _ = gas_from_kn(Kn, R=0.5, T0=1.0)
     rho0 = 1.0
     gas["muRef"] = gas["muRef"] / _ * rho0  # mu = rho0 C L mu_bar with this rho0

@@ -197,3 +197,18 @@ def test_boundary_descriptions_are_checked_before_device_use(built_lib):
     rc, msg = _create_rc(d)
     assert rc == 3 and "plain FP64" in msg
 
+
+
+def test_channel_reaches_uniform_mass_flux(oracle_lib):
+    """Pressure-driven channel (pressureIn / pressureOut, diffuse walls) after
+    2000 steps: the mass flux through every cross-section agrees to < 1e-3, so
+    the patch updates of fvDVM.C:730-806 drive a steady flow."""
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import Oracle
+
+    case = cases.channel2d(16, 8, nxi=24)
+    o = Oracle(case)
+    o.step(cases.stable_dt(case), 2000)
+    c = o.cell()
+    flux = (c["rho"] * c["U"][:, 0]).reshape(8, 16).mean(0)
+    assert flux.min() > 0.1 and (flux.max() - flux.min()) / flux.mean() < 1e-3
