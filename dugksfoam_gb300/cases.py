@@ -424,10 +424,11 @@ def channel2d(nx=40, ny=20, Kn=0.1, nxi=24, p_ratio=1.2):
         "inlet": dict(T=1.0, pressure=p_ratio * p0), "outlet": dict(T=1.0, pressure=p0)})
 
 
-def open_box2d(n=24, Kn=0.1, nxi=16, u_in=60.0):
+def open_box2d(n=24, Kn=0.1, nxi=28, u_in=60.0):
     """2D box with one patch of each open type: farField at x = 0 (rho0, 300 K),
     zeroGradient at x = 1, fixedValue (mixed) at y = 1 moving at u_in, a
-    diffuse wall at y = 0."""
+    diffuse wall at y = 0.  (Like the cavity, long runs on [-4, 4] sqrt(2 R T0)
+    need ~28 velocities per direction; 16 blow up within ~1000 steps.)"""
     gas, rho0 = gas_from_kn(Kn)
     xi_max = 4.0 * math.sqrt(2 * gas["R"] * 273.0)
     mesh = structured_mesh(n, n, 1, two_d=True, patch_defs=[
@@ -438,7 +439,7 @@ def open_box2d(n=24, Kn=0.1, nxi=16, u_in=60.0):
         "outflow": dict(T=273.0)})
 
 
-def half_cavity2d(nx=15, ny=30, Kn=0.075, nxi=16, sym="symmetryPlane"):
+def half_cavity2d(nx=15, ny=30, Kn=0.075, nxi=28, sym="symmetryPlane"):
     """Left half [0,0.5]x[0,1] of the lid-driven cavity with a symmetry patch at
     x = 0.5 (the layout of the reference demo testSymmetry/symmetry):
     ``sym`` = "symmetryPlane" (constraint patch) or "symmetryMod" (DVMsymmetry)."""
