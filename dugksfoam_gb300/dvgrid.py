@@ -19,12 +19,19 @@ Python 3 rewrite of dugksFoam's ``src/scripts/setDV.py`` (Python 2 only):
   (N-1) % 4 == 0 and otherwise uses the highest-order closed composite rule
   whose panel width divides N-1: Simpson 3/8 (3 | N-1), Simpson 1/3
   (2 | N-1), else the trapezoid rule.
+
+Command line (the reference script's interface, ``setDV.py:140-160``), writing
+``constant/Xis`` and ``constant/weights`` of the case in the current directory
+(or ``--case``) as OpenFOAM lists in the same ``% 18.15e`` format:
+
+    python -m dugksfoam_gb300.dvgrid GH 337.196399395 28
+    python -m dugksfoam_gb300.dvgrid NC 1348.0 29
 """
 from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["gauss_hermite_half_range", "newton_cotes", "newton_cotes_rule"]
+__all__ = ["gauss_hermite_half_range", "newton_cotes", "newton_cotes_rule", "write_dv_files", "main"]
 
 
 def gauss_hermite_half_range(C: float, N: int):
@@ -96,3 +103,44 @@ def newton_cotes(xi_max: float, N: int):
     for s in range(0, N - 1, width):
         w[s:s + width + 1] += panel
     return xis, w * dv
+
+
+def _dv_file(obj, values):
+    head = ("FoamFile\n{\n    version     2.0;\n    format      ascii;\n    class       dictionary;\n"
+            f'    location    "constant";\n    object      {obj};\n}}\n\n')
+    return head + f"{len(values)}\n(\n" + "".join("% 18.15e\n" % v for v in values) + ");"
+
+
+def write_dv_files(case_dir, xis, weights):
+    """constant/Xis and constant/weights of ``case_dir`` (the files fvDVM reads)."""
+    import os
+
+    d = os.path.join(case_dir, "constant")
+    os.makedirs(d, exist_ok=True)
+    with open(os.path.join(d, "Xis"), "w") as f:
+        f.write(_dv_file("Xis", xis))
+    with open(os.path.join(d, "weights"), "w") as f:
+        f.write(_dv_file("weights", weights))
+
+
+def main(argv=None):
+    import argparse
+
+    ap = argparse.ArgumentParser(description="Write constant/Xis and constant/weights (setDV.py).")
+    ap.add_argument("rule", choices=["GH", "NC"], help="GH: half-range Gauss-Hermite; NC: Newton-Cotes")
+    ap.add_argument("scale", type=float, help="GH: most probable speed C; NC: largest velocity xi_max")
+    ap.add_argument("n", type=int, help="velocities per direction")
+    ap.add_argument("--case", default=".", help="case directory (default: the current one)")
+    a = ap.parse_args(argv)
+    if a.rule == "GH":
+        if a.n % 2 != 0 or a.n < 7:  # the reference's check (setDV.py:145)
+            ap.error("GH needs an even number of velocities, at least 8")
+        xis, w = gauss_hermite_half_range(a.scale, a.n)
+    else:
+        xis, w = newton_cotes(a.scale, a.n)
+    write_dv_files(a.case, xis, w)
+    return xis, w
+
+
+if __name__ == "__main__":
+    main()

@@ -28,3 +28,18 @@ def test_gauss_hermite_integrates_maxwellian_moments():
     f = np.exp(-(x / C) ** 2) / (np.sqrt(np.pi) * C)
     for k, exact in ((0, 1.0), (2, C * C / 2), (4, 3 * C ** 4 / 4)):
         assert abs((w * f * x ** k).sum() / exact - 1) < 1e-12
+
+
+def test_command_line_writes_files_the_reader_takes(built_lib, tmp_path):
+    """`python -m dugksfoam_gb300.dvgrid GH 337.196399395 28` (the reference's
+    setDV.py interface) writes the demo case's grid; the case reader takes it."""
+    from dugksfoam_gb300 import cases, dvgrid, foamio, solver
+
+    case = cases.cavity2d(n=5, nxi=28)
+    foamio.write_case(case, tmp_path)
+    dvgrid.main(["GH", "337.196399395", "28", "--case", str(tmp_path)])
+    ref = json.load(open(os.path.join(HERE, "golden", "demo_cavity_dv.json")))
+    txt = (tmp_path / "constant" / "Xis").read_text()
+    x = np.array([float(v) for v in txt[txt.index("(") + 1:txt.rindex(")")].split()])
+    assert np.abs(x - np.array(ref["Xis"])).max() / np.abs(x).max() < 1e-13
+    assert solver.inspect_case_dir(tmp_path)["n_xi_per_dim"] == 28
