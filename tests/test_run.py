@@ -54,3 +54,16 @@ def test_loop_writes_time_directories(built_lib, tmp_path, capsys):
     assert [x["step"] for x in lines] == [2, 4, 6] and all(x["U_change"] > 0 for x in lines)
     written = sorted(p.name for p in tmp_path.iterdir() if p.name not in ("0", "constant", "system"))
     assert len(written) == 2 and (tmp_path / "0" / "DF2").exists()
+
+
+@pytest.mark.skipif(not __import__("os").path.isdir("/root/reference/demo/cavity"),
+                    reason="reference demo case not present")
+def test_reference_demo_control_dict():
+    """The reference demo's controlDict: adjustable time step at maxCo 0.8,
+    writes every 1000 steps, 9-digit time names."""
+    from dugksfoam_gb300 import run
+
+    c = run.time_controls(run.read_control_dict("/root/reference/demo/cavity"))
+    assert c["adjust"] and c["max_co"] == 0.8 and c["max_dt"] == 1.0
+    assert (c["dt"], c["end"], c["write_control"], c["write_interval"]) == (4e-4, 200.0, "timeStep", 1000.0)
+    assert c["time_precision"] == 9
