@@ -18,6 +18,13 @@
 // whose work overlaps on the GPU (two streams, two handles) race and must be
 // serialised by the caller.  Each call overwrites every scratch entry it later
 // reads, so nothing has to be cleared between calls.
+//
+// The array belongs to this file's device module: CUDA allocates it when it
+// loads the module (at library load, or at the first call under lazy module
+// loading), never inside a later call.  Its device address is looked up once
+// per device, on the first call with that device current, and cached for the
+// life of the process; a cudaDeviceReset ends the context that holds the
+// array (and every handle's memory with it), so no call may follow a reset.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -125,6 +132,15 @@ int macros_noalloc(const StepArgs& a, int device, cudaStream_t s, const double* 
         err = "dugks_macros_noalloc: " + std::to_string(a.nC) + " cells exceed the scratch limit of " +
               std::to_string(kNoAllocMaxCells) + " cells";
         return DUGKS_ERR_ARG;
+    }
+    if (a.nC == 0) return DUGKS_OK;
+    {  // an error left by the caller's earlier work is not this call's: report it, launch nothing
+        const cudaError_t pending = cudaPeekAtLastError();
+        if (pending != cudaSuccess) {
+            err = std::string("dugks_macros_noalloc: CUDA error pending before the call: ") +
+                  cudaGetErrorString(pending);
+            return DUGKS_ERR_CUDA;
+        }
     }
     double* scratch = nullptr;
     if (int e = scratch_address(device, &scratch, err)) return e;

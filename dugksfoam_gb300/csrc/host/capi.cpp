@@ -349,8 +349,20 @@ int dugks_macros_noalloc(dugks_handle* h, const double* g, const double* hh, dou
                          double* q) {
     return call(h, [&](dugks::Solver& s) -> int {
         std::string err;
-        cudaSetDevice(s.device());
+        int prev = -1;  // the caller's current device, restored before returning
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            cudaGetLastError();
+            return s.fail(DUGKS_ERR_CUDA, "dugks_macros_noalloc: cudaGetDevice failed");
+        }
+        if (prev != s.device()) {
+            const cudaError_t e = cudaSetDevice(s.device());
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                return s.fail(DUGKS_ERR_CUDA, std::string("dugks_macros_noalloc: cudaSetDevice: ") + cudaGetErrorString(e));
+            }
+        }
         const int rc = dugks::macros_noalloc(s.stepArgs(), s.device(), s.stream(), g, hh, rho, U, T, q, err);
+        if (prev != s.device()) cudaSetDevice(prev);
         if (rc != DUGKS_OK) return s.fail(rc, err);
         return DUGKS_OK;
     });

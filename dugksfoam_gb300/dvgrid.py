@@ -131,12 +131,17 @@ def main(argv=None):
     ap.add_argument("scale", type=float, help="GH: most probable speed C; NC: largest velocity xi_max")
     ap.add_argument("n", type=int, help="velocities per direction")
     ap.add_argument("--case", default=".", help="case directory (default: the current one)")
+    ap.add_argument("--allow-other-rules", action="store_true",
+                    help="NC with n != 4Z+1: composite Simpson-3/8, Simpson or trapezoid panels "
+                         "(setDV.py refuses these n)")
     a = ap.parse_args(argv)
     if a.rule == "GH":
         if a.n % 2 != 0 or a.n < 7:  # the reference's check (setDV.py:145)
             ap.error("GH needs an even number of velocities, at least 8")
         xis, w = gauss_hermite_half_range(a.scale, a.n)
     else:
+        if (a.n - 1) % 4 != 0 and not a.allow_other_rules:  # the reference's check (setDV.py:153-156)
+            ap.error("NC needs 4Z+1 velocities per direction (--allow-other-rules for other n)")
         xis, w = newton_cotes(a.scale, a.n)
     write_dv_files(a.case, xis, w)
     return xis, w

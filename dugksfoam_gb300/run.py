@@ -66,6 +66,21 @@ def new_delta_t(dt, co, max_co, max_dt):
     return min(min(min(fact, 1.0 + 0.1 * fact), 1.2) * dt, max_dt)
 
 
+def adjust_to_write_time(dt, t, c, write_index):
+    """Time::adjustDeltaT of OpenFOAM (called by Time::setDeltaT, which
+    setDeltaTvar.H uses): under writeControl adjustableRunTime the step is
+    stretched or shrunk so that a whole number of steps reaches the next
+    write time, by at most 2x up and 5x down."""
+    if c["write_control"] != "adjustableRunTime":
+        return dt
+    to_next = max(0.0, (write_index + 1) * c["write_interval"] - (t - c["start"]))
+    n = to_next / dt - SMALL
+    if n >= 2.0 ** 31 - 1:
+        return dt
+    new = to_next / (int(n) + 1)
+    return min(new, 2.0 * dt) if new >= dt else max(new, 0.2 * dt)
+
+
 def time_name(t, precision=6):
     """Time::timeName in the general format with timePrecision digits."""
     s = f"{t:.{precision}g}"
@@ -99,10 +114,12 @@ def run(case_dir, precision, max_steps=None, out=None):
     dt = c["dt"] if c["dt"] > 0 else dvm.dt
     t, it, uchange = c["start"], 0, 1.0
     clock = OutputClock(c)
-    while t < c["end"] - 1e-12 * max(1.0, abs(c["end"])) and uchange > c["converge_tol"]:
+    # Time::run(): value() < endTime - 0.5 deltaT, with the step of the previous iteration
+    while t < c["end"] - 0.5 * dt and uchange > c["converge_tol"]:
         co, mean_co = dvm.getCoNum()
         if c["adjust"]:
             dt = new_delta_t(dt, co, c["max_co"], c["max_dt"])
+            dt = adjust_to_write_time(dt, t, c, clock.index)
         dvm.set_dt(dt)
         t += dt
         it += 1

@@ -49,8 +49,9 @@ enum dugks_precision {
 
 /* Patch kinds: the rho boundary-condition type of 0/rho
  * (discreteVelocity::setBCtype, discreteVelocity.C:250-300, maps it to the
- * g/h surface patch type given in brackets).  Kinds 2..8 run on the plain FP64
- * pipeline (DUGKS_FP64 with DUGKS_PIPE_REFERENCE or AUTO); the FP32 pipeline
+ * g/h surface patch type given in brackets).  Every kind runs on the plain
+ * FP64 pipeline (DUGKS_FP64 with DUGKS_PIPE_REFERENCE or AUTO) and on the FP32
+ * pipeline (DUGKS_FP32_FP64MOM); the fused FP64 sweeps, the batched kernels
  * and the gradient harness take diffuse walls and empty patches only. */
 enum dugks_patch_kind {
     DUGKS_PATCH_EMPTY = 0,          /* "empty" (2D front/back)                            */
@@ -136,8 +137,10 @@ int dugks_create(const dugks_case_desc* desc, dugks_handle** out);
 
 /* fvDVM::fvDVM from an OpenFOAM case directory: constant/polyMesh/{points,faces,owner,neighbour,boundary},
  * constant/DVMProperties, constant/Xis, constant/weights, 0/{rho,U,T},
- * system/controlDict (deltaT).  rho patch types supported: calculatedMaxwell,
- * empty. */
+ * system/controlDict (deltaT).  rho patch types supported: empty,
+ * calculatedMaxwell, zeroGradient, fixedValue, farField, pressureIn,
+ * pressureOut, symmetryMod and the symmetryPlane constraint (dugks_patch_kind);
+ * any other type fails with DUGKS_ERR_UNSUPPORTED. */
 int dugks_create_from_case_dir(const char* case_dir, int32_t precision, dugks_handle** out);
 
 int dugks_destroy(dugks_handle* h);
@@ -225,8 +228,11 @@ int dugks_launches_per_step(dugks_handle* h, int32_t* n);
  * Scratch is a static device array shared by all calls: at most 262144 cells
  * (larger cases are rejected with DUGKS_ERR_ARG); calls whose work overlaps on
  * the GPU race.  The first call on each device looks up the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture. */
+ * address (cudaGetSymbolAddress) and caches it for the process; make that
+ * first call before any stream capture, and none after a cudaDeviceReset.
+ * The caller's current device is left as it was; a CUDA error pending from
+ * the caller's earlier work is reported (DUGKS_ERR_CUDA) without launching;
+ * n_cells == 0 returns DUGKS_OK without launching. */
 int dugks_macros_noalloc(dugks_handle* h, const double* g, const double* hh, double* rho, double* U, double* T,
                          double* q);
 

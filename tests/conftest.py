@@ -8,6 +8,14 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 
+def reference_path(*parts):
+    """A path inside the reference checkout named by DUGKS_REFERENCE_ROOT, or
+    "" when the variable is unset (tests that read the reference's own demo
+    cases in place skip then)."""
+    root = os.environ.get("DUGKS_REFERENCE_ROOT", "")
+    return os.path.join(root, *parts) if root else ""
+
+
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs through libdugks on cuda:0)")
 

@@ -48,7 +48,9 @@ def _read_list(path):
     return vals
 
 
-def dv(ref_root="/root/reference"):
+def dv(ref_root=None):
+    """The demo case's Xis/weights from the reference checkout (DUGKS_REFERENCE_ROOT)."""
+    ref_root = ref_root or os.environ["DUGKS_REFERENCE_ROOT"]
     d = os.path.join(ref_root, "demo", "cavity", "constant")
     out = dict(C=337.196399395, N=28, Xis=_read_list(os.path.join(d, "Xis")),
                weights=_read_list(os.path.join(d, "weights")),

@@ -9,7 +9,9 @@ import os
 import numpy as np
 import pytest
 
-REF_SYM = "/root/reference/demo/testSymmetry/symmetry"
+from conftest import reference_path
+
+REF_SYM = reference_path("demo", "testSymmetry", "symmetry")
 
 
 def _cases():
@@ -97,7 +99,8 @@ def test_written_cases_read_back(built_lib, tmp_path):
             assert prho[p["name"]][0] == solver.patch_bc(p)
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SYM), reason="reference demo case not present")
+@pytest.mark.skipif(not REF_SYM or not os.path.isdir(REF_SYM),
+                    reason="reference demo case not present (set DUGKS_REFERENCE_ROOT)")
 def test_reference_symmetry_demo_case(built_lib):
     """demo/testSymmetry/symmetry: the left half (30 x 60 quads) of the cavity
     with a symmetryMod (DVMsymmetry) patch of 60 faces at x = 0.5."""

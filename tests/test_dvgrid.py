@@ -4,6 +4,7 @@ import json
 import os
 
 import numpy as np
+import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
@@ -43,3 +44,16 @@ def test_command_line_writes_files_the_reader_takes(built_lib, tmp_path):
     x = np.array([float(v) for v in txt[txt.index("(") + 1:txt.rindex(")")].split()])
     assert np.abs(x - np.array(ref["Xis"])).max() / np.abs(x).max() < 1e-13
     assert solver.inspect_case_dir(tmp_path)["n_xi_per_dim"] == 28
+
+
+def test_command_line_refuses_nc_off_4z_plus_1(tmp_path):
+    """setDV.py refuses NC grids with n != 4Z+1 (setDV.py:153-156); the other
+    composite rules need --allow-other-rules."""
+    from dugksfoam_gb300 import dvgrid
+
+    with pytest.raises(SystemExit):
+        dvgrid.main(["NC", "1348.0", "28", "--case", str(tmp_path)])
+    xis, w = dvgrid.main(["NC", "1348.0", "29", "--case", str(tmp_path)])
+    assert len(xis) == 29
+    xis, w = dvgrid.main(["NC", "1348.0", "28", "--case", str(tmp_path), "--allow-other-rules"])
+    assert len(xis) == 28 and abs(w.sum() - 2 * 1348.0) < 1e-9

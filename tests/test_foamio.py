@@ -8,7 +8,9 @@ import re
 import numpy as np
 import pytest
 
-REF_DEMO = "/root/reference/demo/cavity"
+from conftest import reference_path
+
+REF_DEMO = reference_path("demo", "cavity")
 
 
 def _case():
@@ -76,7 +78,8 @@ def test_missing_field_and_unsupported_bc_are_errors(built_lib, tmp_path):
     assert e.value.code == 3  # DUGKS_ERR_UNSUPPORTED
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_DEMO), reason="reference demo case not present")
+@pytest.mark.skipif(not REF_DEMO or not os.path.isdir(REF_DEMO),
+                    reason="reference demo case not present (set DUGKS_REFERENCE_ROOT)")
 def test_reference_demo_case(built_lib):
     """demo/cavity: 3600 cells, 14520 faces, 7080 internal (owner file note),
     the 28-point velocity grid; gas constants as in its DVMProperties.  Its

@@ -2,8 +2,13 @@
 reading, the damped time-step rule of setDeltaTvar.H and the output clock, on
 the CPU; the loop itself on a GPU."""
 import json
+import os
 
 import pytest
+
+from conftest import reference_path
+
+REF_DEMO = reference_path("demo", "cavity")
 
 
 def test_control_dict_and_defaults(tmp_path):
@@ -56,14 +61,46 @@ def test_loop_writes_time_directories(built_lib, tmp_path, capsys):
     assert len(written) == 2 and (tmp_path / "0" / "DF2").exists()
 
 
-@pytest.mark.skipif(not __import__("os").path.isdir("/root/reference/demo/cavity"),
-                    reason="reference demo case not present")
+@pytest.mark.skipif(not REF_DEMO or not os.path.isdir(REF_DEMO),
+                    reason="reference demo case not present (set DUGKS_REFERENCE_ROOT)")
 def test_reference_demo_control_dict():
     """The reference demo's controlDict: adjustable time step at maxCo 0.8,
     writes every 1000 steps, 9-digit time names."""
     from dugksfoam_gb300 import run
 
-    c = run.time_controls(run.read_control_dict("/root/reference/demo/cavity"))
+    c = run.time_controls(run.read_control_dict(REF_DEMO))
     assert c["adjust"] and c["max_co"] == 0.8 and c["max_dt"] == 1.0
     assert (c["dt"], c["end"], c["write_control"], c["write_interval"]) == (4e-4, 200.0, "timeStep", 1000.0)
     assert c["time_precision"] == 9
+
+
+def test_adjustable_run_time_lands_on_write_times():
+    """Time::adjustDeltaT under adjustableRunTime: the step is reshaped so that
+    a whole number of steps reaches the next write time (2x up, 5x down)."""
+    from dugksfoam_gb300 import run
+
+    c = dict(write_control="adjustableRunTime", write_interval=0.1, start=0.0)
+    assert run.adjust_to_write_time(0.03, 0.0, c, 0) == pytest.approx(0.1 / 4)
+    assert run.adjust_to_write_time(0.03, 0.08, c, 0) == pytest.approx(0.02)
+    assert run.adjust_to_write_time(0.001, 0.0995, c, 0) == pytest.approx(0.0005)
+    assert run.adjust_to_write_time(0.5, 0.0, c, 0) == pytest.approx(0.1)  # shrink at most 5x
+    c2 = dict(c, write_control="timeStep")
+    assert run.adjust_to_write_time(0.03, 0.0, c2, 0) == 0.03
+    # a loop that follows the adjusted step hits every write time exactly
+    t, dt, clock, hits = 0.0, 0.03, run.OutputClock(c), []
+    while t < 0.4 - 0.5 * dt:
+        dt = run.adjust_to_write_time(dt, t, c, clock.index)
+        t += dt
+        if clock(0, t):
+            hits.append(t)
+    assert hits == pytest.approx([0.1, 0.2, 0.3, 0.4], abs=1e-12)
+
+
+def test_run_condition_follows_time_run():
+    """Time::run() is value() < endTime - 0.5 deltaT: a step that does not
+    divide endTime takes no step past it."""
+    t, dt, end, n = 0.0, 0.3, 1.0, 0
+    while t < end - 0.5 * dt:
+        t += dt
+        n += 1
+    assert n == 3
