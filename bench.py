@@ -12,7 +12,10 @@ FP32-bulk / FP64-moment fused pipeline.  A "step" is one fvDVM::evolution()
   e2e        the same metric through the C ABI as dugksFoam's time loop uses
              the engine: per step dugks_get_conum (D2H), dugks_set_dt (H2D),
              dugks_step, dugks_get_macros into pinned host buffers (D2H)
-  fp64_plain the plain FP64 pipeline on the same workload (fewer steps)
+  fp64_plain the plain FP64 pipeline on the same workload (the accuracy run)
+  accuracy   field-normalised L-inf/L2 errors of rho, U, T, q of the FP32 step
+             against the plain FP64 step after --accuracy-steps steps from the
+             same initial state (gate 1e-5)
   roofline   the dominant kernel against measured HBM bandwidth: its
              algorithmic bytes (each array it reads or writes touched once)
              per launch over its CUDA-event launch time; step_frac is the
@@ -54,6 +57,18 @@ def alg_bytes(info):
     nC, nA = info["n_cells"], info["n_internal_faces"] + info["n_wall_faces"]
     return {"k_face_sides": 4 * nd * V * (nC + nA), "k_cell_gather": 4 * nd * V * (2 * nC + nA),
             "k_face_macros": nA * (2 * 16 * 8 + 160)}
+
+
+def rel_err(a, b):
+    """Field-normalised L-inf and L2 errors (vector fields by the magnitude of the difference)."""
+    import numpy as np
+
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    if a.ndim == 2:
+        d, r = np.linalg.norm(a - b, axis=1), np.linalg.norm(b, axis=1)
+    else:
+        d, r = np.abs(a - b), np.abs(b)
+    return {"linf": float(d.max() / r.max()), "l2": float(np.linalg.norm(d) / np.linalg.norm(r))}
 
 
 def _peaks():
@@ -287,8 +302,11 @@ def run_engine(args):
     t_e2e = _allreduce_max(time.perf_counter() - t0, world)
     e2e = n_upd * ek * world / t_e2e
     d2h = sum(a.nbytes for a in hb.values()) + 16
-    # ---- plain FP64 pipeline on the same workload (rank 0 only)
+    # ---- plain FP64 pipeline on the same workload (rank 0 only), then the
+    # accuracy of the FP32 step against it: a fresh FP32 handle and the FP64
+    # handle advance the same number of steps from the same initial state
     fp64 = None
+    accuracy = None
     if rank == 0 and not args.skip_fp64:
         s64 = solver.FvDVM(case, precision=solver.FP64, pipeline=solver.PIPE_REFERENCE, device=local)
         st64 = torch.cuda.Stream()
@@ -296,7 +314,8 @@ def run_engine(args):
         s64.set_dt(dt)
         s64.evolution(1)
         s64.synchronize()
-        k64 = max(2, args.steps // 5)
+        n_acc = max(args.accuracy_steps, 0)
+        k64 = max(2, args.steps // 5, n_acc - 1)
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a0.record(st64)
         s64.evolution(k64)
@@ -305,6 +324,19 @@ def run_engine(args):
         ms64 = a0.elapsed_time(a1)
         fp64 = {"value": n_upd * k64 / (ms64 / 1e3), "ms_per_step": ms64 / k64, "steps": k64,
                 "pipeline": "reference (one FP64 kernel per fvDVM pass)"}
+        if n_acc > 0:
+            m64 = s64.macros()
+            s32 = solver.FvDVM(case, precision=solver.FP32_FP64MOM, pipeline=solver.PIPE_FUSED, device=local)
+            s32.set_dt(dt)
+            s32.evolution(k64 + 1)
+            m32 = s32.macros()
+            s32.close()
+            accuracy = {"steps": k64 + 1, "against": "plain FP64 pipeline, same initial state",
+                        "norm": "field-normalised; vectors by the magnitude of the difference", "gate": 1e-5}
+            for k in ("rho", "U", "T", "q"):
+                accuracy[k] = rel_err(m32[k], m64[k])
+            accuracy["max"] = max(max(accuracy[k].values()) for k in ("rho", "U", "T", "q"))
+            accuracy["pass"] = accuracy["max"] <= accuracy["gate"]
         s64.close()
     if rank != 0:
         return
@@ -340,6 +372,7 @@ def run_engine(args):
         "clocks": clk.summary(),
         "fp64_plain": fp64,
         "speedup_vs_fp64_plain": (value / world / fp64["value"]) if fp64 else None,
+        "accuracy": accuracy,
     }
     s.close()
     if not args.skip_cpu:
@@ -361,6 +394,8 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--accuracy-steps", type=int, default=500,
+                    help="steps of the FP32-vs-FP64 accuracy check after the timed run (0: none)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

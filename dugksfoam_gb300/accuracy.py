@@ -28,23 +28,40 @@ def main(argv=None):
     ap.add_argument("--workload", default="delaunay2d", choices=["delaunay2d", "cavity2d", "cavity3d"])
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--n3d", type=int, default=48)
+    ap.add_argument("--at", default="", help="comma-separated step counts at which to report as well (trajectory)")
+    ap.add_argument("--delaunay-interior", type=int, default=49200)
+    ap.add_argument("--delaunay-side", type=int, default=400)
     a = ap.parse_args(argv)
-    case = {"delaunay2d": lambda: cases.delaunay2d(), "cavity2d": lambda: cases.cavity2d(61, nxi=28),
+    case = {"delaunay2d": lambda: cases.delaunay2d(n_interior=a.delaunay_interior, n_side=a.delaunay_side),
+            "cavity2d": lambda: cases.cavity2d(61, nxi=28),
             "cavity3d": lambda: cases.cavity3d(a.n3d, nxi=20)}[a.workload]()
     dt = cases.case_dt(case)
-    out = dict(workload=a.workload, steps=a.steps, dt=dt)
-    fields = {}
+    marks = sorted({int(x) for x in a.at.split(",") if x} | {a.steps})
+    runs = {}
     for name, prec, pipe in (("fp32", solver.FP32_FP64MOM, solver.PIPE_FUSED), ("fp64", solver.FP64, solver.PIPE_REFERENCE)):
         s = solver.FvDVM(case, precision=prec, pipeline=pipe)
         s.set_dt(dt)
-        t = time.perf_counter()
-        s.evolution(a.steps)
-        fields[name] = s.macros()
-        out[f"seconds_{name}"] = time.perf_counter() - t
-        out["cells"], out["dvs"] = s.nCells, s.nDV
+        runs[name] = s
+    done = 0
+    for n in marks:
+        out = dict(workload=a.workload, steps=n, dt=dt, cells=runs["fp32"].nCells, dvs=runs["fp32"].nDV)
+        fields = {}
+        for name, s in runs.items():
+            t = time.perf_counter()
+            try:
+                s.evolution(n - done)
+                fields[name] = s.macros()
+            except solver.DugksError as e:  # a run that blew up: NaN/Inf or non-positive rho/T
+                out[f"failed_{name}"] = str(e)
+            out[f"seconds_{name}"] = time.perf_counter() - t
+        done = n
+        if len(fields) == 2:
+            out["error_fp32_vs_fp64"] = {k: rel_err(fields["fp32"][k], fields["fp64"][k]) for k in ("rho", "U", "T", "q")}
+        print(json.dumps(out), flush=True)
+        if len(fields) < 2:
+            break
+    for s in runs.values():
         s.close()
-    out["error_fp32_vs_fp64"] = {k: rel_err(fields["fp32"][k], fields["fp64"][k]) for k in ("rho", "U", "T", "q")}
-    print(json.dumps(out), flush=True)
 
 
 if __name__ == "__main__":

@@ -36,6 +36,15 @@
 namespace dugks {
 
 
+// 2^x by the hardware approximation (ex2.approx.ftz.f32, PTX ISA).  Flushing
+// a result below 2^-126 to zero moves an equilibrium value by less than 1e-38
+// of its peak (the grids here reach |xi - U|^2 / 2RT = 48 at T = T0).
+__device__ __forceinline__ float ex2f(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // Packed FP32 pair arithmetic (sm_100+): each lane's NPL velocities are held
 // as NPL/2 float2 pairs and every per-velocity operation is one packed
 // instruction per pair.
@@ -185,7 +194,7 @@ struct Eq32 {
             phi = fma2(cz, f2(qz), phi);
         }
         const float2 t = mul2(c2, f2(kexp));
-        const float2 e = mul2(make_float2(exp2f(t.x), exp2f(t.y)), f2(aA));
+        const float2 e = mul2(make_float2(ex2f(t.x), ex2f(t.y)), f2(aA));
         const float2 c2n = mul2(c2, f2(invRT));
         const float2 ep = mul2(e, phi);
         const float2 ags = fma2(ep, add2(c2n, f2(-(float)(D + 2))), e);

@@ -242,3 +242,25 @@ def test_cavity61_2000_steps_against_golden(built_lib, precision, pipeline, tol)
         einf, el2 = rel_err(got[k], ref[k])
         assert einf <= tol and el2 <= tol, (k, einf, el2)
     s.close()
+
+
+def test_fp32_delaunay24k_500_steps_against_fp64(built_lib):
+    """The headline workload's shape at a quarter of its size (~25k seeded
+    Delaunay triangles, 32x32 velocities, Kn 0.01), 500 steps: the FP32 /
+    FP64-moment step within 1e-5 (L-inf and L2) of the plain FP64 step, whose
+    pipeline the tests above pin to the oracle at 1e-12."""
+    from dugksfoam_gb300 import cases, solver
+
+    case = cases.delaunay2d(n_interior=12300, n_side=200)
+    dt = cases.case_dt(case)
+    out = {}
+    for name, prec, pipe in (("fp32", solver.FP32_FP64MOM, solver.PIPE_FUSED),
+                             ("fp64", solver.FP64, solver.PIPE_REFERENCE)):
+        s = solver.FvDVM(case, precision=prec, pipeline=pipe)
+        s.set_dt(dt)
+        s.evolution(500)
+        out[name] = s.macros()
+        s.close()
+    for k in FIELDS:
+        einf, el2 = rel_err(out["fp32"][k], out["fp64"][k])
+        assert einf <= TOL32 and el2 <= TOL32, (k, einf, el2)
