@@ -307,6 +307,9 @@ def make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=50.0, T0=273.0, Tw
             Tb[s:e] = bv.get("T", T0)
             if "pressure" in bv:
                 p["pressure"] = float(bv["pressure"])
+            for f in ("T", "U"):  # zeroGradient T / U: the patch follows its owner cells
+                if bv.get(f + "_bc"):
+                    p[f + "_bc"] = bv[f + "_bc"]
             continue
         if p["type"] != "wall":
             Tb[s:e] = 0.0
@@ -405,10 +408,12 @@ def cavity3d(n=48, Kn=0.1, nxi=20):
     return make_case(mesh, gas, rho0, nxi, xi_max, two_d=False)
 
 
-def channel2d(nx=40, ny=20, Kn=0.1, nxi=24, p_ratio=1.2):
+def channel2d(nx=40, ny=20, Kn=0.1, nxi=24, p_ratio=1.2, inlet_T_zero_gradient=False):
     """2D channel [0,2]x[0,1] in reduced units (R = 1/2, T0 = 1, rho0 = 1, so
     2 R T0 = 1): pressureIn (x = 0) at p_ratio p0, pressureOut (x = 2) at
-    p0 = rho0 R T0, diffuse walls top and bottom.  Long runs need >= 24
+    p0 = rho0 R T0, diffuse walls top and bottom (``inlet_T_zero_gradient``:
+    the inlet's T is zeroGradient, so rho_b = p/(R T_b) follows the inlet
+    cells' temperature).  Long runs need >= 24
     velocities per direction on [-4, 4]: on 16 the pressureOut feedback
     (rho_b, T_b from the owner cell's macros) drifts and the run blows up
     within a few hundred steps (in the oracle and the engine alike)."""
@@ -421,22 +426,34 @@ def channel2d(nx=40, ny=20, Kn=0.1, nxi=24, p_ratio=1.2):
         ("inlet", "patch", ["x0"], "pressureIn"), ("outlet", "patch", ["x1"], "pressureOut"),
         ("walls", "wall", ["y0", "y1"], None)])
     return make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=0.0, T0=1.0, bvals={
-        "inlet": dict(T=1.0, pressure=p_ratio * p0), "outlet": dict(T=1.0, pressure=p0)})
+        "inlet": dict(T=1.0, pressure=p_ratio * p0, T_bc="zeroGradient" if inlet_T_zero_gradient else None),
+        "outlet": dict(T=1.0, pressure=p0)})
 
 
-def open_box2d(n=24, Kn=0.1, nxi=28, u_in=60.0):
+def open_box2d(n=24, Kn=0.1, nxi=28, u_in=60.0, zero_gradient_tu=False):
     """2D box with one patch of each open type: farField at x = 0 (rho0, 300 K),
     zeroGradient at x = 1, fixedValue (mixed) at y = 1 moving at u_in, a
-    diffuse wall at y = 0.  (Like the cavity, long runs on [-4, 4] sqrt(2 R T0)
-    need ~28 velocities per direction; 16 blow up within ~1000 steps.)"""
+    diffuse wall at y = 0.  ``zero_gradient_tu``: the farField and outflow
+    patches have zeroGradient T and U (the farField's incoming Maxwellian then
+    takes the temperature of its owner cells), and the initial temperature
+    rises linearly from 273 K to 300 K across the box.  (Like the cavity, long
+    runs on [-4, 4] sqrt(2 R T0) need ~28 velocities per direction; 16 blow up
+    within ~1000 steps.)"""
     gas, rho0 = gas_from_kn(Kn)
     xi_max = 4.0 * math.sqrt(2 * gas["R"] * 273.0)
     mesh = structured_mesh(n, n, 1, two_d=True, patch_defs=[
         ("farfield", "patch", ["x0"], "farField"), ("outflow", "patch", ["x1"], "zeroGradient"),
         ("top", "patch", ["y1"], "fixedValue"), ("bottom", "wall", ["y0"], None)])
-    return make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=0.0, bvals={
-        "farfield": dict(rho=rho0, T=300.0), "top": dict(rho=1.1 * rho0, U=(u_in, 0.0, 0.0), T=290.0),
-        "outflow": dict(T=273.0)})
+    zg = "zeroGradient" if zero_gradient_tu else None
+    case = make_case(mesh, gas, rho0, nxi, xi_max, two_d=True, lid_u=0.0, bvals={
+        "farfield": dict(rho=rho0, T=300.0, T_bc=zg, U_bc=zg), "top": dict(rho=1.1 * rho0, U=(u_in, 0.0, 0.0), T=290.0),
+        "outflow": dict(T=273.0, T_bc=zg, U_bc=zg)})
+    if zero_gradient_tu:
+        from .geometry import cell_centres_volumes
+
+        C, _ = cell_centres_volumes(mesh)
+        case["T0"] = 300.0 - 27.0 * C[:, 0]
+    return case
 
 
 def half_cavity2d(nx=15, ny=30, Kn=0.075, nxi=28, sym="symmetryPlane"):

@@ -62,6 +62,10 @@ struct StepArgs {
     const double* bS0;       // [nW][3] area vector of the first face of the face's patch
     const int* symOff;       // [nW] row of symTab for symmetry faces, else -1
     const int* symTab;       // [rows][nV] mirror velocity of each velocity
+    // zeroGradient U / T patches (Uvol_/Tvol_.correctBoundaryConditions,
+    // fvDVM.C:697-699): bit 0 T, bit 1 U per boundary face; zgMask = their OR
+    const int* bZG;          // [nW]
+    int zgMask;
 };
 
 // Boundary kinds (values of dugks_patch_kind in dugks/dugks.h).

@@ -324,10 +324,11 @@ public:
         else {
             kGather_<<<std::min((a.nC + kGatherWarps - 1) / kGatherWarps, gatherBlocks_), kGatherWarps * 32, gatherSmem_,
                        s>>>(A, gatherMF_);
-            if (a.bcMask & ((1 << kBcPressureIn) | (1 << kBcPressureOut))) {
-                StepArgs n = A.b;  // P10 from the macros this step wrote
+            if (a.zgMask || (a.bcMask & ((1 << kBcPressureIn) | (1 << kBcPressureOut)))) {
+                StepArgs n = A.b;  // zeroGradient U/T patches, then P10, from the macros this step wrote
                 n.rho = A.rhoN; n.U = A.UN; n.T = A.TN;
-                launch_pressure_bc(n, s);
+                launch_zero_gradient_tu(n, s);
+                if (a.bcMask & ((1 << kBcPressureIn) | (1 << kBcPressureOut))) launch_pressure_bc(n, s);
             }
         }
     }

@@ -25,6 +25,8 @@ struct RefBuffers {
 void launch_ref_pass(int pass, const StepArgs& a, const RefBuffers& b, int sms, cudaStream_t s);
 // P10 update of pressureIn / pressureOut patch values from the cell macros in a.
 void launch_pressure_bc(const StepArgs& a, cudaStream_t s);
+// zeroGradient U / T patches take their owner cells' values (no-op without any)
+void launch_zero_gradient_tu(const StepArgs& a, cudaStream_t s);
 // Initial face values of mixed (rho fixedValue) patches; once, at creation.
 void launch_ref_mixed_init(const StepArgs& a, const RefBuffers& b, cudaStream_t s);
 

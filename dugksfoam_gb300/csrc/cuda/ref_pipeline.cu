@@ -436,6 +436,20 @@ __global__ void k_pressure(StepArgs a) {
     for (int k = 0; k < 3; ++k) a.UbM[3 * wf + k] = UnIn * n[k] + (Ui[k] - Un * n[k]);
 }
 
+// Uvol_/Tvol_.correctBoundaryConditions() (fvDVM.C:697-699) after the cell
+// macros: a zeroGradient U or T patch takes its owner cell's new value (before
+// P10, which reads T_b on pressureIn patches).
+__global__ void k_zero_gradient_tu(StepArgs a) {
+    const int wf = blockIdx.x * blockDim.x + threadIdx.x;
+    if (wf >= a.nW) return;
+    const int zg = a.bZG[wf];
+    if (!zg) return;
+    const int P = a.own[a.nI + wf];
+    if (zg & 1) a.TbM[wf] = a.T[P];
+    if (zg & 2)
+        for (int k = 0; k < 3; ++k) a.UbM[3 * wf + k] = a.U[3 * P + k];
+}
+
 // Initial face values of mixed patches (rho fixedValue): the Maxwellian of the
 // patch rho, U, T for every DV (discreteVelocity::initBoundaryField,
 // discreteVelocity.C:302-345, equilibriumMaxwell :1046-1061).
@@ -467,6 +481,10 @@ void launch_pressure_bc(const StepArgs& a, cudaStream_t s) {
     if (a.nW > 0) k_pressure<<<(a.nW + 127) / 128, 128, 0, s>>>(a);
 }
 
+void launch_zero_gradient_tu(const StepArgs& a, cudaStream_t s) {
+    if (a.nW > 0 && a.zgMask) k_zero_gradient_tu<<<(a.nW + 127) / 128, 128, 0, s>>>(a);
+}
+
 void launch_ref_mixed_init(const StepArgs& a, const RefBuffers& b, cudaStream_t s) {
     if (a.nW > 0 && (a.bcMask & (1 << kBcFixedValue))) k_mixed_init<<<a.nW, kRedThreads, 0, s>>>(a, b.gS, b.hS);
 }
@@ -492,6 +510,7 @@ void launch_ref_pass(int pass, const StepArgs& a, const RefBuffers& b, int sms, 
         case 6: k_cell<<<grid_for(nCV, kThreads, sms), kThreads, 0, s>>>(a, b.gT, b.hT, b.gB, b.hB, b.gS, b.hS); break;
         case 7:
             k_cell_mom<<<a.nC, kRedThreads, 0, s>>>(a, b.gT, b.hT);
+            if (a.zgMask) k_zero_gradient_tu<<<(a.nW + 127) / 128, 128, 0, s>>>(a);
             if (a.bcMask & ((1 << kBcPressureIn) | (1 << kBcPressureOut)))
                 k_pressure<<<(a.nW + 127) / 128, 128, 0, s>>>(a);
             break;

@@ -22,6 +22,7 @@ struct dugks_handle {
     std::vector<int32_t> patchStart, patchSize, patchKind;
     std::vector<double> wallU, wallT;  // per boundary face
     std::vector<double> patchPressure; // per patch (pressureIn / pressureOut)
+    std::vector<int32_t> patchTzg, patchUzg;  // per patch: T / U zeroGradient
     std::vector<int32_t> dfCells;      // DFwriteCellList of the case directory
 };
 
@@ -58,7 +59,7 @@ int dugks_create(const dugks_case_desc* desc, dugks_handle** out) {
         int code = DUGKS_OK;
         auto s = dugks::Solver::create(*desc, err, code);
         if (!s) { g_err = err; return code; }
-        auto* h = new dugks_handle{std::move(s), std::string(), {}, {}, {}, {}, {}, {}, {}, {}};
+        auto* h = new dugks_handle{std::move(s), std::string(), {}, {}, {}, {}, {}, {}, {}, {}, {}, {}};
         const int nB = desc->n_faces - desc->n_internal_faces;
         for (int p = 0; p < desc->n_patches; ++p) {
             h->patchNames.push_back("patch" + std::to_string(p));
@@ -69,6 +70,12 @@ int dugks_create(const dugks_case_desc* desc, dugks_handle** out) {
         if (desc->wall_U) h->wallU.assign(desc->wall_U, desc->wall_U + 3 * (size_t)nB);
         if (desc->wall_T) h->wallT.assign(desc->wall_T, desc->wall_T + nB);
         if (desc->patch_pressure) h->patchPressure.assign(desc->patch_pressure, desc->patch_pressure + desc->n_patches);
+        h->patchTzg.assign(desc->n_patches, 0);
+        h->patchUzg.assign(desc->n_patches, 0);
+        for (int p = 0; p < desc->n_patches; ++p) {
+            if (desc->patch_T_zero_gradient) h->patchTzg[p] = desc->patch_T_zero_gradient[p];
+            if (desc->patch_U_zero_gradient) h->patchUzg[p] = desc->patch_U_zero_gradient[p];
+        }
         *out = h;
         return DUGKS_OK;
     } catch (const std::exception& e) {
@@ -96,6 +103,7 @@ int dugks_create_from_case_dir(const char* dir, int32_t precision, dugks_handle*
     d.patch_start = c.patchStart.data(); d.patch_size = c.patchSize.data(); d.patch_kind = c.patchKind.data();
     d.wall_U = c.wallU.data(); d.wall_T = c.wallT.data();
     d.bnd_rho = c.bndRho.data(); d.patch_pressure = c.patchPressure.data();
+    d.patch_T_zero_gradient = c.patchTzg.data(); d.patch_U_zero_gradient = c.patchUzg.data();
     d.n_xi_per_dim = c.nDV; d.xis = c.xis.data(); d.weights = c.weights.data(); d.xi_max = c.xiMax;
     d.R = c.R; d.omega = c.omega; d.Tref = c.Tref; d.muRef = c.muRef; d.Pr = c.Pr; d.KInner = c.KInner;
     d.rho0 = c.rho0.data(); d.U0 = c.U0.data(); d.T0 = c.T0.data();
@@ -184,6 +192,9 @@ int dugks_write_time(dugks_handle* h, const char* case_dir, const char* time_nam
             pr[p] = {h->patchNames[p], kRhoType[kind], {}, {}};
             pu[p] = {h->patchNames[p], uT, {}, {}};
             pt[p] = pu[p];
+            // zeroGradient U / T patches are written as such (their value follows the owner)
+            if (!empty && !plane && !h->patchUzg.empty() && h->patchUzg[p]) pu[p].type = "zeroGradient";
+            if (!empty && !plane && !h->patchTzg.empty() && h->patchTzg[p]) pt[p].type = "zeroGradient";
             pq[p] = {h->patchNames[p], calc, {}, {}};
             pqs[p] = pq[p];
             pst[p] = pq[p];

@@ -347,6 +347,8 @@ bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err) {
     c.wallT.assign(nB, 0.0);
     c.bndRho.assign(nB, 0.0);
     c.patchPressure.assign(nP, 0.0);
+    c.patchTzg.assign(nP, 0);
+    c.patchUzg.assign(nP, 0);
     c.rhoBC.clear();
     c.patchKind.clear();
     // rho boundary type -> kind (discreteVelocity::setBCtype, discreteVelocity.C:250-300)
@@ -397,6 +399,12 @@ bool read_foam_case(const std::string& dir, FoamCase& c, std::string& err) {
         const Dict* pu = bU->sub(c.patchNames[p]);
         const Dict* pt = bT->sub(c.patchNames[p]);
         if (!pu || !pt) { err = "0/U or 0/T: no boundary entry for patch " + c.patchNames[p]; return false; }
+        auto isZG = [](const Dict* d) {
+            const Entry* t = d->find("type");
+            return t && !t->toks.empty() && t->toks[0].s == "zeroGradient";
+        };
+        c.patchTzg[p] = isZG(pt) ? 1 : 0;
+        c.patchUzg[p] = isZG(pu) ? 1 : 0;
         std::vector<double> uv, tv;
         const bool needValues = kind == DUGKS_PATCH_MAXWELL;
         if (pu->find("value") || needValues) {

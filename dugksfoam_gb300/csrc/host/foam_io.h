@@ -28,6 +28,7 @@ struct FoamCase {
     std::vector<double> wallU, wallT;                   // U, T patch values per boundary face
     std::vector<double> bndRho;                         // rho patch values per boundary face
     std::vector<double> patchPressure;                  // pressureIn / pressureOut per patch
+    std::vector<int32_t> patchTzg, patchUzg;            // per patch: 0/T, 0/U type zeroGradient
     // DVMProperties
     int nDV = 0;
     double xiMax = 0, xiMin = 0;

@@ -144,12 +144,25 @@ int Solver::init(const dugks_case_desc& d) {
 
     // ---- boundary data and inComingByRho (fvDVM::setCalculatedMaxwellRhoBC, fvDVM.C:263-309)
     std::vector<double> Uw(3 * (size_t)nW), Tw(nW), incAbs(nW, 1.0), rhoB(nW, 0.0), pB(nW, 0.0), bS0(3 * (size_t)nW);
+    std::vector<int> zg(nW, 0);
+    int zgMask = 0;
     for (int wf = 0; wf < nW; ++wf) {
         int b = m.wallFace[wf] - nI;
         const int kind = m.wallKind[wf], p = m.wallPatch[wf];
         for (int k = 0; k < 3; ++k) Uw[3 * wf + k] = d.wall_U[3 * b + k];
         for (int k = 0; k < 3; ++k) bS0[3 * wf + k] = m.Sf[3 * (size_t)d.patch_start[p] + k];
         Tw[wf] = d.wall_T[b];
+        // zeroGradient T / U: the owner cell's initial value (as OpenFOAM constructs
+        // the patch from its field file), updated after every step
+        zg[wf] = (d.patch_T_zero_gradient && d.patch_T_zero_gradient[p] ? 1 : 0) |
+                 (d.patch_U_zero_gradient && d.patch_U_zero_gradient[p] ? 2 : 0);
+        if (zg[wf] && kind == DUGKS_PATCH_MAXWELL)
+            return fail(DUGKS_ERR_UNSUPPORTED, "zeroGradient T or U on a diffuse-wall patch is not supported "
+                                               "(the wall Maxwellian and inComingByRho are fixed at creation)");
+        if (zg[wf] & 1) Tw[wf] = d.T0[m.owner[m.wallFace[wf]]];
+        if (zg[wf] & 2)
+            for (int k = 0; k < 3; ++k) Uw[3 * wf + k] = d.U0[3 * (size_t)m.owner[m.wallFace[wf]] + k];
+        zgMask |= zg[wf];
         if (d.bnd_rho) rhoB[wf] = d.bnd_rho[b];
         if (kind == DUGKS_PATCH_PRESSURE_IN || kind == DUGKS_PATCH_PRESSURE_OUT) {
             // rho_b (and T_b, U_b) from the initial macros: launch_pressure_bc below
@@ -300,10 +313,13 @@ int Solver::init(const dugks_case_desc& d) {
         int* dk = dalloc<int>(nW);
         double *drB = dalloc<double>(nW), *dpB = dalloc<double>(nW), *dS0 = dalloc<double>(bS0.size());
         int *dsO = dalloc<int>(nW), *dsT = dalloc<int>(std::max<size_t>(symTab.size(), 1));
+        int* dzg = dalloc<int>(nW);
         if (oom_) return fail(DUGKS_ERR_OOM, "device allocation failed");
         chk(up(dk, m.wallKind)); chk(up(drB, rhoB)); chk(up(dpB, pB)); chk(up(dS0, bS0)); chk(up(dsO, symOff));
+        chk(up(dzg, zg));
         if (!symTab.empty()) chk(up(dsT, symTab));
         a.bKind = dk; a.rhoB = drB; a.pB = dpB; a.bS0 = dS0; a.symOff = dsO; a.symTab = dsT;
+        a.bZG = dzg; a.zgMask = zgMask;
     }
 
     // initial macros; face velocity = linear interpolation (fvDVM.C:1074) for the first CFL

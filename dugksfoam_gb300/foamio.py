@@ -107,8 +107,10 @@ def write_case(case, path, delta_t=None, end_time=None, df_cells=None):
         else:  # zeroGradient, fixedValue, farField, pressureIn, pressureOut, symmetryMod
             extra = [f"{bc} {_f(p['pressure'])}"] if bc in ("pressureIn", "pressureOut") else []
             prho.append((p["name"], bc, rhob[s:e], *extra))
-            pU.append((p["name"], "fixedValue", Ub[s:e]))
-            pT.append((p["name"], "fixedValue", Tb[s:e]))
+            pU.append((p["name"], "zeroGradient", None) if p.get("U_bc") == "zeroGradient"
+                      else (p["name"], "fixedValue", Ub[s:e]))
+            pT.append((p["name"], "zeroGradient", None) if p.get("T_bc") == "zeroGradient"
+                      else (p["name"], "fixedValue", Tb[s:e]))
     z = os.path.join(path, "0")
     _field(os.path.join(z, "rho"), "volScalarField", "rho", "[1 -3 0 0 0 0 0]", case["rho0"], prho, False)
     _field(os.path.join(z, "U"), "volVectorField", "U", "[0 1 -1 0 0 0 0]", case["U0"], pU, True)

@@ -63,6 +63,7 @@ class CaseDesc(C.Structure):
         ("Pr", C.c_double), ("KInner", C.c_int32),
         ("rho0", _dp), ("U0", _dp), ("T0", _dp),
         ("precision", C.c_int32), ("pipeline", C.c_int32), ("device", C.c_int32),
+        ("patch_T_zero_gradient", _ip), ("patch_U_zero_gradient", _ip),
     ]
 
 
@@ -206,6 +207,8 @@ def case_desc(case, precision=FP64, pipeline=PIPE_AUTO, device=0):
         Tb=np.ascontiguousarray(case["Tb"], np.float64),
         rhob=np.ascontiguousarray(case.get("rhob", np.zeros(len(case["Tb"]))), np.float64),
         pp=np.ascontiguousarray([p.get("pressure", 0.0) for p in m["patches"]], np.float64),
+        tzg=np.array([1 if p.get("T_bc") == "zeroGradient" else 0 for p in m["patches"]], np.int32),
+        uzg=np.array([1 if p.get("U_bc") == "zeroGradient" else 0 for p in m["patches"]], np.int32),
         xis=np.ascontiguousarray(case["xis"], np.float64),
         w=np.ascontiguousarray(case["weights"], np.float64),
         rho0=np.ascontiguousarray(case["rho0"], np.float64),
@@ -223,6 +226,7 @@ def case_desc(case, precision=FP64, pipeline=PIPE_AUTO, device=0):
         xi_max=float(case["xi_max"]), R=g["R"], omega=g["omega"], Tref=g["Tref"], muRef=g["muRef"],
         Pr=g["Pr"], KInner=int(g["KInner"]), rho0=_d(keep["rho0"]), U0=_d(keep["U0"]), T0=_d(keep["T0"]),
         precision=int(precision), pipeline=int(pipeline), device=int(device),
+        patch_T_zero_gradient=_i(keep["tzg"]), patch_U_zero_gradient=_i(keep["uzg"]),
     )
     return d, keep
 

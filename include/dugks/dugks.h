@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define DUGKS_ABI_VERSION 2
+#define DUGKS_ABI_VERSION 3
 
 typedef struct dugks_handle dugks_handle;
 
@@ -113,6 +113,15 @@ typedef struct dugks_case_desc {
     int32_t precision;               /* dugks_precision                      */
     int32_t pipeline;                /* dugks_pipeline                       */
     int32_t device;                  /* CUDA device ordinal                  */
+    /* ABI version 3: per patch, 1 when the T (U) boundary condition is
+     * zeroGradient, else 0; NULL: none.  Such a patch takes the owner cells'
+     * initial values at creation and their new values after every step
+     * (Tvol_/Uvol_.correctBoundaryConditions(), fvDVM.C:697-699), before the
+     * pressure-patch update; a farField or pressureIn patch then uses that T
+     * for its incoming Maxwellian (and pressureIn for rho_b = p/(R T_b)).
+     * Refused (DUGKS_ERR_UNSUPPORTED) on diffuse-wall patches. */
+    const int32_t* patch_T_zero_gradient;
+    const int32_t* patch_U_zero_gradient;
 } dugks_case_desc;
 
 typedef struct dugks_info {

@@ -66,6 +66,7 @@ typedef struct oracle_t {
     double *Ub, *Tb;   /* [nB][3], [nB]  U, T patch values */
     double *rhob, *pB; /* [nB] rho patch values; pressureIn/Out pressure of the face's patch */
     double* bS0;       /* [nB][3] Sf of the first face of the face's patch (symmetry patches) */
+    int* bZG;          /* [nB] bit 0: T patch zeroGradient, bit 1: U patch zeroGradient */
     double *inByRho, *outGoing, *rhoW; /* [nB] */
     double *qWall, *stressWall;        /* [nB][3], [nB][9] */
     double *rho, *U, *T, *q, *tau;     /* cells */
@@ -230,6 +231,7 @@ static inline double tau_of(const oracle_t* o, double T, double rho) {
 
 /* -------------------------------------------------------------- set-up */
 static void pressure_bc(oracle_t* o);
+static void zero_gradient_tu(oracle_t* o);
 
 void* oracle_create(const oracle_case* c) {
     oracle_t* o = (oracle_t*)xcalloc(1, sizeof(oracle_t));
@@ -456,11 +458,13 @@ void* oracle_create(const oracle_case* c) {
     o->rhob = (double*)xcalloc(nB, sizeof(double));
     o->pB = (double*)xcalloc(nB, sizeof(double));
     o->bS0 = (double*)xcalloc(3 * (size_t)nB, sizeof(double));
+    o->bZG = (int*)xcalloc(nB, sizeof(int));
     if (c->rhob) memcpy(o->rhob, c->rhob, sizeof(double) * nB);
     for (int p = 0; p < c->nPatches; ++p) {
         for (int i = 0; i < c->patchSize[p]; ++i) {
             const int b = c->patchStart[p] + i - nI;
             if (c->patchPressure) o->pB[b] = c->patchPressure[p];
+            o->bZG[b] = (c->patchTzg && c->patchTzg[p] ? 1 : 0) | (c->patchUzg && c->patchUzg[p] ? 2 : 0);
             for (int d = 0; d < 3; ++d) o->bS0[3 * b + d] = o->Sf[3 * (size_t)c->patchStart[p] + d];
         }
     }
@@ -504,6 +508,9 @@ void* oracle_create(const oracle_case* c) {
             shakhov(o, o->rho[i], o->U + 3 * i, o->T[i], q0, o->xi + 3 * v,
                     o->gT + (size_t)v * nC + i, o->hT + (size_t)v * nC + i);
 
+    /* a zeroGradient U or T patch, as constructed from its field file, holds
+       the owner cells' initial values */
+    zero_gradient_tu(o);
     /* discreteVelocity::initBoundaryField (discreteVelocity.C:302-345): the
        mixed patches (rho fixedValue) start at the Maxwellian of the patch values;
        their incoming DFs are never written again. */
@@ -553,7 +560,7 @@ void oracle_destroy(void* h) {
     void* ptrs[] = {o->owner, o->neighbour, o->bKind, o->bCell, o->C, o->V, o->Cf, o->Sf, o->pVec, o->nVec,
                     o->bVec, o->dcI, o->dcB, o->nHatB, o->cellOff, o->cellFaces, o->xi, o->w, o->Ub, o->Tb,
                     o->inByRho, o->outGoing, o->rhoW, o->qWall, o->stressWall, o->rho, o->U, o->T, o->q,
-                    o->rhob, o->pB, o->bS0,
+                    o->rhob, o->pB, o->bS0, o->bZG,
                     o->tau, o->rhoF, o->UF, o->TF, o->qF, o->tauF, o->gT, o->hT, o->gB, o->hB, o->Gg, o->Gh,
                     o->gS, o->hS};
     for (size_t i = 0; i < sizeof(ptrs) / sizeof(ptrs[0]); ++i) free(ptrs[i]);
@@ -954,6 +961,19 @@ static void pressure_bc(oracle_t* o) {
     }
 }
 
+/* Uvol_.correctBoundaryConditions(); Tvol_.correctBoundaryConditions()
+   (fvDVM.C:697-699, after the cell macros): a zeroGradient U or T patch takes
+   its owner cell's value, which a farField or pressureIn patch then uses for
+   its incoming Maxwellian and (pressureIn) its density p/(R T_b). */
+static void zero_gradient_tu(oracle_t* o) {
+    for (int b = 0; b < o->nB; ++b) {
+        const int P = o->bCell[b];
+        if (o->bZG[b] & 1) o->Tb[b] = o->T[P];
+        if (o->bZG[b] & 2)
+            for (int k = 0; k < 3; ++k) o->Ub[3 * b + k] = o->U[3 * P + k];
+    }
+}
+
 /* fvDVM::evolution, fvDVM.C:1086-1108 */
 static void evolution(oracle_t* o) {
     const int nV = o->nV, nC = o->nC, nB = o->nB, nI = o->nI, nF = o->nF;
@@ -989,6 +1009,7 @@ static void evolution(oracle_t* o) {
 #pragma omp parallel for schedule(dynamic, 1)
     for (int v = 0; v < nV; ++v) dv_surf_and_tilde(o, v);
     cell_macros(o);
+    zero_gradient_tu(o);
     pressure_bc(o);
 }
 

@@ -51,6 +51,8 @@ typedef struct oracle_case {
     const double* Tb;                    /* [nFaces-nInternalFaces]    T patch values */
     const double* rhob;                  /* [nFaces-nInternalFaces]    rho patch values (may be NULL) */
     const double* patchPressure;         /* [nPatches] pressureIn / pressureOut (may be NULL) */
+    const int* patchTzg;                 /* [nPatches] 1: T boundary condition zeroGradient (may be NULL) */
+    const int* patchUzg;                 /* [nPatches] 1: U boundary condition zeroGradient (may be NULL) */
     int nXiPerDim;
     const double* xis;                   /* [nXiPerDim] 1-D nodes  (constant/Xis) */
     const double* weights;               /* [nXiPerDim] 1-D weights (constant/weights) */

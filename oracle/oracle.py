@@ -39,7 +39,7 @@ class _Case(C.Structure):
         ("nCells", C.c_int), ("nFaces", C.c_int), ("nInternalFaces", C.c_int),
         ("faceOffsets", _ip), ("faceVerts", _ip), ("owner", _ip), ("neighbour", _ip),
         ("nPatches", C.c_int), ("patchStart", _ip), ("patchSize", _ip), ("patchKind", _ip),
-        ("Ub", _dp), ("Tb", _dp), ("rhob", _dp), ("patchPressure", _dp),
+        ("Ub", _dp), ("Tb", _dp), ("rhob", _dp), ("patchPressure", _dp), ("patchTzg", _ip), ("patchUzg", _ip),
         ("nXiPerDim", C.c_int), ("xis", _dp), ("weights", _dp), ("xiMax", C.c_double),
         ("R", C.c_double), ("omega", C.c_double), ("Tref", C.c_double), ("muRef", C.c_double),
         ("Pr", C.c_double), ("KInner", C.c_int),
@@ -97,6 +97,12 @@ def patch_bc(p):
     return {"empty": "empty", "wall": "calculatedMaxwell", "symmetryPlane": "symmetryPlane"}[p["type"]]
 
 
+def patch_zero_gradient(mesh, field):
+    """Per patch: 1 when the boundary condition of ``field`` (U or T) is
+    zeroGradient (patch entry "T_bc"/"U_bc" == "zeroGradient"), else 0."""
+    return np.array([1 if p.get(field + "_bc") == "zeroGradient" else 0 for p in mesh["patches"]], np.int32)
+
+
 def patch_kinds(mesh):
     return np.array([BC_KINDS[patch_bc(p)] for p in mesh["patches"]], np.int32)
 
@@ -123,6 +129,7 @@ class Oracle:
             Tb=np.ascontiguousarray(case["Tb"], np.float64),
             rhob=np.ascontiguousarray(case.get("rhob", np.zeros(len(case["Tb"]))), np.float64),
             pp=np.ascontiguousarray([p.get("pressure", 0.0) for p in m["patches"]], np.float64),
+            tzg=patch_zero_gradient(m, "T"), uzg=patch_zero_gradient(m, "U"),
             xis=np.ascontiguousarray(case["xis"], np.float64),
             w=np.ascontiguousarray(case["weights"], np.float64),
             rho0=np.ascontiguousarray(case["rho0"], np.float64),
@@ -135,7 +142,7 @@ class Oracle:
             faceOffsets=_i(keep["off"]), faceVerts=_i(keep["fv"]), owner=_i(keep["own"]),
             neighbour=_i(keep["nei"]), nPatches=len(keep["ps"]), patchStart=_i(keep["ps"]),
             patchSize=_i(keep["pn"]), patchKind=_i(keep["pk"]), Ub=_d(keep["Ub"]), Tb=_d(keep["Tb"]),
-            rhob=_d(keep["rhob"]), patchPressure=_d(keep["pp"]),
+            rhob=_d(keep["rhob"]), patchPressure=_d(keep["pp"]), patchTzg=_i(keep["tzg"]), patchUzg=_i(keep["uzg"]),
             nXiPerDim=len(keep["xis"]), xis=_d(keep["xis"]), weights=_d(keep["w"]),
             xiMax=float(case["xi_max"]), R=g["R"], omega=g["omega"], Tref=g["Tref"],
             muRef=g["muRef"], Pr=g["Pr"], KInner=int(g["KInner"]),
@@ -250,14 +257,19 @@ class NumpyOracle:
         kinds = np.zeros(nF - nI, np.int32)
         press = np.zeros(nF - nI)
         first = np.zeros(nF - nI, np.int64)
+        zgT = np.zeros(nF - nI, bool)
+        zgU = np.zeros(nF - nI, bool)
         for p in m["patches"]:
             sl = slice(p["startFace"] - nI, p["startFace"] - nI + p["nFaces"])
             kinds[sl] = BC_KINDS[patch_bc(p)]
             press[sl] = p.get("pressure", 0.0)
             first[sl] = p["startFace"]
+            zgT[sl] = p.get("T_bc") == "zeroGradient"
+            zgU[sl] = p.get("U_bc") == "zeroGradient"
         wall = np.nonzero(kinds != PATCH_EMPTY)[0]  # every active boundary face
         self.kind = kinds[wall]
         self.pB = press[wall]
+        self.zgT, self.zgU = zgT[wall], zgU[wall]
         self.wb = wall
         self.wf = nI + wall
         self.wc = np.asarray(m["owner"])[self.wf]
@@ -283,6 +295,7 @@ class NumpyOracle:
         self.tau = self._tau(self.T, self.rho)
         self.Gg = np.zeros((len(wall), len(self.w)))
         self.Gh = np.zeros_like(self.Gg)
+        self._zero_gradient_tu()  # zeroGradient U/T patches start at the owner cells' values
         xs_w = Sw @ self.xi.T
         Tpos = np.where(self.Tw > 0, self.Tw, 1.0)
         M = self._maxwell(self.Uw, Tpos)
@@ -428,7 +441,14 @@ class NumpyOracle:
         self.g, self.h = gt, ht
         self.rho, self.U, self.T, self.tau, self.q = self._moments(self.g, self.h, dt)
         self.faces = dict(rho=rF, U=UF, T=TF, q=qF, tau=tF, rhoW=rhoW)
+        self._zero_gradient_tu()
         self._pressure_bc()
+
+    def _zero_gradient_tu(self):
+        """U/T correctBoundaryConditions (fvDVM.C:697-699): zeroGradient patches
+        take their owner cells' values."""
+        self.Tw = np.where(self.zgT, self.T[self.wc], self.Tw)
+        self.Uw = np.where(self.zgU[:, None], self.U[self.wc], self.Uw)
 
     def _pressure_bc(self):
         """fvDVM::updatePressureInOutBC (fvDVM.C:730-806) from the current cell macros."""

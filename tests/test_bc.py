@@ -22,6 +22,8 @@ def _cases():
         "open_box": cases.open_box2d(10, nxi=8),
         "half_plane": cases.half_cavity2d(6, 12, nxi=8),
         "half_mod": cases.half_cavity2d(6, 12, nxi=8, sym="symmetryMod"),
+        "open_box_zg": cases.open_box2d(10, nxi=8, zero_gradient_tu=True),
+        "channel_zg": cases.channel2d(16, 8, nxi=8, inlet_T_zero_gradient=True),
     }
 
 
@@ -62,6 +64,39 @@ def test_pressure_patches_follow_the_characteristic_update(oracle_lib):
     np.testing.assert_allclose(b["rho"][so], rho_i + (outlet["pressure"] - rho_i * R * T_i) / a2, rtol=1e-14)
     # the pressure difference drives the gas from the inlet to the outlet
     assert c["U"][:, 0].mean() > 0
+
+
+@pytest.mark.parametrize("name", ["open_box_zg", "channel_zg"])
+def test_zero_gradient_t_and_u_follow_the_owner_cells(oracle_lib, name):
+    """Uvol_/Tvol_.correctBoundaryConditions() (fvDVM.C:697-699): after every
+    step a zeroGradient T or U patch holds its owner cells' new values; a
+    pressureIn patch then sets rho_b = p / (R T_b) from them; and the farField
+    or pressureIn inflow differs from the same case with fixed patch values."""
+    from dugksfoam_gb300 import cases
+    from oracle.oracle import Oracle
+
+    case = _cases()[name]
+    dt = cases.stable_dt(case)
+    o = Oracle(case)
+    o.step(dt, 15)
+    m = case["mesh"]
+    nI = len(m["neighbour"])
+    b, c = o.boundary(), o.cell()
+    own = np.asarray(m["owner"])
+    for p in m["patches"]:
+        sl = slice(p["startFace"] - nI, p["startFace"] - nI + p["nFaces"])
+        cells = own[p["startFace"]:p["startFace"] + p["nFaces"]]
+        if p.get("T_bc") == "zeroGradient":
+            assert np.array_equal(b["T"][sl], c["T"][cells]), p["name"]
+            if p.get("bc") == "pressureIn":
+                assert np.array_equal(b["rho"][sl], p["pressure"] / case["gas"]["R"] / b["T"][sl])
+        if p.get("U_bc") == "zeroGradient":
+            assert np.array_equal(b["U"][sl], c["U"][cells]), p["name"]
+    fixed = {k: v for k, v in case.items()}
+    fixed["mesh"] = dict(m, patches=[{k: v for k, v in p.items() if k not in ("T_bc", "U_bc")} for p in m["patches"]])
+    f = Oracle(fixed)
+    f.step(dt, 15)
+    assert np.abs(f.cell()["T"] - c["T"]).max() > 1e-9 * c["T"].max()
 
 
 def test_mixed_patch_keeps_its_incoming_maxwellian(oracle_lib):
@@ -143,7 +178,8 @@ def _box3d():
                            bvals={"ff": dict(rho=rho0, T=300.0, U=(30.0, 0.0, 0.0)), "zg": dict(T=273.0)})
 
 
-@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod", "tube", "box3d"])
+@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod", "tube", "box3d", "open_box_zg",
+                                  "channel_zg"])
 def test_two_independent_restatements_agree(oracle_lib, name):
     """The C oracle and the vectorised numpy restatement (separate code, separate
     summation order) of every boundary type, in 1D, 2D and 3D, agree to ~1e-13."""

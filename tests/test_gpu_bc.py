@@ -2,7 +2,9 @@
 pipeline through the C ABI against the FP64 oracle on pressure-driven channel
 flow (pressureIn / pressureOut), an open box (farField, zeroGradient, rho
 fixedValue -> mixed, one wall) and the half cavity with a symmetryPlane or a
-symmetryMod (DVMsymmetry) patch, on symmetric velocity grids.
+symmetryMod (DVMsymmetry) patch, on symmetric velocity grids; the open box and
+the channel again with zeroGradient T and U patches, whose values follow their
+owner cells after every step (fvDVM.C:697-699).
 
 Tolerance: <= 1e-12 field-normalised (L-inf and L2) on rho, U, T, q after 40
 steps, and on the face macros and the boundary patch values (patch velocities
@@ -27,10 +29,13 @@ def _cases():
         "open_box": cases.open_box2d(14, nxi=12),
         "half_plane": cases.half_cavity2d(8, 16, nxi=12),
         "half_mod": cases.half_cavity2d(8, 16, nxi=12, sym="symmetryMod"),
+        # zeroGradient T / U on farField, zeroGradient and pressureIn patches
+        "open_box_zg": cases.open_box2d(14, nxi=12, zero_gradient_tu=True),
+        "channel_zg": cases.channel2d(24, 12, nxi=12, inlet_T_zero_gradient=True),
     }
 
 
-@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod"])
+@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod", "open_box_zg", "channel_zg"])
 def test_fp64_boundary_types_match_oracle(built_lib, oracle_lib, name):
     from dugksfoam_gb300 import cases, solver
     from oracle.oracle import Oracle
@@ -67,7 +72,7 @@ def test_fp64_boundary_types_match_oracle(built_lib, oracle_lib, name):
     s.close()
 
 
-@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod"])
+@pytest.mark.parametrize("name", ["channel", "open_box", "half_plane", "half_mod", "open_box_zg", "channel_zg"])
 def test_fp32_boundary_types_match_oracle(built_lib, oracle_lib, name):
     """FP32 bulk / FP64 moments with zeroGradient, fixedValue, farField, the
     pressure and the symmetry patches: within 1e-5 of the FP64 oracle (the FP32

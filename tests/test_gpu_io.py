@@ -130,3 +130,30 @@ def test_cpp_mirror_drives_the_engine(built_lib, tmp_path):
         s.nDV, case["gas"]["R"], case["gas"]["Pr"], 0, len(case["xis"]))
     assert float(m.group(3)) == mac["rho"][0] and float(m.group(4)) == mac["U"][0, 0]
     s.close()
+
+
+def test_zero_gradient_tu_patches_from_case_dir(built_lib, tmp_path):
+    """zeroGradient T and U patches in 0/T and 0/U: the case-directory reader
+    sets them (the run is bit-identical to the in-memory case that flags them),
+    and dugks_write_time writes them back as zeroGradient."""
+    from dugksfoam_gb300 import cases, foamio, solver
+
+    case = cases.open_box2d(8, nxi=8, zero_gradient_tu=True)
+    dt = cases.stable_dt(case)
+    foamio.write_case(case, tmp_path, delta_t=dt)
+    a = solver.FvDVM.from_case_dir(tmp_path, precision=solver.FP64)
+    b = solver.FvDVM(case, precision=solver.FP64)
+    b.set_dt(dt)
+    a.evolution(6)
+    b.evolution(6)
+    ma, mb = a.macros(), b.macros()
+    for k in ("rho", "U", "T", "q"):
+        assert np.array_equal(ma[k], mb[k]), k
+    a.write(tmp_path, "1e-06")
+    _, pt = foamio.read_vol_field(tmp_path / "1e-06" / "T")
+    _, pu = foamio.read_vol_field(tmp_path / "1e-06" / "U")
+    for name in ("farfield", "outflow"):
+        assert pt[name][0] == "zeroGradient" and pu[name][0] == "zeroGradient", name
+    assert pt["top"][0] == "fixedValue"
+    a.close()
+    b.close()
