@@ -25,15 +25,21 @@ def main(argv=None):
     from . import cases, solver
 
     ap = argparse.ArgumentParser(description=__doc__)
-    ap.add_argument("--workload", default="delaunay2d", choices=["delaunay2d", "cavity2d", "cavity3d"])
+    ap.add_argument("--workload", default="delaunay2d",
+                    choices=["delaunay2d", "cavity2d", "cavity3d", "cavity128", "batch"])
+    ap.add_argument("--instances", default="0-7", help="batch: instance range a-b of the seeded cavities")
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--n3d", type=int, default=48)
     ap.add_argument("--at", default="", help="comma-separated step counts at which to report as well (trajectory)")
     ap.add_argument("--delaunay-interior", type=int, default=49200)
     ap.add_argument("--delaunay-side", type=int, default=400)
+    ap.add_argument("--save", default="", help="directory: write both runs' cell fields at every mark (npz)")
     a = ap.parse_args(argv)
+    if a.workload == "batch":
+        return run_batch(a)
     case = {"delaunay2d": lambda: cases.delaunay2d(n_interior=a.delaunay_interior, n_side=a.delaunay_side),
             "cavity2d": lambda: cases.cavity2d(61, nxi=28),
+            "cavity128": lambda: cases.cavity2d(128, Kn=0.075, nxi=32, bottom_patch=True),
             "cavity3d": lambda: cases.cavity3d(a.n3d, nxi=20)}[a.workload]()
     dt = cases.case_dt(case)
     marks = sorted({int(x) for x in a.at.split(",") if x} | {a.steps})
@@ -57,11 +63,47 @@ def main(argv=None):
         done = n
         if len(fields) == 2:
             out["error_fp32_vs_fp64"] = {k: rel_err(fields["fp32"][k], fields["fp64"][k]) for k in ("rho", "U", "T", "q")}
+        if a.save and fields:
+            import os
+
+            import numpy as np
+
+            os.makedirs(a.save, exist_ok=True)
+            np.savez(os.path.join(a.save, f"{a.workload}_{n}.npz"),
+                     **{f"{k}_{name}": f[k] for name, f in fields.items() for k in ("rho", "U", "T", "q")})
         print(json.dumps(out), flush=True)
         if len(fields) < 2:
             break
     for s in runs.values():
         s.close()
+
+
+def run_batch(a):
+    """The batched cavities (the seeded instances of the batched runner),
+    advanced together by the batched FP32 engine, each against the same case
+    run alone on the plain FP64 pipeline; one JSON line per instance."""
+    from . import cases, solver
+
+    lo, hi = (int(x) for x in a.instances.split("-"))
+    inst = cases.batch_instances(hi + 1, a.steps)[lo:hi + 1]
+    cs = [cases.batch_case(i) for i in inst]
+    dts = [cases.stable_dt(c) for c in cs]
+    b = solver.Batch(cs, autotune=False)
+    for i, dt in enumerate(dts):
+        b.set_dt(i, dt)
+    b.step(a.steps)
+    got = [b.macros(i) for i in range(len(cs))]
+    b.close()
+    for i, c in enumerate(cs):
+        s = solver.FvDVM(c, precision=solver.FP64, pipeline=solver.PIPE_REFERENCE)
+        s.set_dt(dts[i])
+        s.evolution(a.steps)
+        want = s.macros()
+        out = dict(workload="batch", instance=lo + i, N=inst[i]["N"], M=inst[i]["M"], Kn=inst[i]["Kn"],
+                   steps=a.steps, cells=s.nCells, dvs=s.nDV,
+                   error_fp32_vs_fp64={k: rel_err(got[i][k], want[k]) for k in ("rho", "U", "T", "q")})
+        s.close()
+        print(json.dumps(out), flush=True)
 
 
 if __name__ == "__main__":

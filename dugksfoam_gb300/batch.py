@@ -3,7 +3,9 @@ N in 32..128, M x M velocity grids with M in 16..40, Kn log-uniform in
 [0.01, 1], lid 10..100 m/s, Tw 250..350 K), FP32 bulk / FP64 moments,
 advanced together with the batched engine (one launch per pass over all
 cases, two steps per CUDA graph, autotuned DVs per lane and tile cap), and the
-same cases stepped one after another as separate engines for comparison.
+same cases stepped one after another as separate engines, and the persistent
+kernel (every pass and step of every case in one cooperative launch), for
+comparison.
 One JSON line on stdout."""
 from __future__ import annotations
 
@@ -47,6 +49,19 @@ def main(argv=None):
     ms = wall * 1e3  # the batch runs on its own stream: wall time around a synchronised region
     ok = all(float(b.macros(i)["rho"].min()) > 0 for i in range(len(cs)))
     b.close()
+    # the persistent kernel: every pass and step in one cooperative launch
+    p = solver.Batch(cs, persistent=True)
+    for i, dt in enumerate(dts):
+        p.set_dt(i, dt)
+    p.step(4)
+    p.synchronize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    p.step(a.steps)
+    p.synchronize()
+    wall_p = time.perf_counter() - t0
+    ok_p = all(float(p.macros(i)["rho"].min()) > 0 for i in range(len(cs)))
+    p.close()
     # separate engines, one case after another per step
     eng = []
     for i, c in enumerate(cs):
@@ -74,6 +89,8 @@ def main(argv=None):
                      dv_per_lane=info["dv_per_lane"], tile_cap=info["tile_cap"], tuned=info["tuned"],
                      launches_per_step=info["launches_per_step"], steps_per_graph=info["steps_per_graph"],
                      build_and_tune_s=t_build, finite=ok),
+        persistent=dict(ms_per_step=wall_p * 1e3 / a.steps, cell_dv_per_s=cdv * a.steps / wall_p,
+                        launches=1, finite=ok_p),
         separate_engines=dict(ms_per_step=sep * 1e3, cell_dv_per_s=cdv / sep, launches_per_step=3 * a.cases),
         speedup=(sep * 1e3) / (ms / a.steps))), flush=True)
 

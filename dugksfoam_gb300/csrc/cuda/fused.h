@@ -64,11 +64,22 @@ struct BatchLaunch {
     size_t gatherSmem = 0;
     int gatherBlocks = 1;
     int D = 2, H = 1, npl = 4;
+    // persistent kernel (all passes and steps in one cooperative launch)
+    size_t persistSmem = 0;
+    int persistBlocks = 0;
 };
 // Set function attributes and the persistent gather grid; false if the
 // (D, H, npl) combination has no kernels.
 bool fused_batch_prepare(BatchLaunch& L, int sms);
 void fused_batch_launch(int k, const BatchLaunch& L, int sms, cudaStream_t s);
+// The persistent batched kernel: shared memory and the co-resident grid
+// (false if it does not fit), and one cooperative launch of nSteps steps from
+// parity0 (L0 / L1: the launch descriptions of parity 0 / 1).  bar: two
+// zeroed unsigned counters; status receives DUGKS_ERR_TIMEOUT when a grid
+// barrier wait gives up after cap polls.
+bool fused_batch_persistent_prepare(BatchLaunch& L, int sms);
+cudaError_t fused_batch_persistent_launch(const BatchLaunch& L0, const BatchLaunch& L1, int nSteps, int parity0,
+                                          unsigned* bar, long long cap, int* status, cudaStream_t s);
 
 // Allow a kernel the device's opt-in maximum of dynamic shared memory (less
 // its static shared memory).  The limit belongs to the kernel function, which

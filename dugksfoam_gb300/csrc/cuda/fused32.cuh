@@ -27,8 +27,10 @@
 //    (The Mref part of the face flux, Mref xi.sum_f(+-S_f), vanishes for a
 //    closed cell and is not formed.)
 //  * no FP64 instruction runs inside the DV chunk loops (GB300 issues FP64 at
-//    1/64 of the FP32 rate): per-chunk warp totals go into FP32 Kahan pairs
-//    and are finished in FP64, batched so that whole warps do the FP64 work.
+//    1/64 of the FP32 rate): the face sweep's per-chunk warp totals go into
+//    FP32 Kahan pairs per face side; the gather keeps per-lane FP32 partial
+//    sums over all chunks of a cell and reduces them across the warp once;
+//    both are finished in FP64, batched so that whole warps do the FP64 work.
 #pragma once
 
 #include "fused_impl.cuh"
@@ -1062,8 +1064,10 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
     const float4 u4 = reinterpret_cast<const float4*>(cblk)[0];
     const float ur[3] = {u4.x, u4.y, u4.z};
     const float kv = -A.dt * A.invVf[c];
-    Acc<float> acc;
-    acc.zero();
+    // cell moments: per-lane partial sums over all chunks, one warp reduction per cell
+    float m[NS];
+#pragma unroll
+    for (int s2 = 0; s2 < NS; ++s2) m[s2] = 0.0f;
     const int nChunks = Vp / KC;
     issue(0, 0);
     for (int ch = 0; ch < nChunks; ++ch) {
@@ -1087,6 +1091,7 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
             t[p] = fma2(sub2(g, g0[p]), f2(1.0f / 3.0f), g);  // exact when g+ == g~
             th[p] = H ? fma2(sub2(h, h0[p]), f2(1.0f / 3.0f), h) : f2(0.f);
         }
+#pragma unroll 3  // a triangle's three faces: independent relaxations interleave
         for (int e = e0; e < e1; ++e) {
             const int f = e - e0;
             const float4 ent = A.cfEnt[e];
@@ -1153,13 +1158,9 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
         const size_t gi = (size_t)c * Vp + v0 + col;
         stp_cs<NP>(A.gTn + gi, t);
         if (H) stp_cs<NP>(A.hTn + gi, th);
-        float m[NS];
-#pragma unroll
-        for (int s2 = 0; s2 < NS; ++s2) m[s2] = 0.0f;
         mom32<D, H, NPL, NS>(m, L, ur, t, th, nullptr);
-        acc.add(reduce_scatter<NS, float>(m, lane));
     }
-    return acc.value();
+    return (double)reduce_scatter<NS, float>(m, lane);
 }
 
 // Warps stride over the cells (persistent grid); per cell, all DV chunks:
@@ -1234,6 +1235,137 @@ __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32_batch(const FusedA
             __syncwarp();
             nb = 0;
         }
+    }
+}
+
+// ------------------------------------------------- persistent batched step
+// Grid-wide barrier of a cooperative launch (every block resident): an
+// arrival counter bar[0] and a generation bar[1] in global memory (zeroed
+// before the launch).  A wait polls at most `cap` times; then it sets
+// *status = DUGKS_ERR_TIMEOUT (6) and the barrier returns false in every
+// block that reaches it afterwards, so all blocks leave the kernel.  Callers
+// reach it only with no asynchronous copy in flight.
+constexpr int kStatusTimeout = 6;
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, long long cap, int* status) {
+    __shared__ int sOk;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vb = bar;
+        int ok = 1;
+        const unsigned gen = vb[1];
+        __threadfence();
+        if (atomicAdd(bar, 1u) == gridDim.x - 1) {  // last to arrive: reset, release the others
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            long long it = 0;
+            while (vb[1] == gen) {
+                if (++it > cap) {
+                    ok = 0;
+                    atomicExch(status, kStatusTimeout);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        if (*(volatile int*)status == kStatusTimeout) ok = 0;
+        sOk = ok;
+    }
+    __syncthreads();
+    return sOk != 0;
+}
+
+// Cells finished per warp batch in the persistent kernel's gather pass.
+constexpr int kPersistBatch = 16;
+
+// Dynamic shared memory of the persistent kernel's gather pass: the warps'
+// row stages, their case-argument copies, slot totals and cell / case ids.
+template <int D, bool H>
+__host__ __device__ inline size_t persist_gather_smem(int nw, int mf, int kc) {
+    return gather_smem(nw, mf, kc, H) + (size_t)nw * sizeof(FusedArgs<float>) +
+           (size_t)nw * kPersistBatch * Slots<D, H>::NS * sizeof(double) + 2 * (size_t)nw * kPersistBatch * sizeof(int);
+}
+
+// Several independent cases, nSteps whole steps in one cooperative launch:
+// per step the face-side tiles of all cases (blocks stride over the work
+// list), a grid barrier, the face macros of all cases (threads stride over
+// the faces), a barrier, the cell gather of all cases (warps stride over the
+// cells), a barrier.  Step s uses the argument arrays of parity
+// (parity0 + s) & 1 (double buffers swapped).  The pass bodies are those of
+// the single-case kernels.
+template <int D, bool H, int NPL, int NW>
+__global__ void __launch_bounds__(NW * 32, 1)
+    k_batch_persistent32(const FusedArgs<float>* __restrict__ AA0, const FusedArgs<float>* __restrict__ AA1,
+                         const int2* __restrict__ work, int nWork, const int* __restrict__ faceOff,
+                         const int* __restrict__ cellOff, int nCases, int MF, int nSteps, int parity0, unsigned* bar,
+                         long long cap, int* status) {
+    using SL = Slots<D, H>;
+    constexpr int NS = SL::NS, KC = 32 * NPL, NR = H ? 2 : 1;
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ FusedArgs<float> sA;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    constexpr int W8 = (int)(sizeof(FusedArgs<float>) / 8);
+    static_assert(sizeof(FusedArgs<float>) % 8 == 0, "argument block is copied in 8-byte words");
+    // gather-pass carve-up of the dynamic shared memory
+    float* gsm = reinterpret_cast<float*>(smem);
+    const size_t stBytes = gather_smem(NW, MF, KC, H);
+    FusedArgs<float>* sAw = reinterpret_cast<FusedArgs<float>*>(smem + stBytes);
+    double* sM = reinterpret_cast<double*>(smem + stBytes + NW * sizeof(FusedArgs<float>));
+    int* sC = reinterpret_cast<int*>(sM + (size_t)NW * kPersistBatch * NS);
+    int* sI = sC + NW * kPersistBatch;
+    float* wb = gsm + (size_t)warp * 2 * (1 + MF) * NR * KC + lane * NPL;
+    const int myslot = slot_of<NS>(lane);
+    const bool writer = NS == 16 ? (lane & 1) == 0 : true;
+    const int totalFaces = faceOff[nCases], totalCells = cellOff[nCases];
+    for (int s = 0; s < nSteps; ++s) {
+        const FusedArgs<float>* AA = ((parity0 + s) & 1) ? AA1 : AA0;
+        // ---- face sides (P1-P3 and the per-side face moments)
+        for (int w = blockIdx.x; w < nWork; w += gridDim.x) {
+            const int2 wk = work[w];
+            const long long* src = reinterpret_cast<const long long*>(AA + wk.x);
+            long long* dst = reinterpret_cast<long long*>(&sA);
+            for (int k = threadIdx.x; k < W8; k += blockDim.x) dst[k] = src[k];
+            __syncthreads();
+            face_sides_body<D, H, NPL, NW, false>(sA, wk.y, smem);
+            __syncthreads();
+        }
+        if (!grid_barrier(bar, cap, status)) return;
+        // ---- face macros (P4-P6)
+        for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < totalFaces; g += gridDim.x * blockDim.x) {
+            const int i = case_of(faceOff, nCases, g);
+            face_macros_one<D, H>(AA[i], g - faceOff[i]);
+        }
+        if (!grid_barrier(bar, cap, status)) return;
+        // ---- cell gather (P7-P9)
+        int nb = 0, cur = -1;
+        const int TW = gridDim.x * NW;
+        for (int g = blockIdx.x * NW + warp; g < totalCells; g += TW) {
+            const int i = case_of(cellOff, nCases, g), c = g - cellOff[i];
+            if (i != cur) {
+                const long long* src = reinterpret_cast<const long long*>(AA + i);
+                long long* dst = reinterpret_cast<long long*>(sAw + warp);
+                __syncwarp();
+                for (int k = lane; k < W8; k += 32) dst[k] = src[k];
+                __syncwarp();
+                cur = i;
+            }
+            const double tot = gather_cell<D, H, NPL>(sAw[warp], c, MF, wb, lane);
+            double* mw = sM + ((size_t)warp * kPersistBatch + nb) * NS;
+            if (writer) mw[myslot] = tot;
+            if (lane == 0) { sC[warp * kPersistBatch + nb] = c; sI[warp * kPersistBatch + nb] = i; }
+            ++nb;
+            if (nb == kPersistBatch || g + TW >= totalCells) {
+                __syncwarp();
+                if (lane < nb)
+                    finalize_cell32<D, H>(AA[sI[warp * kPersistBatch + lane]], sC[warp * kPersistBatch + lane],
+                                          sM + ((size_t)warp * kPersistBatch + lane) * NS);
+                __syncwarp();
+                nb = 0;
+            }
+        }
+        if (!grid_barrier(bar, cap, status)) return;
     }
 }
 

@@ -13,6 +13,8 @@ void Batch::release() {
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
     for (auto& g : single_)
         if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+    bar_ = nullptr;
+    tstatus_ = nullptr;  // freed with dev_
     for (auto e : ev_) cudaEventDestroy(e);
     ev_.clear();
     for (auto st : side_) cudaStreamDestroy(st);
@@ -34,7 +36,8 @@ int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap, int 
     npl_ = npl;
     tileCap_ = tileCap;
     perCase_ = groups == 0;  // every case its own graph branch with its own kernels
-    groups_ = perCase_ ? n : std::max(1, std::min(groups, n));
+    persistent_ = groups < 0;  // one cooperative launch for all passes and steps
+    groups_ = perCase_ ? n : (persistent_ ? 1 : std::max(1, std::min(groups, n)));
     if (int e = check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "stream")) return e;
     for (int g = 1; g < groups_; ++g) {
         cudaStream_t st = nullptr;
@@ -157,9 +160,21 @@ int Batch::prepare() {
             L.H = a0.hasH;
             L.npl = npl_;
             if (!fused_batch_prepare(L, sms_)) return fail(DUGKS_ERR_UNSUPPORTED, "batch: no kernels for this case shape");
+            if (persistent_ && !fused_batch_persistent_prepare(L, sms_))
+                return fail(DUGKS_ERR_UNSUPPORTED, "batch: the persistent kernel does not fit this case shape");
             // the groups run side by side: share the SMs in the persistent gather grid
             L.gatherBlocks = std::max(1, L.gatherBlocks / groups_);
         }
+    }
+    if (persistent_) {
+        const unsigned zero[2] = {0u, 0u};
+        const int z = 0;
+        bar_ = static_cast<unsigned*>(up(zero, sizeof(zero)));
+        tstatus_ = static_cast<int*>(up(&z, sizeof(z)));
+        if (!bar_ || !tstatus_) return fail(DUGKS_ERR_OOM, "batch: device allocation failed");
+        dirty_ = false;
+        parity_ = 0;
+        return DUGKS_OK;
     }
     for (int q = 0; q < 2; ++q) {
         if (int e = capture(q, 2, graph_[q])) return e;
@@ -207,6 +222,18 @@ int Batch::step(int n) {
         if (!(c->dt() > 0)) return fail(DUGKS_ERR_ARG, "set every case's dt before stepping");
     if (dirty_)
         if (int e = prepare()) return e;
+    if (persistent_) {
+        if (n > 0) {
+            if (int e = check(cudaMemsetAsync(bar_, 0, 2 * sizeof(unsigned), stream_), "barrier reset")) return e;
+            if (int e = check(fused_batch_persistent_launch(L_[0][0], L_[1][0], n, parity_, bar_, waitLimit_, tstatus_,
+                                                           stream_),
+                              "persistent launch"))
+                return e;
+            parity_ ^= n & 1;
+        }
+        for (auto& c : cases_) c->advanceExternal(n);
+        return DUGKS_OK;
+    }
     int left = n;
     while (left >= 2) {
         if (int e = check(cudaGraphLaunch(graph_[parity_], stream_), "graph launch")) return e;
@@ -223,6 +250,14 @@ int Batch::step(int n) {
 
 int Batch::synchronize() {
     if (int e = check(cudaStreamSynchronize(stream_), "batch synchronize")) return e;
+    if (tstatus_) {
+        int st = 0;
+        if (int e = check(cudaMemcpy(&st, tstatus_, sizeof(int), cudaMemcpyDeviceToHost), "batch status")) return e;
+        if (st != 0) {
+            cudaMemset(tstatus_, 0, sizeof(int));
+            return fail(DUGKS_ERR_TIMEOUT, "batch: a grid barrier wait of the persistent kernel gave up");
+        }
+    }
     for (size_t i = 0; i < cases_.size(); ++i)
         if (int e = cases_[i]->synchronize()) return fail(e, "case " + std::to_string(i) + ": " + cases_[i]->error());
     return DUGKS_OK;
@@ -241,9 +276,9 @@ void Batch::info(dugks_batch_info& o) const {
     o.n_cases = (int32_t)cases_.size();
     o.dv_per_lane = npl_;
     o.tile_cap = tileCap_;
-    o.launches_per_step = 3 * groups_;  // kernel nodes per step inside the graph (per case or per group)
-    o.steps_per_graph = 2;
-    o.groups = perCase_ ? 0 : groups_;
+    o.launches_per_step = persistent_ ? 1 : 3 * groups_;  // kernel nodes per step (persistent: one per step call)
+    o.steps_per_graph = persistent_ ? 0 : 2;
+    o.groups = perCase_ ? 0 : (persistent_ ? -1 : groups_);
     o.cells = cells_;
     o.cell_dv = cellDV_;
     o.n_tuned = (int32_t)std::min<size_t>(tuneMs_.size(), 8);
@@ -259,12 +294,14 @@ std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int au
     std::unique_ptr<Batch> b(new Batch());
     code = DUGKS_OK;
     if (!descs || n < 1) { err = "batch: need at least one case"; code = DUGKS_ERR_ARG; return nullptr; }
-    int bestNpl = 4, bestCap = 0, bestGroups = 1;
-    if (autotune) {
+    // autotune 2: the persistent kernel, untuned
+    int bestNpl = 4, bestCap = 0, bestGroups = autotune == 2 ? -1 : 1;
+    if (autotune == 1) {
         // candidates: DVs per lane, cap on cells per tile (0: the largest that
         // fits), concurrent groups
         // (groups 0: every case its own graph branch with its own kernels)
-        const int cand[][3] = {{4, 0, 1}, {4, 0, 4}, {4, 0, 0}, {4, 32, 1}, {2, 0, 1}};
+        // (groups -1: the persistent kernel)
+        const int cand[][3] = {{4, 0, 1}, {4, 0, 4}, {4, 0, 0}, {4, 32, 1}, {2, 0, 1}, {4, 0, -1}};
         double best = 1e300;
         for (auto& c : cand) {
             if (int e = b->build(descs, n, c[0], c[1], c[2])) { err = b->err_; code = e; return nullptr; }
@@ -282,10 +319,11 @@ std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int au
             cudaEventElapsedTime(&ms, e0, e1);
             cudaEventDestroy(e0);
             cudaEventDestroy(e1);
+            if (rc == DUGKS_ERR_UNSUPPORTED && c[2] < 0) continue;  // the persistent kernel does not fit
             if (rc) { err = b->err_; code = rc; return nullptr; }
             b->tuneNpl_.push_back(c[0]);
             b->tuneCap_.push_back(c[1]);
-            b->tuneGroups_.push_back(b->perCase_ ? 0 : b->groups_);
+            b->tuneGroups_.push_back(b->perCase_ ? 0 : (b->persistent_ ? -1 : b->groups_));
             b->tuneMs_.push_back(ms / 6.0);
             if (ms < best) { best = ms; bestNpl = c[0]; bestCap = c[1]; bestGroups = c[2]; }
         }

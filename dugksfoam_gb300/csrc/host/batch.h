@@ -5,7 +5,8 @@
 // one CUDA graph (two steps per graph, replayed), so one group's face sweep
 // overlaps another's cell gather; an autotuner picks the DVs per lane, the
 // tile-size cap and G by timing, or every case as its own branch with its own
-// kernels (G = 0).
+// kernels (G = 0), or the persistent kernel (G = -1): every pass of every
+// step of every case in one cooperative launch with bounded grid barriers.
 #pragma once
 
 #include <memory>
@@ -27,6 +28,8 @@ public:
     int step(int n);
     int synchronize();
     int setDt(int i, double dt);
+    // polls a grid-barrier wait of the persistent kernel makes before it gives up
+    void setWaitLimit(long long polls) { waitLimit_ = polls; }
     Solver& at(int i) { return *cases_[i]; }
     int nCases() const { return (int)cases_.size(); }
     void info(dugks_batch_info& out) const;
@@ -49,6 +52,10 @@ private:
     std::vector<cudaEvent_t> ev_;
     int sms_ = 1, npl_ = 4, tileCap_ = 0, groups_ = 1;
     bool perCase_ = false;
+    bool persistent_ = false;
+    unsigned* bar_ = nullptr;   // persistent kernel: barrier counters
+    int* tstatus_ = nullptr;    // persistent kernel: DUGKS_ERR_TIMEOUT when a barrier wait gave up
+    long long waitLimit_ = 1LL << 24;
     std::vector<StepArgs> base_;       // base step arguments of each case at graph build
     std::vector<BatchLaunch> L_[2];    // per parity, per group
     std::vector<void*> dev_;

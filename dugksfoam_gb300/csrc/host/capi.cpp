@@ -501,5 +501,13 @@ int dugks_batch_get_info(dugks_batch* b, dugks_batch_info* out) {
     });
 }
 
+int dugks_batch_set_wait_limit(dugks_batch* b, int64_t polls) {
+    if (polls < 0) return DUGKS_ERR_ARG;
+    return bcall(b, [&](dugks::Batch& x) -> int {
+        x.setWaitLimit(polls);
+        return DUGKS_OK;
+    });
+}
+
 }  // extern "C"
 

@@ -37,7 +37,7 @@ EXPORTS = [
     "dugks_inspect_case_dir", "dugks_write_time", "dugks_write_df_on_cells",
     "dugks_objective_value", "dugks_objective_tangent", "dugks_objective_adjoint",
     "dugks_batch_create", "dugks_batch_destroy", "dugks_batch_last_error", "dugks_batch_set_dt", "dugks_batch_step",
-    "dugks_batch_synchronize", "dugks_batch_get_macros", "dugks_batch_get_info",
+    "dugks_batch_synchronize", "dugks_batch_get_macros", "dugks_batch_get_info", "dugks_batch_set_wait_limit",
 ]
 
 
@@ -157,6 +157,7 @@ def load_library(path: str | None = None):
     lib.dugks_batch_synchronize.argtypes = [vp]
     lib.dugks_batch_get_macros.argtypes = [vp, C.c_int32] + [_dp] * 4
     lib.dugks_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+    lib.dugks_batch_set_wait_limit.argtypes = [vp, C.c_int64]
     _lib = lib
     return lib
 
@@ -485,9 +486,10 @@ class FvDVM:
 class Batch:
     """Independent 2D cases advanced together (dugks_batch_*): one launch per
     pass over all cases, two steps per CUDA graph, autotuned DVs per lane and
-    tile cap.  Every case uses the FP32 / FP64-moment pipeline."""
+    tile cap; or (``persistent=True``) every pass of every step in one
+    cooperative launch.  Every case uses the FP32 / FP64-moment pipeline."""
 
-    def __init__(self, case_list, autotune=True, device=0):
+    def __init__(self, case_list, autotune=True, device=0, persistent=False):
         self._lib = load_library()
         self._h = C.c_void_p()
         descs, self._keep = [], []
@@ -496,7 +498,8 @@ class Batch:
             descs.append(d)
             self._keep.append(k)
         arr = (CaseDesc * len(descs))(*descs)
-        rc = self._lib.dugks_batch_create(arr, len(descs), int(bool(autotune)), C.byref(self._h))
+        mode = 2 if persistent else int(bool(autotune))
+        rc = self._lib.dugks_batch_create(arr, len(descs), mode, C.byref(self._h))
         if rc != 0:
             raise DugksError(rc, self._lib.dugks_global_error().decode())
         self.cells = [int(c["mesh"]["n_cells"]) for c in case_list]
@@ -521,6 +524,10 @@ class Batch:
 
     def step(self, n):
         self._check(self._lib.dugks_batch_step(self._h, int(n)))
+
+    def set_wait_limit(self, polls):
+        """Polls a grid-barrier wait of the persistent kernel makes before giving up."""
+        self._check(self._lib.dugks_batch_set_wait_limit(self._h, int(polls)))
 
     def synchronize(self):
         self._check(self._lib.dugks_batch_synchronize(self._h))

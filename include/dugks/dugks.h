@@ -300,12 +300,16 @@ int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J
  * Independent 2D cases (uneven meshes and velocity grids) advanced together
  * with the FP32 pipeline: every pass of the step is one launch over all cases,
  * the cases are split into groups whose launch chains are independent
- * branches of one CUDA graph (two steps per graph, replayed).  With
- * autotune != 0 the DVs per lane (2 or 4), the cap on cells per tile and the
- * number of groups (0: every case its own graph branch with its own kernels)
- * are chosen by timing a few steps of each candidate (otherwise 4 DVs per
- * lane, no cap, one group).  Each case starts from its own initial state;
- * set each case's dt before stepping. */
+ * branches of one CUDA graph (two steps per graph, replayed); or the
+ * persistent kernel (groups -1): every pass of every step of every case in
+ * one cooperative launch per dugks_batch_step, the passes separated by
+ * grid-wide barriers whose waits give up after a bounded number of polls
+ * (dugks_batch_synchronize then returns DUGKS_ERR_TIMEOUT).  autotune 1: the
+ * DVs per lane (2 or 4), the cap on cells per tile and the number of groups
+ * (0: every case its own graph branch with its own kernels; -1: persistent)
+ * are chosen by timing a few steps of each candidate; 0: 4 DVs per lane, no
+ * cap, one group; 2: the persistent kernel.  Each case starts from its own
+ * initial state; set each case's dt before stepping. */
 typedef struct dugks_batch dugks_batch;
 typedef struct dugks_batch_info {
     int32_t n_cases, dv_per_lane, tile_cap, groups, launches_per_step /* kernel nodes per step */, steps_per_graph,
@@ -323,6 +327,9 @@ int dugks_batch_step(dugks_batch* b, int32_t nsteps);      /* asynchronous */
 int dugks_batch_synchronize(dugks_batch* b);
 int dugks_batch_get_macros(dugks_batch* b, int32_t i, double* rho, double* U, double* T, double* q);
 int dugks_batch_get_info(dugks_batch* b, dugks_batch_info* out);
+/* Polls a grid-barrier wait of the persistent kernel makes before it gives up
+ * (default 2^24, about a second); 0 makes every wait that has to wait give up. */
+int dugks_batch_set_wait_limit(dugks_batch* b, int64_t polls);
 
 #ifdef __cplusplus
 }
