@@ -157,3 +157,12 @@ template void launch_import_dist<double>(const StepArgs&, const double*, double*
 template void launch_import_dist<float>(const StepArgs&, const double*, float*, double, int, cudaStream_t);
 
 }  // namespace dugks
+
+// 1 when this library was compiled with the device-side index checks.
+extern "C" int dugks_checked_build(void) {
+#if defined(DUGKS_CHECKED) && DUGKS_CHECKED
+    return 1;
+#else
+    return 0;
+#endif
+}

@@ -73,6 +73,26 @@ constexpr int kBcEmpty = 0, kBcMaxwell = 1, kBcZeroGradient = 2, kBcFixedValue =
               kBcPressureIn = 5, kBcPressureOut = 6, kBcSymmetryMod = 7, kBcSymmetryPlane = 8;
 
 #ifdef __CUDACC__
+// Index check of the checked build (compiled with -DDUGKS_CHECKED=1, the
+// library libdugks_checked.so): an index read from mesh or tile data that is
+// outside [0, n) sets the status word to DUGKS_ERR_BOUNDS (8) and is replaced
+// by 0, so the access stays inside the array and the step finishes; the host
+// reports the error at the next synchronising call.  In the normal build it
+// is the index itself.
+constexpr int kStatusBounds = 8;
+__device__ __forceinline__ int chk(int i, int n, int* status) {
+#if defined(DUGKS_CHECKED) && DUGKS_CHECKED
+    if ((unsigned)i >= (unsigned)n) {
+        atomicExch(status, kStatusBounds);
+        return 0;
+    }
+#else
+    (void)n;
+    (void)status;
+#endif
+    return i;
+}
+
 __device__ __forceinline__ void shakhov_ref(double rho, double Ux, double Uy, double Uz, double T,
                                             double qx, double qy, double qz, double xx, double xy,
                                             double xz, double R, double Pr, int D, int K, double& gEq,

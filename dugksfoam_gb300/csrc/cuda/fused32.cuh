@@ -136,6 +136,37 @@ __device__ __forceinline__ TileMeta32 stage_meta(const FusedArgs<float>& A, cons
     return m;
 }
 
+#if defined(DUGKS_CHECKED) && DUGKS_CHECKED
+// Checked build: every index of a staged tile block within its range (rows
+// of T u H1, faces, walls, stencil entries, cells); an index outside is
+// replaced by 0 in the staged copy and reported (chk).
+template <int NT>
+__device__ void check_tile_meta32(const FusedArgs<float>& A, const TileHdr& hd, unsigned char* at) {
+    int4* sm = reinterpret_cast<int4*>(at);
+    int* st = A.b.status;
+    for (int k = threadIdx.x; k < hd.nFB; k += NT) {
+        int4& r = sm[5 * k];  // {ownL, neiL, a, w}
+        r.x = chk(r.x, hd.nT2, st);
+        if (r.y >= 0) r.y = chk(r.y, hd.nT2, st);
+        r.z = chk(r.z, A.b.nA, st);
+        if (r.w >= 0) r.w = chk(r.w, A.b.nW, st);
+        int4& e = sm[5 * k + 1];  // stencil ranges, tile-relative
+        e.x = chk(e.x, hd.nEnt + 1, st); e.y = chk(e.y, hd.nEnt + 1, st);
+        e.z = chk(e.z, hd.nEnt + 1, st); e.w = chk(e.w, hd.nEnt + 1, st);
+    }
+    float4* E = reinterpret_cast<float4*>(sm + 5 * hd.nFB);
+    for (int k = threadIdx.x; k < hd.nEnt; k += NT) {
+        const int o = __float_as_int(E[k].w);
+        const int ok = o >= 0 ? chk(o, hd.nT2, st) : -1 - chk(-o - 1, A.b.nW, st);
+        E[k].w = __int_as_float(ok);
+    }
+    int* C = reinterpret_cast<int*>(sm + 5 * hd.nFB + hd.nEnt);
+    for (int k = threadIdx.x; k < hd.nT2; k += NT) C[k] = chk(C[k], A.b.nC, st);
+    int* S = reinterpret_cast<int*>(sm + 5 * hd.nFB + hd.nEnt + (hd.nT2 + 3) / 4);
+    for (int k = threadIdx.x; k <= hd.nT; k += NT) S[k] = chk(S[k], hd.nEnt + 1, st);
+}
+#endif
+
 // Equilibrium table entry {U, kexp} {1/RT, q'} {a, a A, RT, 0} from a
 // coefficient block and the relaxation weight a.
 __device__ __forceinline__ void eq_table(float4* q, const float* blk, float a) {
@@ -663,6 +694,10 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
     float4* sU = tm.dyn;            // [nFB] face Uref
     float4* ceq = tm.dyn + hd.nFB;  // [nT2][3] cell equilibria
     __syncthreads();
+#if defined(DUGKS_CHECKED) && DUGKS_CHECKED
+    check_tile_meta32<NW * 32>(A, hd, smem + LY::meta(hd.nT2, hd.nFB, hd.nT));
+    __syncthreads();
+#endif
     for (int i = threadIdx.x; i < hd.nFB; i += NW * 32) sU[i] = A.uref4[tm.F[5 * i].z];
     for (int i = threadIdx.x; i < hd.nT2; i += NW * 32) {
         const float* blk = A.cc + (size_t)tm.C[i] * kNCoef;
@@ -849,7 +884,7 @@ __global__ void k_open_faces32(FusedArgs<float> A) {
     for (int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < b.nW; w += gridDim.x * (blockDim.x >> 5)) {
         const int kind = b.bKind[w];
         if (kind == kBcMaxwell) continue;  // warp-uniform
-        const int a = b.nI + w, own = b.own[a];
+        const int a = b.nI + w, own = chk(b.own[a], b.nC, b.status);
         const float sx = (float)b.Sf[3 * a], sy = (float)b.Sf[3 * a + 1], sz = (float)b.Sf[3 * a + 2];
         const float4 u4 = A.uref4[a];
         const float ur[3] = {u4.x, u4.y, u4.z};
@@ -900,11 +935,11 @@ __global__ void k_open_faces32(FusedArgs<float> A) {
                 for (int j = 0; j < NPL; ++j) {
                     const int v = v0 + col + j;
                     if (v >= b.nV || !incoming(v)) continue;
-                    int cur = v, u = tab[v];
+                    int cur = v, u = chk(tab[v], b.nV, b.status);
                     if (kind == kBcSymmetryPlane)
                         for (int guard = 0; guard < b.nV && u < cur && incoming(u); ++guard) {
                             cur = u;
-                            u = tab[u];
+                            u = chk(tab[u], b.nV, b.status);
                         }
                     gs[j] = snG[u];
                     if (H) hs[j] = snH[u];
@@ -1047,7 +1082,7 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
         cp_async_row(st, A.gT + gi, NPL);
         if (H) cp_async_row(st + KC, A.hT + gi, NPL);
         for (int f = 0; f < nfs; ++f) {
-            const int a = __float_as_int(A.cfEnt[e0 + f].w);
+            const int a = chk(__float_as_int(A.cfEnt[e0 + f].w), b.nA, b.status);
             const size_t fi = (size_t)a * Vp + v0 + col;
             cp_async_row(st + (1 + f) * NR * KC, A.gF + fi, NPL);
             if (H) cp_async_row(st + ((1 + f) * NR + 1) * KC, A.hF + fi, NPL);
@@ -1095,7 +1130,7 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
         for (int e = e0; e < e1; ++e) {
             const int f = e - e0;
             const float4 ent = A.cfEnt[e];
-            const int a = __float_as_int(ent.w);
+            const int a = chk(__float_as_int(ent.w), b.nA, b.status);
             float2 gf[NP], hf[NP];
             if (f < nfs) {
                 ldp<NP>(gf, st + (1 + f) * NR * KC);

@@ -65,9 +65,9 @@ __global__ void k_grad(StepArgs a, const double* __restrict__ gB, const double* 
         const double gc = gB[i];
         const double hc = a.hasH ? hB[i] : 0.0;
         for (int j = a.cellOff[c]; j < a.cellOff[c + 1]; ++j) {
-            int e = a.cellFace[j], f = e >> 1, side = e & 1;
+            int e = a.cellFace[j], f = chk(e >> 1, a.nA, a.status), side = e & 1;
             if (f < a.nI) {
-                int o = a.own[f], nb = a.nei[f];
+                int o = chk(a.own[f], a.nC, a.status), nb = chk(a.nei[f], a.nC, a.status);
                 double dg = gB[(long long)nb * Vp + v] - gB[(long long)o * Vp + v];
                 double dh = a.hasH ? hB[(long long)nb * Vp + v] - hB[(long long)o * Vp + v] : 0.0;
                 const double* L = side ? a.nVec + 3 * f : a.pVec + 3 * f;
@@ -95,7 +95,7 @@ __global__ void k_grad(StepArgs a, const double* __restrict__ gB, const double* 
             if (a.hasH) hG[((long long)c * D + k) * Vp + v] = h[k];
         }
         for (int j = a.cellOff[c]; j < a.cellOff[c + 1]; ++j) {
-            int f = a.cellFace[j] >> 1;
+            int f = chk(a.cellFace[j] >> 1, a.nA, a.status);
             if (f < a.nI) continue;
             int wf = f - a.nI;
             const double* nh = a.nHatW + 3 * wf;
@@ -130,7 +130,7 @@ __global__ void k_recon(StepArgs a, const double* __restrict__ gB, const double*
         const double* dO = a.dO + 3 * f;
         if (f < a.nI) {
             const double* dN = a.dN + 3 * f;
-            int o = a.own[f], nb = a.nei[f];
+            int o = chk(a.own[f], a.nC, a.status), nb = chk(a.nei[f], a.nC, a.status);
             if (xs >= kVSmall) {
                 gS[i] = recon(gB, gG, o, v, Vp, D, dO, xi, a.dt);
                 if (a.hasH) hS[i] = recon(hB, hG, o, v, Vp, D, dO, xi, a.dt);
@@ -143,7 +143,7 @@ __global__ void k_recon(StepArgs a, const double* __restrict__ gB, const double*
                     hS[i] = 0.5 * (recon(hB, hG, nb, v, Vp, D, dN, xi, a.dt) + recon(hB, hG, o, v, Vp, D, dO, xi, a.dt));
             }
         } else {
-            const int wf = f - a.nI, kind = a.bKind[wf], o = a.own[f];
+            const int wf = f - a.nI, kind = a.bKind[wf], o = chk(a.own[f], a.nC, a.status);
             if (kind == kBcZeroGradient) {  // gSurf == gBarPvol patchInternalField, every DV
                 gS[i] = gB[(long long)o * Vp + v];
                 if (a.hasH) hS[i] = hB[(long long)o * Vp + v];
@@ -350,7 +350,7 @@ __global__ void k_cell(StepArgs a, double* __restrict__ gT, double* __restrict__
         double g = -1.0 / 3 * gT[i] + 4.0 / 3 * gB[i];
         double h = a.hasH ? -1.0 / 3 * hT[i] + 4.0 / 3 * hB[i] : 0.0;
         for (int j = a.cellOff[c]; j < a.cellOff[c + 1]; ++j) {
-            int e = a.cellFace[j], f = e >> 1;
+            int e = a.cellFace[j], f = chk(e >> 1, a.nA, a.status);
             const double* S = a.Sf + 3 * f;
             double xs = x0 * S[0] + x1 * S[1] + x2 * S[2];
             long long fi = (long long)f * Vp + v;

@@ -434,6 +434,8 @@ int Solver::synchronize() {
     if (int e = checkCuda(cudaMemcpy(&st, base_.status, sizeof(int), cudaMemcpyDeviceToHost), "status")) return e;
     if (st != 0) {
         cudaMemset(base_.status, 0, sizeof(int));
+        if (st == DUGKS_ERR_BOUNDS)
+            return fail(DUGKS_ERR_BOUNDS, "checked build: an index read from mesh or tile data was out of range");
         return fail(st == DUGKS_ERR_TIMEOUT ? DUGKS_ERR_TIMEOUT : DUGKS_ERR_NUMERIC,
                     st == DUGKS_ERR_TIMEOUT ? "device wait timed out"
                                             : "non-finite or non-positive rho/T detected in the cell moments");

@@ -25,7 +25,7 @@ BC_KINDS = {"empty": 0, "calculatedMaxwell": 1, "zeroGradient": 2, "fixedValue":
             "pressureIn": 5, "pressureOut": 6, "symmetryMod": 7, "symmetryPlane": 8}
 
 ERRORS = {0: "OK", 1: "DUGKS_ERR_ARG", 2: "DUGKS_ERR_IO", 3: "DUGKS_ERR_UNSUPPORTED", 4: "DUGKS_ERR_CUDA",
-          5: "DUGKS_ERR_NUMERIC", 6: "DUGKS_ERR_TIMEOUT", 7: "DUGKS_ERR_OOM"}
+          5: "DUGKS_ERR_NUMERIC", 6: "DUGKS_ERR_TIMEOUT", 7: "DUGKS_ERR_OOM", 8: "DUGKS_ERR_BOUNDS"}
 
 # Every entry point declared in include/dugks/dugks.h.
 EXPORTS = [
@@ -38,6 +38,7 @@ EXPORTS = [
     "dugks_objective_value", "dugks_objective_tangent", "dugks_objective_adjoint",
     "dugks_batch_create", "dugks_batch_destroy", "dugks_batch_last_error", "dugks_batch_set_dt", "dugks_batch_step",
     "dugks_batch_synchronize", "dugks_batch_get_macros", "dugks_batch_get_info", "dugks_batch_set_wait_limit",
+    "dugks_checked_build",
 ]
 
 
@@ -102,15 +103,15 @@ class BatchInfo(C.Structure):
                 ("tuned_ms_per_step", C.c_double * 8)]
 
 
-_lib = None
+_libs = {}
 
 
 def load_library(path: str | None = None):
-    """Load libdugks.so (raises if it has not been built)."""
-    global _lib
-    if _lib is not None:
-        return _lib
+    """Load libdugks.so, or the library at ``path`` (the index-checked build
+    libdugks_checked.so), once per path (raises if it has not been built)."""
     path = path or LIB_PATH
+    if path in _libs:
+        return _libs[path]
     if not os.path.exists(path):
         raise DugksError(4, f"{path} not built; run dugksfoam_gb300.build.build()")
     lib = C.CDLL(path)
@@ -158,7 +159,7 @@ def load_library(path: str | None = None):
     lib.dugks_batch_get_macros.argtypes = [vp, C.c_int32] + [_dp] * 4
     lib.dugks_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
     lib.dugks_batch_set_wait_limit.argtypes = [vp, C.c_int64]
-    _lib = lib
+    _libs[path] = lib
     return lib
 
 
@@ -235,8 +236,8 @@ def case_desc(case, precision=FP64, pipeline=PIPE_AUTO, device=0):
 class FvDVM:
     """One DUGKS case resident on one GPU (the reference's fvDVM)."""
 
-    def __init__(self, case=None, precision=FP64, pipeline=PIPE_AUTO, device=0, _handle=None):
-        self._lib = load_library()
+    def __init__(self, case=None, precision=FP64, pipeline=PIPE_AUTO, device=0, _handle=None, lib_path=None):
+        self._lib = load_library(lib_path)
         self._h = C.c_void_p()
         if _handle is not None:
             self._h = _handle

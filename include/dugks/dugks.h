@@ -38,8 +38,14 @@ enum dugks_status {
     DUGKS_ERR_CUDA = 4,         /* CUDA runtime error / no device         */
     DUGKS_ERR_NUMERIC = 5,      /* NaN/Inf or non-positive rho or T found */
     DUGKS_ERR_TIMEOUT = 6,      /* a bounded device wait gave up          */
-    DUGKS_ERR_OOM = 7           /* device allocation failed               */
+    DUGKS_ERR_OOM = 7,          /* device allocation failed               */
+    DUGKS_ERR_BOUNDS = 8        /* checked build: an index read from mesh
+                                   or tile data was out of range           */
 };
+
+/* 1 in the checked build (libdugks_checked.so: device-side index checks that
+ * report DUGKS_ERR_BOUNDS instead of reading out of range), else 0. */
+int dugks_checked_build(void);
 
 /* Storage/arithmetic precision of the distributions. */
 enum dugks_precision {
