@@ -33,7 +33,8 @@ public:
     virtual std::string describe() const = 0;
 
     // ---- batched stepping of several cases (FP32 pipeline only)
-    virtual bool batchable() const { return false; }
+    virtual bool batchable() const { return false; }        // may join a batch (FP32 pipeline)
+    virtual bool batchKernels() const { return false; }     // fits the batched kernels (diffuse walls only)
     // Kernel arguments (a FusedArgs<float>) of the step that starts `parity`
     // steps from now (0 or 1), for base arguments `a` of the current step.
     virtual void batchArgs(const StepArgs& a, int parity, void* out) const { (void)a; (void)parity; (void)out; }

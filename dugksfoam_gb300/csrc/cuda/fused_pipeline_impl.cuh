@@ -296,7 +296,8 @@ public:
         return A;
     }
 
-    bool batchable() const override { return fp32_ && (bcMask_ & ~(1 << kBcMaxwell)) == 0; }
+    bool batchable() const override { return fp32_; }
+    bool batchKernels() const override { return fp32_ && (bcMask_ & ~(1 << kBcMaxwell)) == 0; }
     void batchArgs(const StepArgs& a, int parity, void* out) const override {
         const FusedArgs<S> A = stepArgs(a, parity);
         std::memcpy(out, &A, sizeof(A));

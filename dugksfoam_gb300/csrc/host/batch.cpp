@@ -51,6 +51,7 @@ int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap, int 
     }
     fused_set_tuning(npl, tileCap);
     cells_ = cellDV_ = 0;
+    open_ = false;
     for (int i = 0; i < n; ++i) {
         dugks_case_desc d = descs[i];
         d.precision = DUGKS_FP32_FP64MOM;
@@ -64,6 +65,7 @@ int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap, int 
         }
         FusedPipeline* fp = s->fusedPipeline();
         if (!fp || !fp->batchable()) { fused_set_tuning(0, 0); return fail(DUGKS_ERR_UNSUPPORTED, "case is not batchable"); }
+        if (!fp->batchKernels()) open_ = true;
         if (s->stepArgs().D != 2) { fused_set_tuning(0, 0); return fail(DUGKS_ERR_UNSUPPORTED, "batched cases must be 2D"); }
         if (int e = s->setStream(stream_)) { fused_set_tuning(0, 0); return fail(e, s->error()); }
         cells_ += s->stepArgs().nC;
@@ -71,9 +73,13 @@ int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap, int 
         cases_.push_back(std::move(s));
     }
     fused_set_tuning(0, 0);
+    // open boundary types run each case's own kernels (its graph branch): the
+    // batched kernels and the persistent kernel take diffuse walls only
+    if (open_ && !perCase_)
+        return fail(DUGKS_ERR_UNSUPPORTED, "batch: boundary types other than diffuse walls need the per-case mode");
     const StepArgs a0 = cases_[0]->stepArgs();
     for (auto& c : cases_)
-        if (c->stepArgs().hasH != a0.hasH) return fail(DUGKS_ERR_UNSUPPORTED, "batched cases must agree on h");
+        if (!perCase_ && c->stepArgs().hasH != a0.hasH) return fail(DUGKS_ERR_UNSUPPORTED, "batched cases must agree on h");
     sms_ = cases_[0]->sms();
     dirty_ = true;
     parity_ = 0;
@@ -304,7 +310,12 @@ std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int au
         const int cand[][3] = {{4, 0, 1}, {4, 0, 4}, {4, 0, 0}, {4, 32, 1}, {2, 0, 1}, {4, 0, -1}};
         double best = 1e300;
         for (auto& c : cand) {
-            if (int e = b->build(descs, n, c[0], c[1], c[2])) { err = b->err_; code = e; return nullptr; }
+            if (int e = b->build(descs, n, c[0], c[1], c[2])) {
+                if (e == DUGKS_ERR_UNSUPPORTED && b->open_) continue;  // a mode the open boundary types exclude
+                err = b->err_;
+                code = e;
+                return nullptr;
+            }
             for (auto& s : b->cases_) s->setDt(1e-30);  // timing only: a vanishing step
             b->dirty_ = true;
             cudaEvent_t e0, e1;
@@ -330,7 +341,9 @@ std::unique_ptr<Batch> Batch::create(const dugks_case_desc* descs, int n, int au
     }
     std::vector<double> ms = b->tuneMs_;
     std::vector<int> tn = b->tuneNpl_, tc = b->tuneCap_, tg = b->tuneGroups_;
-    if (int e = b->build(descs, n, bestNpl, bestCap, bestGroups)) { err = b->err_; code = e; return nullptr; }
+    int rc = b->build(descs, n, bestNpl, bestCap, bestGroups);
+    if (rc == DUGKS_ERR_UNSUPPORTED && b->open_ && autotune == 0) rc = b->build(descs, n, bestNpl, bestCap, 0);
+    if (rc) { err = b->err_; code = rc; return nullptr; }
     b->tuneMs_ = ms;
     b->tuneNpl_ = tn;
     b->tuneCap_ = tc;

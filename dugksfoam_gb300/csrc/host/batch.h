@@ -53,6 +53,7 @@ private:
     int sms_ = 1, npl_ = 4, tileCap_ = 0, groups_ = 1;
     bool perCase_ = false;
     bool persistent_ = false;
+    bool open_ = false;         // some case has boundary types other than diffuse walls
     unsigned* bar_ = nullptr;   // persistent kernel: barrier counters
     int* tstatus_ = nullptr;    // persistent kernel: DUGKS_ERR_TIMEOUT when a barrier wait gave up
     long long waitLimit_ = 1LL << 24;

@@ -314,8 +314,10 @@ int dugks_objective_adjoint(dugks_handle* h, const dugks_objective* o, double* J
  * DVs per lane (2 or 4), the cap on cells per tile and the number of groups
  * (0: every case its own graph branch with its own kernels; -1: persistent)
  * are chosen by timing a few steps of each candidate; 0: 4 DVs per lane, no
- * cap, one group; 2: the persistent kernel.  Each case starts from its own
- * initial state; set each case's dt before stepping. */
+ * cap, one group; 2: the persistent kernel.  Cases with boundary types other
+ * than diffuse walls run each with its own kernels as a branch of the graph
+ * (groups 0; chosen by autotune 0 and 1, refused by 2).  Each case starts
+ * from its own initial state; set each case's dt before stepping. */
 typedef struct dugks_batch dugks_batch;
 typedef struct dugks_batch_info {
     int32_t n_cases, dv_per_lane, tile_cap, groups, launches_per_step /* kernel nodes per step */, steps_per_graph,

@@ -144,3 +144,40 @@ def test_persistent_batch_barrier_timeout_is_reported(built_lib):
     assert ei.value.code == 6
     out = _run_persistent(cs, dts)
     assert all(np.all(np.isfinite(m["rho"])) and np.all(m["rho"] > 0) for m in out)
+
+
+def test_batch_with_open_boundary_types(built_lib, oracle_lib):
+    """Cases with farField, zeroGradient, fixedValue and pressure patches (and
+    zeroGradient U/T) batch in the per-case mode: each case its own kernels as
+    a graph branch, bit-identical to the case run alone and within 1e-5 of the
+    oracle; the batched and the persistent kernels refuse them."""
+    from conftest import rel_err
+    from dugksfoam_gb300 import cases, solver
+    from oracle.oracle import Oracle
+
+    cs = [cases.open_box2d(8, nxi=8, zero_gradient_tu=True), cases.channel2d(12, 6, nxi=8, inlet_T_zero_gradient=True),
+          cases.batch_case(_instances()[0])]
+    dts = [cases.stable_dt(c) for c in cs]
+    b = solver.Batch(cs, autotune=False)
+    assert b.info()["groups"] == 0
+    for i, dt in enumerate(dts):
+        b.set_dt(i, dt)
+    b.step(9)
+    got = [b.macros(i) for i in range(len(cs))]
+    b.close()
+    for i, c in enumerate(cs):
+        s = solver.FvDVM(c, precision=solver.FP32_FP64MOM, pipeline=solver.PIPE_FUSED)
+        s.set_dt(dts[i])
+        s.evolution(9)
+        want = s.macros()
+        s.close()
+        ref = Oracle(c)
+        ref.step(dts[i], 9)
+        oracle = ref.cell()
+        for k in ("rho", "U", "T", "q"):
+            assert np.array_equal(got[i][k], want[k]), (i, k)
+            einf, el2 = rel_err(got[i][k], oracle[k])
+            assert einf <= 1e-5 and el2 <= 1e-5, (i, k, einf, el2)
+    with pytest.raises(solver.DugksError) as ei:
+        solver.Batch(cs, persistent=True)
+    assert ei.value.code == 3
