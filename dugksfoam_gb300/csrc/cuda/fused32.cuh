@@ -1276,26 +1276,31 @@ __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32_batch(const FusedA
 // ------------------------------------------------- persistent batched step
 // Grid-wide barrier of a cooperative launch (every block resident): an
 // arrival counter bar[0] and a generation bar[1] in global memory (zeroed
-// before the launch).  A wait polls at most `cap` times; then it sets
-// *status = DUGKS_ERR_TIMEOUT (6) and the barrier returns false in every
-// block that reaches it afterwards, so all blocks leave the kernel.  Callers
-// reach it only with no asynchronous copy in flight.
+// before the launch).  Arrival is an acquire-release add, the last arrival
+// releases the generation and the waiters acquire it, so that after the
+// barrier every block sees what every block wrote before it (the acquire
+// also keeps stale L1 lines from being read).  A wait polls at most `cap`
+// times; then it sets *status = DUGKS_ERR_TIMEOUT (6) and the barrier returns
+// false in every block that reaches it afterwards, so all blocks leave the
+// kernel.  Callers reach it only with no asynchronous copy in flight.
 constexpr int kStatusTimeout = 6;
 __device__ __forceinline__ bool grid_barrier(unsigned* bar, long long cap, int* status) {
     __shared__ int sOk;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned* vb = bar;
         int ok = 1;
-        const unsigned gen = vb[1];
-        __threadfence();
-        if (atomicAdd(bar, 1u) == gridDim.x - 1) {  // last to arrive: reset, release the others
+        const unsigned gen = *(volatile unsigned*)(bar + 1);
+        unsigned old;
+        asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;" : "=r"(old) : "l"(bar) : "memory");
+        if (old == gridDim.x - 1) {  // last to arrive: reset, release the others
             atomicExch(bar, 0u);
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
+            asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar + 1) : "memory");
         } else {
             long long it = 0;
-            while (vb[1] == gen) {
+            for (;;) {
+                unsigned g;
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(g) : "l"(bar + 1) : "memory");
+                if (g != gen) break;
                 if (++it > cap) {
                     ok = 0;
                     atomicExch(status, kStatusTimeout);
@@ -1304,7 +1309,6 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, long long cap, int* 
                 __nanosleep(64);
             }
         }
-        __threadfence();
         if (*(volatile int*)status == kStatusTimeout) ok = 0;
         sOk = ok;
     }
