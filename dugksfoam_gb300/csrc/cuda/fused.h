@@ -99,8 +99,11 @@ inline cudaError_t allow_max_dynamic_smem(F* func) {
 
 // Tuning override for pipelines created while it is set (0 = default):
 // DVs per lane and the tile-size cap of the face sweep.
-void fused_set_tuning(int npl, int maxTileCells);
+// waveBalance: size the FP32 face-sweep tiles to fill whole waves of the SMs
+// (a case whose tiles share the grid with other cases' passes false)
+void fused_set_tuning(int npl, int maxTileCells, bool waveBalance = true);
 int fused_tile_cap();
+bool fused_wave_balance();
 
 // DVs per lane of the fused kernels for a precision (FP32: DUGKS_NPL, default 4).
 int fused_npl(int precision);

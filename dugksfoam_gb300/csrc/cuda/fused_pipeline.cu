@@ -8,14 +8,17 @@ namespace dugks {
 
 namespace {
 thread_local int g_tuneNpl = 0, g_tuneTile = 0;
+thread_local bool g_tuneWave = true;
 }
 
-void fused_set_tuning(int npl, int maxTileCells) {
+void fused_set_tuning(int npl, int maxTileCells, bool waveBalance) {
     g_tuneNpl = npl;
     g_tuneTile = maxTileCells;
+    g_tuneWave = waveBalance;
 }
 
 int fused_tile_cap() { return g_tuneTile; }
+bool fused_wave_balance() { return g_tuneWave && g_tuneTile <= 0; }
 
 int fused_npl(int precision) {
     if (precision == DUGKS_FP64) return 1;

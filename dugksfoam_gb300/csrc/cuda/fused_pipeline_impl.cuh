@@ -48,7 +48,13 @@ public:
         const int maxCells = fused_tile_cap() > 0 ? fused_tile_cap() : (envT ? std::max(1, std::atoi(envT)) : 4096);
         // FP32: sweep A alone is tiled (one-ring halo); FP64: both sweeps (two-ring halo)
         const SmemFn fn = [this](const TileDims& d) { return fp32_ ? smemFace(d) : std::max(smemFace(d), smemCell(d)); };
-        if (!build_tile_plan(m, maxCells, fn, budget, plan_, err, fp32_ ? 1 : 2)) return false;
+        // one tile per SM at a time: balance the waves of the FP32 face sweep,
+        // unless a cap was asked for or the case's tiles share the batched
+        // kernels' grid with other cases' tiles
+        int nsmPlan = 0;
+        cudaDeviceGetAttribute(&nsmPlan, cudaDevAttrMultiProcessorCount, dev);
+        const int waveSlots = fp32_ && fused_wave_balance() && !envT ? nsmPlan : 0;
+        if (!build_tile_plan(m, maxCells, fn, budget, plan_, err, fp32_ ? 1 : 2, waveSlots)) return false;
         smemA_ = smemB_ = 0;
         for (const TileHdr& h : plan_.hdr) {
             TileDims d;

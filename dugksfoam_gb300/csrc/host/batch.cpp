@@ -49,7 +49,9 @@ int Batch::build(const dugks_case_desc* descs, int n, int npl, int tileCap, int 
         if (int r = check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event")) return r;
         ev_.push_back(e);
     }
-    fused_set_tuning(npl, tileCap);
+    // per-case mode: each case keeps the plan it has when run alone (the
+    // same tiles, so bit-identical results)
+    fused_set_tuning(npl, tileCap, perCase_);
     cells_ = cellDV_ = 0;
     open_ = false;
     for (int i = 0; i < n; ++i) {

@@ -97,7 +97,7 @@ void rcb(const Mesh& m, std::vector<int>& cells, int b, int e, int N, std::vecto
 }  // namespace
 
 bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t budget, TilePlan& p,
-                     std::string& err, int rings) {
+                     std::string& err, int rings, int waveSlots) {
     if (rings != 1 && rings != 2) { err = "tile plan: rings must be 1 or 2"; return false; }
     const int nC = m.nC, nI = m.nI;
     if (maxTileCells < 1) { err = "tile size must be positive"; return false; }
@@ -124,6 +124,18 @@ bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t
         const int mid = (lo + hi + 1) / 2;
         if (fits(mid)) lo = mid;
         else hi = mid - 1;
+    }
+    if (waveSlots > 0) {  // fill the last wave: the smallest size with no more waves
+        partition(lo);
+        const long long slots = ((long long)parts.size() + waveSlots - 1) / waveSlots * waveSlots;
+        int a = 1, b = lo;  // smallest N in [1, lo] with count(N) <= slots (count falls as N grows)
+        while (a < b) {
+            const int mid = (a + b) / 2;
+            partition(mid);
+            if ((long long)parts.size() <= slots) b = mid;
+            else a = mid + 1;
+        }
+        lo = a;  // smaller tiles than a size that fits: they fit too
     }
     partition(lo);
     p.tileCells = lo;

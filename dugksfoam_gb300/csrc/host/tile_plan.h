@@ -66,7 +66,12 @@ using SmemFn = std::function<size_t(const TileDims&)>;
 // candidates both have their gradients in the tile).  rings = 1: rows of
 // T u H1, stencils of T only (nT2 == nT1); a face's stencil range is set for
 // the sides whose cell is in T and empty otherwise.
+//
+// waveSlots > 0 (tiles that run at once: SMs x tiles per SM): after the
+// largest fitting tile size is found, the tiles are shrunk to the smallest
+// size whose count still fills the same number of waves, so that the last
+// wave is (nearly) full instead of leaving SMs idle.
 bool build_tile_plan(const Mesh& m, int maxTileCells, const SmemFn& smem, size_t budget, TilePlan& p,
-                     std::string& err, int rings = 2);
+                     std::string& err, int rings = 2, int waveSlots = 0);
 
 }  // namespace dugks
