@@ -72,6 +72,9 @@ struct BatchLaunch {
 // Set function attributes and the persistent gather grid; false if the
 // (D, H, npl) combination has no kernels.
 bool fused_batch_prepare(BatchLaunch& L, int sms);
+// Dynamic shared memory of the FP32 gather sweep for nw warps per block, MF
+// staged faces per cell and a DV chunk of kc velocities (with h or not).
+size_t fused_gather_smem(int nw, int mf, int kc, bool h);
 void fused_batch_launch(int k, const BatchLaunch& L, int sms, cudaStream_t s);
 // The persistent batched kernel: shared memory and the co-resident grid
 // (false if it does not fit), and one cooperative launch of nSteps steps from

@@ -294,6 +294,7 @@ __device__ __forceinline__ void relax_rows32(const FusedArgs<float>& A, const Ti
 struct Face32 {
     TileFace r;
     float Sx, Sy, Sz, iVo, dOx, dOy, dOz, iVn, dNx, dNy, dNz;
+    int plain;  // stencil entries of the owner (bits 0-7) and neighbour (8-15) side when all are cell rows, else 0
     __device__ __forceinline__ void load(const int4* p) {  // a staged face record
         const int4 a = p[0], b = p[1];
         r.ownL = a.x; r.neiL = a.y; r.a = a.z; r.w = a.w;
@@ -303,6 +304,7 @@ struct Face32 {
         Sx = g0.x; Sy = g0.y; Sz = g0.z; iVo = g0.w;
         dOx = g1.x; dOy = g1.y; dOz = g1.z; iVn = g1.w;
         dNx = g2.x; dNy = g2.y; dNz = g2.z;
+        plain = __float_as_int(g2.w);
     }
     template <int D, int NPL>
     __device__ __forceinline__ float2 xs(const Lane32<D, NPL>& L, int p) const {
@@ -315,7 +317,8 @@ struct Face32 {
 // One side's reconstruction sum over its stencil entry k:
 //   acc += beta (phi_o - phi_u),  beta = L.(d_u - xi dt/2),
 // with the neighbour row (or the lagged wall gradient) read for all pairs.
-template <int D, bool H, int NP, bool GRAD>
+// PLAIN: the entry is known to be a cell row (no wall branch).
+template <int D, bool H, int NP, bool GRAD, bool PLAIN = false>
 __device__ __forceinline__ void side_entry(const FusedArgs<float>& A, const float4* E, int e, float dx, float dy, float dz,
                                            const float2 (&cu)[NP], const float2 (&hu)[NP], const float* sg,
                                            const float* sh, int col, int v0, const float2* xx, const float2* xy,
@@ -329,7 +332,7 @@ __device__ __forceinline__ void side_entry(const FusedArgs<float>& A, const floa
     if (D == 3) al = fmaf(ent.z, dz, al);
     const float2 lx = f2(hdt * ent.x), ly = f2(hdt * ent.y), lz = f2(hdt * ent.z);
     float2 r[NP], q[NP];
-    if (o >= 0) {
+    if (PLAIN || o >= 0) {
         ldp<NP>(r, sg + o * KC + col);
         if (H) ldp<NP>(q, sh + o * KC + col);
     } else {  // wall entry: phi_b - phi_P = G_b / deltaCoeff
@@ -366,6 +369,17 @@ __device__ __forceinline__ void side_entry(const FusedArgs<float>& A, const floa
             }
         }
     }
+}
+
+// Upwind weight of the owner side of a face for one velocity from s = xi.S:
+// 1 for s > 0, 0 for s < 0, 1/2 for s == 0 (one saturating FMA; |s| below
+// 2^-101 would count as a partial tie, far below any xi.S of a real face).
+__device__ __forceinline__ float2 upwind_w2(float2 s) {
+    return make_float2(__saturatef(fmaf(s.x, 0x1p100f, 0.5f)), __saturatef(fmaf(s.y, 0x1p100f, 0.5f)));
+}
+// w go + (1 - w) gn, exactly go for w = 1 and gn for w = 0.
+__device__ __forceinline__ float2 blend2(float2 w, float2 go, float2 gn) {
+    return fma2(w, go, mul2(sub2(f2(1.0f), w), gn));
 }
 
 // Upwind reconstruction gbar_f = gbar+_u + sum_e (L_e.(d_u - xi dt/2)) (gbar+_o(e) - gbar+_u)
@@ -416,53 +430,120 @@ __device__ __forceinline__ void recon32(const FusedArgs<float>& A, const float4*
     }
 #pragma unroll
     for (int p = 0; p < NP; ++p) {
-        const float2 go = add2(cO[p], aO[p]), gn = add2(cN[p], aN[p]);
-        const float2 ho = H ? add2(hO[p], ahO[p]) : f2(0.f), hn = H ? add2(hN[p], ahN[p]) : f2(0.f);
-        const float2 gt = mul2(add2(gn, go), f2(0.5f)), ht = mul2(add2(hn, ho), f2(0.5f));
-        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f, n0 = xs[p].x < 0.f, n1 = xs[p].y < 0.f;
-        gf[p] = sel2(o0, o1, go, sel2(n0, n1, gn, gt));
-        if (H) hf[p] = sel2(o0, o1, ho, sel2(n0, n1, hn, ht));
+        const float2 w = upwind_w2(xs[p]);
+        gf[p] = blend2(w, add2(cO[p], aO[p]), add2(cN[p], aN[p]));
+        if (H) hf[p] = blend2(w, add2(hO[p], ahO[p]), add2(hN[p], ahN[p]));
+    }
+}
+
+// recon32 for an internal face whose two stencils are plain (NE cell-row
+// entries each, no wall entry): both sides summed with the entry loop
+// unrolled, then the per-velocity upwind blend.
+template <int D, bool H, int NPL, int NE>
+__device__ __forceinline__ void recon_plain32(const FusedArgs<float>& A, const float4* E, const Face32& F,
+                                              const Lane32<D, NPL>& L, const float* sg, const float* sh, int lane,
+                                              int v0, const float2* xs, float2 (&gf)[NPL / 2], float2 (&hf)[NPL / 2]) {
+    constexpr int KC = 32 * NPL, NP = NPL / 2;
+    const int col = lane * NPL;
+    float2 cO[NP], hO[NP], cN[NP], hN[NP], aO[NP], ahO[NP], aN[NP], ahN[NP], gw[D][NP], hw[D][NP];
+    ldp<NP>(cO, sg + F.r.ownL * KC + col);
+    ldp<NP>(cN, sg + F.r.neiL * KC + col);
+    if (H) {
+        ldp<NP>(hO, sh + F.r.ownL * KC + col);
+        ldp<NP>(hN, sh + F.r.neiL * KC + col);
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        aO[p] = f2(0.f); ahO[p] = f2(0.f); aN[p] = f2(0.f); ahN[p] = f2(0.f);
+        if (!H) { hO[p] = f2(0.f); hN[p] = f2(0.f); }
+    }
+#pragma unroll
+    for (int k = 0; k < NE; ++k) {
+        side_entry<D, H, NP, false, true>(A, E, F.r.stO0 + k, F.dOx, F.dOy, F.dOz, cO, hO, sg, sh, col, v0, L.x, L.y,
+                                          L.z, aO, ahO, gw, hw);
+        side_entry<D, H, NP, false, true>(A, E, F.r.stN0 + k, F.dNx, F.dNy, F.dNz, cN, hN, sg, sh, col, v0, L.x, L.y,
+                                          L.z, aN, ahN, gw, hw);
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        const float2 w = upwind_w2(xs[p]);
+        gf[p] = blend2(w, add2(cO[p], aO[p]), add2(cN[p], aN[p]));
+        hf[p] = H ? blend2(w, add2(hO[p], ahO[p]), add2(hN[p], ahN[p])) : f2(0.f);
+    }
+}
+
+// recon_one32 for a plain side of NE cell-row entries (loop unrolled).
+template <int D, bool H, int NPL, int NE>
+__device__ __forceinline__ void recon_one_plain32(const FusedArgs<float>& A, const float4* E, int e0, int lu, float dx,
+                                                  float dy, float dz, const Lane32<D, NPL>& L, const float* sg,
+                                                  const float* sh, int lane, int v0, float2 (&gv)[NPL / 2],
+                                                  float2 (&hv)[NPL / 2]) {
+    constexpr int KC = 32 * NPL, NP = NPL / 2;
+    const int col = lane * NPL;
+    float2 c[NP], hc[NP], ac[NP], ah[NP], gw[D][NP], hw[D][NP];
+    ldp<NP>(c, sg + lu * KC + col);
+    if (H) ldp<NP>(hc, sh + lu * KC + col);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        ac[p] = f2(0.f);
+        ah[p] = f2(0.f);
+        if (!H) hc[p] = f2(0.f);
+    }
+#pragma unroll
+    for (int k = 0; k < NE; ++k)
+        side_entry<D, H, NP, false, true>(A, E, e0 + k, dx, dy, dz, c, hc, sg, sh, col, v0, L.x, L.y, L.z, ac, ah, gw,
+                                          hw);
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        gv[p] = add2(c[p], ac[p]);
+        hv[p] = H ? add2(hc[p], ah[p]) : f2(0.f);
     }
 }
 
 // Deviation moments of the lane's velocities about ur into its slots
-// (mask: per-velocity inclusion, used on walls for the outgoing half).
-template <int D, bool H, int NPL, int NS>
+// (mask: per-velocity inclusion, used on walls for the outgoing half);
+// ASSIGN: the slots of the moments are set, else added to.
+template <int D, bool H, int NPL, int NS, bool ASSIGN = false>
 __device__ __forceinline__ void mom32(float (&m)[NS], const Lane32<D, NPL>& L, const float* ur,
                                       const float2 (&g)[NPL / 2], const float2 (&h)[NPL / 2], const float2* mask) {
     using SL = Slots<D, H>;
     constexpr int NP = NPL / 2;
     float2 m2[NS];
 #pragma unroll
-    for (int s = 0; s < NS; ++s) m2[s] = f2(0.f);
-#pragma unroll
-    for (int p = 0; p < NP; ++p) {
+    for (int p = 0; p < NP; ++p) {  // pair 0 sets the packed sums, the others add
+        const bool first = p == 0;
         const float2 c[3] = {sub2(L.x[p], f2(ur[0])), sub2(L.y[p], f2(ur[1])),
                              D == 3 ? sub2(L.z[p], f2(ur[2])) : f2(0.f)};
         float2 wg = mul2(L.w[p], g[p]);
         if (mask) wg = mul2(wg, mask[p]);
-        m2[0] = add2(m2[0], wg);
+        m2[0] = first ? wg : add2(m2[0], wg);
         float2 c2 = mul2(c[0], c[0]);
 #pragma unroll
         for (int i = 1; i < D; ++i) c2 = fma2(c[i], c[i], c2);
 #pragma unroll
         for (int i = 0; i < D; ++i) {
             const float2 t = mul2(wg, c[i]);
-            m2[SL::M1 + i] = add2(m2[SL::M1 + i], t);
+            m2[SL::M1 + i] = first ? t : add2(m2[SL::M1 + i], t);
 #pragma unroll
-            for (int k = i; k < D; ++k) m2[SL::M2 + sym<D>(i, k)] = fma2(t, c[k], m2[SL::M2 + sym<D>(i, k)]);
-            m2[SL::M3 + i] = fma2(t, c2, m2[SL::M3 + i]);
+            for (int k = i; k < D; ++k) {
+                const int j = SL::M2 + sym<D>(i, k);
+                m2[j] = first ? mul2(t, c[k]) : fma2(t, c[k], m2[j]);
+            }
+            m2[SL::M3 + i] = first ? mul2(t, c2) : fma2(t, c2, m2[SL::M3 + i]);
         }
         if (H) {
             float2 wh = mul2(L.w[p], h[p]);
             if (mask) wh = mul2(wh, mask[p]);
-            m2[SL::H0] = add2(m2[SL::H0], wh);
+            m2[SL::H0] = first ? wh : add2(m2[SL::H0], wh);
 #pragma unroll
-            for (int i = 0; i < D; ++i) m2[SL::H1 + i] = fma2(wh, c[i], m2[SL::H1 + i]);
+            for (int i = 0; i < D; ++i) m2[SL::H1 + i] = first ? mul2(wh, c[i]) : fma2(wh, c[i], m2[SL::H1 + i]);
         }
     }
 #pragma unroll
-    for (int s = 0; s < SL::NM; ++s) m[s] += m2[s].x + m2[s].y;
+    for (int s = 0; s < SL::NM; ++s) {
+        if (ASSIGN) m[s] = m2[s].x + m2[s].y;
+        else m[s] += m2[s].x + m2[s].y;
+    }
 }
 
 // Moments of the reference Maxwellian about u (FP64, scaled units) from its raw
@@ -768,7 +849,7 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
                 const size_t wi = (size_t)F.r.w * Vp + v0 + col;
                 stp<NP>(A.Gbgn + wi, gn);
                 if (H) stp<NP>(A.Gbhn + wi, hn);
-                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, use);
+                mom32<D, H, NPL, NS, true>(m, L, ur, gf, hf, use);
                 stp<NP>(A.gF + fi, gf);
                 if (H) stp<NP>(A.hF + fi, hf);
             } else if (F.r.ownL < hd.nT && F.r.neiL < hd.nT) {  // both sides in T: complete
@@ -778,33 +859,42 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
                     side_value_g<D, H, NPL>(L, cg, chh, gbuf, F.r.neiL, dN, A.dt, col, gn2, hn2);
 #pragma unroll
                     for (int p = 0; p < NP; ++p) {
-                        const bool o0 = xs[p].x > 0.f, o1 = xs[p].y > 0.f, n0 = xs[p].x < 0.f, n1 = xs[p].y < 0.f;
-                        gf[p] = sel2(o0, o1, go[p], sel2(n0, n1, gn2[p], mul2(add2(gn2[p], go[p]), f2(0.5f))));
-                        hf[p] = H ? sel2(o0, o1, ho[p], sel2(n0, n1, hn2[p], mul2(add2(hn2[p], ho[p]), f2(0.5f)))) : f2(0.f);
+                        const float2 w = upwind_w2(xs[p]);
+                        gf[p] = blend2(w, go[p], gn2[p]);
+                        hf[p] = H ? blend2(w, ho[p], hn2[p]) : f2(0.f);
                     }
+                } else if (D == 2 && F.plain == (3 | 3 << 8)) {  // two triangles
+                    recon_plain32<D, H, NPL, 3>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf);
+                } else if (D == 2 && F.plain == (4 | 4 << 8)) {  // two quadrilaterals
+                    recon_plain32<D, H, NPL, 4>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf);
                 } else {
                     recon32<D, H, NPL, false>(A, tm.E, F, L, cg, chh, lane, v0, xs, gf, hf, gw, hw);
                 }
-                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
+                mom32<D, H, NPL, NS, true>(m, L, ur, gf, hf, nullptr);
                 stp<NP>(A.gF + fi, gf);
                 if (H) stp<NP>(A.hF + fi, hf);
             } else {  // one side in T
                 const bool own = F.r.ownL < hd.nT;
+                const int nPlain = own ? F.plain & 255 : (F.plain >> 8) & 255;
+                const int e0 = own ? F.r.stO0 : F.r.stN0, lu = own ? F.r.ownL : F.r.neiL;
+                const float* du = own ? dO : dN;
                 if (GR)
-                    side_value_g<D, H, NPL>(L, cg, chh, gbuf, own ? F.r.ownL : F.r.neiL, own ? dO : dN, A.dt, col, gf, hf);
-                else if (own)
-                    recon_one32<D, H, NPL>(A, tm.E, F.r.stO0, F.r.stO1, F.r.ownL, F.dOx, F.dOy, F.dOz, L, cg, chh, lane,
-                                           v0, gf, hf);
+                    side_value_g<D, H, NPL>(L, cg, chh, gbuf, lu, du, A.dt, col, gf, hf);
+                else if (D == 2 && nPlain == 3)
+                    recon_one_plain32<D, H, NPL, 3>(A, tm.E, e0, lu, du[0], du[1], du[2], L, cg, chh, lane, v0, gf, hf);
+                else if (D == 2 && nPlain == 4)
+                    recon_one_plain32<D, H, NPL, 4>(A, tm.E, e0, lu, du[0], du[1], du[2], L, cg, chh, lane, v0, gf, hf);
                 else
-                    recon_one32<D, H, NPL>(A, tm.E, F.r.stN0, F.r.stN1, F.r.neiL, F.dNx, F.dNy, F.dNz, L, cg, chh, lane,
-                                           v0, gf, hf);
+                    recon_one32<D, H, NPL>(A, tm.E, e0, own ? F.r.stO1 : F.r.stN1, lu, du[0], du[1], du[2], L, cg, chh,
+                                           lane, v0, gf, hf);
                 float2 wt[NP];
                 float* dg = A.gF + fi;
                 float* dh = H ? A.hF + fi : nullptr;
 #pragma unroll
                 for (int p = 0; p < NP; ++p) {
-                    const bool u0 = own ? xs[p].x > 0.f : xs[p].x < 0.f, u1 = own ? xs[p].y > 0.f : xs[p].y < 0.f;
-                    wt[p] = make_float2(u0 ? 1.f : (xs[p].x == 0.f ? 0.5f : 0.f), u1 ? 1.f : (xs[p].y == 0.f ? 0.5f : 0.f));
+                    const float2 w = upwind_w2(xs[p]);
+                    wt[p] = own ? w : sub2(f2(1.f), w);  // this side's share: 1 upwind, 1/2 tie
+                    const bool u0 = wt[p].x == 1.f, u1 = wt[p].y == 1.f;
                     if (u0) {
                         dg[2 * p] = gf[p].x;
                         if (H) dh[2 * p] = hf[p].x;
@@ -814,7 +904,7 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
                         if (H) dh[2 * p + 1] = hf[p].y;
                     }
                 }
-                mom32<D, H, NPL, NS>(m, L, ur, gf, hf, wt);
+                mom32<D, H, NPL, NS, true>(m, L, ur, gf, hf, wt);
             }
             const float tot = reduce_scatter<NS, float>(m, lane);
             if (writer && myslot <= SL::FLUX) mom[lf * NS + myslot].add(tot);

@@ -89,6 +89,8 @@ bool dispatch2d(const BatchLaunch& L, F&& f) {
 
 }  // namespace
 
+size_t fused_gather_smem(int nw, int mf, int kc, bool h) { return gather_smem(nw, mf, kc, h); }
+
 bool fused_batch_prepare(BatchLaunch& L, int sms) {
     return dispatch2d(L, [&](auto K) { return decltype(K)::prepare(L, sms); });
 }

@@ -100,7 +100,17 @@ public:
                 const double iVo = 1.0 / m.V[o], iVn = r.a < m.nI ? 1.0 / m.V[m.neighbour[f]] : 0.0;
                 fg4[3 * k] = make_float4((float)Sv[0], (float)Sv[1], (float)Sv[2], (float)iVo);
                 fg4[3 * k + 1] = make_float4((float)dO[0], (float)dO[1], (float)dO[2], (float)iVn);
-                fg4[3 * k + 2] = make_float4((float)dN[0], (float)dN[1], (float)dN[2], 0.0f);
+                // plain-stencil code: entries of each side when every one is
+                // a cell row (no wall entry), else 0; owner | neighbour << 8
+                auto plainN = [&](int e0, int e1) {
+                    for (int e = e0; e < e1; ++e)
+                        if (plan_.stEnt[e] < 0) return 0;
+                    return std::min(e1 - e0, 255);
+                };
+                const int plain = plainN(r.stO0, r.stO1) | (r.neiL >= 0 ? plainN(r.stN0, r.stN1) << 8 : 0);
+                float pw;
+                std::memcpy(&pw, &plain, 4);
+                fg4[3 * k + 2] = make_float4((float)dN[0], (float)dN[1], (float)dN[2], pw);
             }
             // per-tile blocks: face records (stencil ranges relative to the
             // tile's first entry) + geometry, entries, cells, colour order

@@ -163,7 +163,7 @@ int Batch::prepare() {
             L.nFaces = faceOff[m];
             L.smemFace = smem;
             L.MF = MF;
-            L.gatherSmem = (size_t)8 * 2 * (1 + MF) * (a0.hasH ? 2 : 1) * 32 * npl_ * sizeof(float);
+            L.gatherSmem = fused_gather_smem(8, MF, 32 * npl_, a0.hasH != 0);
             L.D = 2;
             L.H = a0.hasH;
             L.npl = npl_;
