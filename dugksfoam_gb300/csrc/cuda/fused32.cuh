@@ -201,19 +201,23 @@ struct Lane32 {
     }
 };
 
-// Shakhov relaxation in deviation form: out = G - a (G + Mref) + a g^S.
+// Shakhov relaxation in deviation form: out = G - a (G + Mref) + a g^S, with
+//   a g^S = aA e [1 + phi u],   e = exp(-c^2 / 2RT),  u = c^2/RT - (D+2),
+//   a h^S = RT [aA e phi ((K+3-D) u + 6 - 2D) + aA e (K+3-D)]
+// (phi = the Shakhov heat-flux term q'.c; the h form is the reference's
+// ((c^2/RT - D)(K+3-D) - 2K) regrouped about u, so that g and h share u).
 template <int D, bool H>
 struct Eq32 {
-    float ux, uy, uz, kexp, invRT, qx, qy, qz, a, aA, RT, KD, K2, hf;
+    float ux, uy, uz, kexp, invRT, qx, qy, qz, a, aA, KDRT, C0RT, hf;
     __device__ __forceinline__ void load(const float4* q, int K, float hrefFac) {  // an eq_table entry
         const float4 b0 = q[0], b1 = q[1], b2 = q[2];
         ux = b0.x; uy = b0.y; uz = b0.z; kexp = b0.w;
         invRT = b1.x; qx = b1.y; qy = b1.z; qz = b1.w;
         a = b2.x;
         aA = b2.y;
-        RT = b2.z;
-        KD = (float)(K + 3 - D);
-        K2 = -2.0f * (float)K;
+        const float RT = b2.z;
+        KDRT = (float)(K + 3 - D) * RT;
+        C0RT = (float)(6 - 2 * D) * RT;
         hf = hrefFac;
     }
     template <int NPL>
@@ -228,13 +232,12 @@ struct Eq32 {
         }
         const float2 t = mul2(c2, f2(kexp));
         const float2 e = mul2(make_float2(ex2f(t.x), ex2f(t.y)), f2(aA));
-        const float2 c2n = mul2(c2, f2(invRT));
+        const float2 u = fma2(c2, f2(invRT), f2(-(float)(D + 2)));
         const float2 ep = mul2(e, phi);
-        const float2 ags = fma2(ep, add2(c2n, f2(-(float)(D + 2))), e);
+        const float2 ags = fma2(ep, u, e);
         g = fma2(f2(-a), add2(g, L.mr[p]), add2(g, ags));
         if (H) {
-            const float2 eh = mul2(e, f2(RT));
-            const float2 ahs = fma2(mul2(ep, f2(RT)), fma2(add2(c2n, f2(-(float)D)), f2(KD), f2(K2)), mul2(eh, f2(KD)));
+            const float2 ahs = fma2(ep, fma2(u, f2(KDRT), f2(C0RT)), mul2(e, f2(KDRT)));
             h = fma2(f2(-a), add2(h, mul2(L.mr[p], f2(hf))), add2(h, ahs));
         }
     }
