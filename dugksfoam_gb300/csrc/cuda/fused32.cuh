@@ -256,18 +256,20 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// Raw g~ (and h~) rows of T u H1 u H2 for the DV chunk at v0 into shared
-// memory, 16-byte asynchronous copies spread over the block (one commit group).
-template <int NPL, bool H, int NT>
+// Raw g~ (and h~) rows of T u H1 for the DV chunk at v0 into shared memory,
+// 16-byte asynchronous copies (one commit group).  Warp w copies rows w,
+// w + NW, ... -- the rows it relaxes -- so that after its own wait_group and
+// a __syncwarp it may relax them without a block barrier.
+template <int NPL, bool H, int NW>
 __device__ __forceinline__ void issue_rows32(const FusedArgs<float>& A, const TileHdr& hd, const int* C, float* sg,
-                                             float* sh, int v0) {
+                                             float* sh, int v0, int warp, int lane) {
     constexpr int KC = 32 * NPL, SEG = KC / 4;
-    const int n = hd.nT2 * SEG;
-    for (int i = threadIdx.x; i < n; i += NT) {
-        const int r = i / SEG, sgm = i - r * SEG;
-        const size_t gi = (size_t)C[r] * A.b.Vp + v0 + sgm * 4;
-        cp_async_row(sg + r * KC + sgm * 4, A.gT + gi, 4);
-        if (H) cp_async_row(sh + r * KC + sgm * 4, A.hT + gi, 4);
+    for (int r = warp; r < hd.nT2; r += NW) {
+        const size_t gr = (size_t)C[r] * A.b.Vp + v0;
+        for (int sgm = lane; sgm < SEG; sgm += 32) {
+            cp_async_row(sg + r * KC + sgm * 4, A.gT + gr + sgm * 4, 4);
+            if (H) cp_async_row(sh + r * KC + sgm * 4, A.hT + gr + sgm * 4, 4);
+        }
     }
     cp_async_commit();
 }
@@ -787,24 +789,30 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
         const float* blk = A.cc + (size_t)tm.C[i] * kNCoef;
         eq_table(ceq + 3 * i, blk, cell_weight(A.dt, blk));
     }
-    issue_rows32<NPL, H, NW * 32>(A, hd, tm.C, sg, sh, 0);
+    issue_rows32<NPL, H, NW>(A, hd, tm.C, sg, sh, 0, warp, lane);
     const int nChunks = Vp / KC;
     const int myslot = slot_of<NS>(lane);
     const bool writer = NS == 16 ? (lane & 1) == 0 : true;
+    __syncthreads();  // face Uref and cell equilibria
 
+    // One block barrier per chunk: a warp relaxes the rows it copied itself
+    // as soon as its copies have landed (a warp still in the previous
+    // chunk's faces reads the other buffer), the barrier after the
+    // relaxation releases the faces, and only then are the next chunk's
+    // rows copied into the buffer that the previous chunk's faces read.
     for (int ch = 0; ch < nChunks; ++ch) {
         const int v0 = ch * KC;
         Lane32<D, NPL> L;
         L.load(A, v0, lane);
         cp_async_wait<0>();
-        __syncthreads();
+        __syncwarp();
         float* cg = sg + (ch & 1) * bufStride;
         float* chh = sh + (ch & 1) * bufStride;
-        if (ch + 1 < nChunks)
-            issue_rows32<NPL, H, NW * 32>(A, hd, tm.C, sg + ((ch + 1) & 1) * bufStride, sh + ((ch + 1) & 1) * bufStride,
-                                          v0 + KC);
         relax_rows32<D, H, NPL, NW>(A, hd, ceq, L, lane, warp, cg, chh);
         __syncthreads();
+        if (ch + 1 < nChunks)
+            issue_rows32<NPL, H, NW>(A, hd, tm.C, sg + ((ch + 1) & 1) * bufStride, sh + ((ch + 1) & 1) * bufStride,
+                                     v0 + KC, warp, lane);
         if (GR) {
             cell_gradients32<D, H, NPL, NW>(A, hd, tm, cg, chh, gbuf, lane, warp, v0);
             __syncthreads();
