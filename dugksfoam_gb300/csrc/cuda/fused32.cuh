@@ -917,7 +917,7 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
                 }
                 mom32<D, H, NPL, NS, true>(m, L, ur, gf, hf, wt);
             }
-            const float tot = reduce_scatter<NS, float>(m, lane);
+            const float tot = reduce_scatter<NS, float, SL::FLUX + 1>(m, lane);
             if (writer && myslot <= SL::FLUX) mom[lf * NS + myslot].add(tot);
         }
     }
@@ -1082,7 +1082,7 @@ __global__ void k_open_faces32(FusedArgs<float> A) {
 #pragma unroll
             for (int s2 = 0; s2 < NS; ++s2) m[s2] = 0.0f;
             mom32<D, H, NPL, NS>(m, L, ur, gf, hf, nullptr);
-            acc.add(reduce_scatter<NS, float>(m, lane));
+            acc.add(reduce_scatter<NS, float, SL::FLUX + 1>(m, lane));
         }
         double* dst = A.faceMom + (size_t)a * 2 * NS;
         if (writer && myslot < NS) {
@@ -1296,7 +1296,7 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
         if (H) stp_cs<NP>(A.hTn + gi, th);
         mom32<D, H, NPL, NS>(m, L, ur, t, th, nullptr);
     }
-    return (double)reduce_scatter<NS, float>(m, lane);
+    return (double)reduce_scatter<NS, float, SL::NM>(m, lane);
 }
 
 // Warps stride over the cells (persistent grid); per cell, all DV chunks:

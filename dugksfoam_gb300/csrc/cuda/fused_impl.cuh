@@ -128,13 +128,21 @@ __host__ __device__ __forceinline__ constexpr int sym(int i, int j) {
 
 // Reduce NS per-lane values over the warp; afterwards lane holds the total of
 // slot slot_of(lane) (lanes 2k and 2k+1 hold the same slot when NS == 16).
-template <int NS, typename T>
+// NU: slots [NU, NS) are zero in every lane and their totals are not used;
+// in the first exchange a pair whose upper slot is such a slot is summed in
+// place (no select: the upper lanes then hold a meaningless value there,
+// which later exchanges keep in unused slot positions).
+template <int NS, typename T, int NU = NS>
 __device__ __forceinline__ T reduce_scatter(T (&v)[NS], int lane) {
 #pragma unroll
     for (int half = NS / 2, xm = 16; half >= 1; half >>= 1, xm >>= 1) {
         const bool up = lane & xm;
 #pragma unroll
         for (int i = 0; i < half; ++i) {
+            if (half == NS / 2 && i + half >= NU) {
+                v[i] = v[i] + __shfl_xor_sync(0xffffffffu, v[i], xm);
+                continue;
+            }
             T send = up ? v[i] : v[i + half];
             T keep = up ? v[i + half] : v[i];
             v[i] = keep + __shfl_xor_sync(0xffffffffu, send, xm);
