@@ -358,7 +358,7 @@ def run_engine(args):
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 distributions, f64 moments", "data": "synthetic",
         "config": {"workload": desc, "cells": s.nCells, "dvs": s.nDV, "dv_padded": info["n_dv_padded"],
-                   "state_bytes": int(2 * 4 * s.nCells * info["n_dv_padded"]),
+                   "state_bytes": int((2 if info["has_h"] else 1) * 4 * s.nCells * info["n_dv_padded"]),
                    "l2": "state larger than the 129 MB L2; no flush needed", "dt": dt,
                    "parallelism": f"replicas x{world}"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
