@@ -54,6 +54,7 @@ Solver::~Solver() {
     fused_.reset();
     for (void* p : allocs_) cudaFree(p);
     if (ownStream_) cudaStreamDestroy(ownStream_);
+    if (pin_) cudaFreeHost(pin_);
 }
 
 std::unique_ptr<Solver> Solver::create(const dugks_case_desc& d, std::string& err, int& code) {
@@ -298,6 +299,11 @@ int Solver::init(const dugks_case_desc& d) {
     a.status = dalloc<int>(1);
     Uo_ = dalloc<double>(3 * (size_t)nC); To_ = dalloc<double>(nC); ro_ = dalloc<double>(nC); red_ = dalloc<double>(8 + 128 * 8);  // results + per-block partials
     if (oom_) return fail(DUGKS_ERR_OOM, "device allocation failed");
+    if (cudaHostAlloc(reinterpret_cast<void**>(&pin_), 8 + 8 * sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+        pin_ = nullptr;
+        cudaGetLastError();
+        return fail(DUGKS_ERR_OOM, "pinned host allocation failed");
+    }
     cudaError_t ce = cudaSuccess;
     auto chk = [&](cudaError_t e) { if (ce == cudaSuccess) ce = e; };
     chk(up(dSf, Sf)); chk(up(ddO, dO)); chk(up(ddN, dN)); chk(up(down, own)); chk(up(dnei, nei));
@@ -429,9 +435,14 @@ int Solver::evolution(int n) {
 
 int Solver::synchronize() {
     cudaSetDevice(device_);
-    if (int e = checkCuda(cudaStreamSynchronize(stream_), "step")) return e;
-    int st = 0;
-    if (int e = checkCuda(cudaMemcpy(&st, base_.status, sizeof(int), cudaMemcpyDeviceToHost), "status")) return e;
+    return syncStatus("step");
+}
+
+int Solver::syncStatus(const char* what) {
+    cudaError_t ce = cudaMemcpyAsync(pinStatus(), base_.status, sizeof(int), cudaMemcpyDeviceToHost, stream_);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream_);
+    if (int e = checkCuda(ce, what)) return e;
+    const int st = *pinStatus();
     if (st != 0) {
         cudaMemset(base_.status, 0, sizeof(int));
         if (st == DUGKS_ERR_BOUNDS)
@@ -449,27 +460,30 @@ void Solver::advanceExternal(int n) {
     steps_ += n;
 }
 
+// The Courant number and the cell macros are enqueued behind the step's
+// kernels on the engine's stream and finished by one stream wait that also
+// reads the status word (an error of the step is reported by these calls).
 int Solver::getCoNum(double& maxCo, double& meanCo) {
-    if (int e = synchronize()) return e;
+    cudaSetDevice(device_);
     launch_conum(argsNow(), dcI_, xiMax_, red_, stream_);
-    double h[2];
-    if (int e = checkCuda(cudaMemcpyAsync(h, red_, sizeof(h), cudaMemcpyDeviceToHost, stream_), "conum")) return e;
-    if (int e = checkCuda(cudaStreamSynchronize(stream_), "conum")) return e;
-    maxCo = h[0] * dt_;
-    meanCo = (mesh_.nI > 0 ? h[1] / mesh_.nI : 0.0) * dt_;
+    if (int e = checkCuda(cudaMemcpyAsync(pinRed(), red_, 2 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "conum"))
+        return e;
+    if (int e = syncStatus("conum")) return e;
+    maxCo = pinRed()[0] * dt_;
+    meanCo = (mesh_.nI > 0 ? pinRed()[1] / mesh_.nI : 0.0) * dt_;
     return DUGKS_OK;
 }
 
 int Solver::macros(double* rho, double* U, double* T, double* q, double* tau) {
-    if (int e = synchronize()) return e;
+    cudaSetDevice(device_);
     const size_t n = mesh_.nC;
     cudaError_t ce = cudaSuccess;
     auto cp = [&](double* dst, const double* src, size_t k) {
         if (dst && ce == cudaSuccess) ce = cudaMemcpyAsync(dst, src, k * sizeof(double), cudaMemcpyDeviceToHost, stream_);
     };
     cp(rho, base_.rho, n); cp(U, base_.U, 3 * n); cp(T, base_.T, n); cp(q, base_.q, 3 * n); cp(tau, base_.tau, n);
-    if (ce == cudaSuccess) ce = cudaStreamSynchronize(stream_);
-    return checkCuda(ce, "get macros");
+    if (int e = checkCuda(ce, "get macros")) return e;
+    return syncStatus("get macros");
 }
 
 int Solver::faceMacros(double* rho, double* U, double* T, double* q, double* tau) {
@@ -511,11 +525,12 @@ int Solver::boundary(int patch, double* rho, double* U, double* T) {
 }
 
 int Solver::residual(double res[3]) {
-    if (int e = synchronize()) return e;
+    cudaSetDevice(device_);
     launch_residual(argsNow(), Uo_, To_, ro_, red_, stream_);
-    double s[6];
-    if (int e = checkCuda(cudaMemcpyAsync(s, red_, sizeof(s), cudaMemcpyDeviceToHost, stream_), "residual")) return e;
-    if (int e = checkCuda(cudaStreamSynchronize(stream_), "residual")) return e;
+    double* s = pinRed();
+    if (int e = checkCuda(cudaMemcpyAsync(s, red_, 6 * sizeof(double), cudaMemcpyDeviceToHost, stream_), "residual"))
+        return e;
+    if (int e = syncStatus("residual")) return e;
     res[0] = s[1] > 0 ? s[0] / s[1] : 0.0;
     res[1] = s[3] > 0 ? s[2] / s[3] : 0.0;
     res[2] = s[5] > 0 ? s[4] / s[5] : 0.0;

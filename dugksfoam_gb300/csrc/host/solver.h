@@ -68,6 +68,9 @@ public:
     T* dalloc(size_t n);
     int fail(int code, const std::string& msg);
     int checkCuda(cudaError_t e, const char* what);
+    // Wait for the stream and report the status word the kernels set, in one
+    // host round trip (the word is copied into pinned memory behind the work).
+    int syncStatus(const char* what);
 
 private:
     Solver() = default;
@@ -94,6 +97,10 @@ private:
     RefBuffers ref_{};
     // residual "old" fields and scratch
     double *Uo_ = nullptr, *To_ = nullptr, *ro_ = nullptr, *red_ = nullptr;
+    // pinned host words: [0] the status word, [8..] reduction results (doubles)
+    unsigned char* pin_ = nullptr;
+    int* pinStatus() const { return reinterpret_cast<int*>(pin_); }
+    double* pinRed() const { return reinterpret_cast<double*>(pin_ + 8); }
     // fused pipeline
     std::unique_ptr<FusedPipeline> fused_;
     std::vector<int32_t> patchFirstWall_, patchNWall_;
