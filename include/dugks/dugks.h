@@ -182,7 +182,9 @@ int dugks_synchronize(dugks_handle* h);
 int dugks_get_conum(dugks_handle* h, double* max_co, double* mean_co);
 
 /* Accessors rhoVol(), Uvol(), Tvol(), qVol(), tauVol() (fvDVMI.H:26-155).
- * Any pointer may be NULL. */
+ * Any pointer may be NULL.  The copies are queued behind the handle's
+ * stream and finished by one wait; when that wait reports an error of a
+ * previous step (DUGKS_ERR_NUMERIC, ...), the buffers hold that step's values. */
 int dugks_get_macros(dugks_handle* h, double* rho, double* U, double* T, double* q, double* tau);
 
 /* rhoSurf(), Usurf(), Tsurf(), qSurf(), tauSurf() for internal faces then
