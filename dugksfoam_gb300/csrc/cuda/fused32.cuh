@@ -96,12 +96,16 @@ __host__ __device__ constexpr int tile_meta32_bound(int nFB, int nEnt, int nT2) 
 //   2 x rows(T u H1) | face moments | metadata | face Uref | cell equilibria
 // (the next DV chunk's raw rows stream into the second row buffer).
 // (GR: gradients of the cells of T kept per chunk, [nT][D][g, h][KC], after the rows.)
+// With per-cell gradients (GR) the faces read only the rows of T, so the
+// halo rows have a single buffer (refilled after the gradient pass) and only
+// the rows of T are double-buffered: [T rows x2 | halo rows].
 template <int D, bool H, int NPL, bool GR = false>
 struct SmemLayout32 {
     static constexpr int KC = 32 * NPL, NS = Slots<D, H>::NS;
     __host__ __device__ static size_t rows(int n) { return (size_t)n * KC * sizeof(float) * (H ? 2 : 1); }
     __host__ __device__ static size_t grad(int nT) { return GR ? (size_t)nT * D * rows(1) : 0; }
-    __host__ __device__ static size_t mom(int nRows, int nT) { return 2 * rows(nRows) + grad(nT); }
+    __host__ __device__ static size_t rowBlock(int nRows, int nT) { return GR ? rows(nT) + rows(nRows) : 2 * rows(nRows); }
+    __host__ __device__ static size_t mom(int nRows, int nT) { return rowBlock(nRows, nT) + grad(nT); }
     __host__ __device__ static size_t meta(int nRows, int nF, int nT) {
         return mom(nRows, nT) + (size_t)nF * NS * sizeof(Acc<float>);
     }
@@ -260,29 +264,48 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // 16-byte asynchronous copies (one commit group).  Warp w copies rows w,
 // w + NW, ... -- the rows it relaxes -- so that after its own wait_group and
 // a __syncwarp it may relax them without a block barrier.
-template <int NPL, bool H, int NW>
-__device__ __forceinline__ void issue_rows32(const FusedArgs<float>& A, const TileHdr& hd, const int* C, float* sg,
-                                             float* sh, int v0, int warp, int lane) {
+// Rows of one DV chunk in shared memory: row r of field f (0 g, 1 h) at
+// t[f] + r KC for the cells of T (r < nT) and at hh[f] + (r - nT) KC for the
+// halo; hh[f] = t[f] + nT KC when the halo follows T in one block.
+struct Rows32 {
+    float* t[2];
+    float* hh[2];
+    int nT;
+    template <bool SPLIT>  // halo rows apart from the rows of T
+    __device__ __forceinline__ float* row(int f, int r, int KC) const {
+        if (!SPLIT) return t[f] + r * KC;
+        return r < nT ? t[f] + r * KC : hh[f] + (r - nT) * KC;
+    }
+};
+
+template <int NPL, bool H, int NW, bool SPLIT>
+__device__ __forceinline__ void issue_rows32(const FusedArgs<float>& A, const TileHdr& hd, const int* C,
+                                             const Rows32& rs, int v0, int warp, int lane, int r0, int r1) {
     constexpr int KC = 32 * NPL, SEG = KC / 4;
     for (int r = warp; r < hd.nT2; r += NW) {
+        if (r < r0 || r >= r1) continue;
         const size_t gr = (size_t)C[r] * A.b.Vp + v0;
+        float* dg = rs.row<SPLIT>(0, r, KC);
+        float* dh = H ? rs.row<SPLIT>(1, r, KC) : nullptr;
         for (int sgm = lane; sgm < SEG; sgm += 32) {
-            cp_async_row(sg + r * KC + sgm * 4, A.gT + gr + sgm * 4, 4);
-            if (H) cp_async_row(sh + r * KC + sgm * 4, A.hT + gr + sgm * 4, 4);
+            cp_async_row(dg + sgm * 4, A.gT + gr + sgm * 4, 4);
+            if (H) cp_async_row(dh + sgm * 4, A.hT + gr + sgm * 4, 4);
         }
     }
     cp_async_commit();
 }
 
 // gbar+ = relaxation of the raw rows in place (shared memory only).
-template <int D, bool H, int NPL, int NW>
+template <int D, bool H, int NPL, int NW, bool SPLIT>
 __device__ __forceinline__ void relax_rows32(const FusedArgs<float>& A, const TileHdr& hd, const float4* ceq,
-                                             const Lane32<D, NPL>& L, int lane, int warp, float* sg, float* sh) {
+                                             const Lane32<D, NPL>& L, int lane, int warp, const Rows32& rs) {
     constexpr int KC = 32 * NPL, NP = NPL / 2;
     for (int r = warp; r < hd.nT2; r += NW) {
         float2 g[NP], h[NP];
-        ldp<NP>(g, sg + r * KC + lane * NPL);
-        if (H) ldp<NP>(h, sh + r * KC + lane * NPL);
+        float* sg = rs.row<SPLIT>(0, r, KC);
+        float* sh = H ? rs.row<SPLIT>(1, r, KC) : sg;
+        ldp<NP>(g, sg + lane * NPL);
+        if (H) ldp<NP>(h, sh + lane * NPL);
         Eq32<D, H> e;
         e.load(ceq + 3 * r, A.b.K, A.hrefFac);
 #pragma unroll
@@ -290,8 +313,8 @@ __device__ __forceinline__ void relax_rows32(const FusedArgs<float>& A, const Ti
             if (!H) h[p] = f2(0.f);
             e.relax(L, p, g[p], h[p]);
         }
-        stp<NP>(sg + r * KC + lane * NPL, g);
-        if (H) stp<NP>(sh + r * KC + lane * NPL, h);
+        stp<NP>(sg + lane * NPL, g);
+        if (H) stp<NP>(sh + lane * NPL, h);
     }
 }
 
@@ -679,14 +702,13 @@ __device__ __forceinline__ void recon_one32(const FusedArgs<float>& A, const flo
 // L_b G_b / deltaCoeff (the lagged boundary gradient).
 template <int D, bool H, int NPL, int NW>
 __device__ __forceinline__ void cell_gradients32(const FusedArgs<float>& A, const TileHdr& hd, const TileMeta32& tm,
-                                                 const float* sg, const float* sh, float* gbuf, int lane, int warp,
-                                                 int v0) {
+                                                 const Rows32& rs, float* gbuf, int lane, int warp, int v0) {
     constexpr int KC = 32 * NPL, NP = NPL / 2, NR = H ? 2 : 1;
     const int col = lane * NPL, Vp = A.b.Vp;
     for (int lc = warp; lc < hd.nT; lc += NW) {
         float2 c[NP], hc[NP], gg[D][NP], hg[D][NP];
-        ldp<NP>(c, sg + lc * KC + col);
-        if (H) ldp<NP>(hc, sh + lc * KC + col);
+        ldp<NP>(c, rs.row<true>(0, lc, KC) + col);
+        if (H) ldp<NP>(hc, rs.row<true>(1, lc, KC) + col);
 #pragma unroll
         for (int k = 0; k < D; ++k)
 #pragma unroll
@@ -698,8 +720,8 @@ __device__ __forceinline__ void cell_gradients32(const FusedArgs<float>& A, cons
             float2 dg[NP], dh[NP];
             if (o >= 0) {
                 float2 r[NP], q[NP];
-                ldp<NP>(r, sg + o * KC + col);
-                if (H) ldp<NP>(q, sh + o * KC + col);
+                ldp<NP>(r, rs.row<true>(0, o, KC) + col);
+                if (H) ldp<NP>(q, rs.row<true>(1, o, KC) + col);
 #pragma unroll
                 for (int p = 0; p < NP; ++p) {
                     dg[p] = sub2(r[p], c[p]);
@@ -770,10 +792,26 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int Vp = b.Vp, col = lane * NPL;
     using LY = SmemLayout32<D, H, NPL, GR>;
-    float* sg = reinterpret_cast<float*>(smem);
-    float* sh = sg + (size_t)hd.nT2 * KC;
-    const size_t bufStride = LY::rows(hd.nT2) / sizeof(float);
-    float* gbuf = reinterpret_cast<float*>(smem + 2 * LY::rows(hd.nT2));  // GR: gradients of T
+    // the row buffer of chunk parity bf
+    float* const rowBase = reinterpret_cast<float*>(smem);
+    const size_t nTK = (size_t)hd.nT * KC, nHK = (size_t)(hd.nT2 - hd.nT) * KC;
+    auto rowsOf = [&](int bf) {
+        Rows32 r;
+        r.nT = hd.nT;
+        if (GR) {  // [T g,h (buffer 0)][T g,h (buffer 1)][halo g,h]
+            r.t[0] = rowBase + bf * (H ? 2 : 1) * nTK;
+            r.t[1] = r.t[0] + nTK;
+            r.hh[0] = rowBase + 2 * (H ? 2 : 1) * nTK;
+            r.hh[1] = r.hh[0] + nHK;
+        } else {  // per buffer: g rows of T u H1, then h rows
+            r.t[0] = rowBase + bf * (H ? 2 : 1) * (nTK + nHK);
+            r.t[1] = r.t[0] + nTK + nHK;
+            r.hh[0] = r.t[0] + nTK;
+            r.hh[1] = r.t[1] + nTK;
+        }
+        return r;
+    };
+    float* gbuf = reinterpret_cast<float*>(smem + LY::rowBlock(hd.nT2, hd.nT));  // GR: gradients of T
     Acc<float>* mom = reinterpret_cast<Acc<float>*>(smem + LY::mom(hd.nT2, hd.nT));
     for (int i = threadIdx.x; i < hd.nFB * NS; i += NW * 32) mom[i].zero();
     const TileMeta32 tm = stage_meta<NW * 32>(A, hd, tile, smem + LY::meta(hd.nT2, hd.nFB, hd.nT));
@@ -789,7 +827,7 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
         const float* blk = A.cc + (size_t)tm.C[i] * kNCoef;
         eq_table(ceq + 3 * i, blk, cell_weight(A.dt, blk));
     }
-    issue_rows32<NPL, H, NW>(A, hd, tm.C, sg, sh, 0, warp, lane);
+    issue_rows32<NPL, H, NW, GR>(A, hd, tm.C, rowsOf(0), 0, warp, lane, 0, hd.nT2);
     const int nChunks = Vp / KC;
     const int myslot = slot_of<NS>(lane);
     const bool writer = NS == 16 ? (lane & 1) == 0 : true;
@@ -806,16 +844,21 @@ __device__ __forceinline__ void face_sides_body(const FusedArgs<float>& A, int t
         L.load(A, v0, lane);
         cp_async_wait<0>();
         __syncwarp();
-        float* cg = sg + (ch & 1) * bufStride;
-        float* chh = sh + (ch & 1) * bufStride;
-        relax_rows32<D, H, NPL, NW>(A, hd, ceq, L, lane, warp, cg, chh);
+        const Rows32 rc = rowsOf(ch & 1);
+        float* cg = rc.t[0];
+        float* chh = rc.t[1];
+        relax_rows32<D, H, NPL, NW, GR>(A, hd, ceq, L, lane, warp, rc);
         __syncthreads();
+        // next chunk's rows: those of T now (the faces of this chunk read the
+        // other buffer); with per-cell gradients the halo rows, single
+        // buffered, only after the gradient pass has read them
         if (ch + 1 < nChunks)
-            issue_rows32<NPL, H, NW>(A, hd, tm.C, sg + ((ch + 1) & 1) * bufStride, sh + ((ch + 1) & 1) * bufStride,
-                                     v0 + KC, warp, lane);
+            issue_rows32<NPL, H, NW, GR>(A, hd, tm.C, rowsOf((ch + 1) & 1), v0 + KC, warp, lane, 0, GR ? hd.nT : hd.nT2);
         if (GR) {
-            cell_gradients32<D, H, NPL, NW>(A, hd, tm, cg, chh, gbuf, lane, warp, v0);
+            cell_gradients32<D, H, NPL, NW>(A, hd, tm, rc, gbuf, lane, warp, v0);
             __syncthreads();
+            if (ch + 1 < nChunks)
+                issue_rows32<NPL, H, NW, GR>(A, hd, tm.C, rowsOf((ch + 1) & 1), v0 + KC, warp, lane, hd.nT, hd.nT2);
         }
         for (int lf = warp; lf < hd.nFB; lf += NW) {
             Face32 F;
