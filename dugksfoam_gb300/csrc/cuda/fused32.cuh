@@ -624,7 +624,7 @@ __device__ __forceinline__ void finalize_face32(const FusedArgs<float>& A, int a
     }
     for (int s = 0; s < SL::NM; ++s) M[s] *= A.invGscale;
     double rho, U[3], T, tau, qr[3];
-    macros_from_moments<D, H>(M, ur, b, rho, U, T, tau, qr);
+    macros_from_moments<D, H, true>(M, ur, b, rho, U, T, tau, qr);
     const double fac = 2.0 * tau / (2.0 * tau + 0.5 * b.dt * b.Pr);
     double q[3] = {fac * qr[0], fac * qr[1], fac * qr[2]};
     b.rhoF[a] = rho;

@@ -344,7 +344,12 @@ __device__ __forceinline__ void add_moments(T (&m)[NS], S w, S g, S h, const S* 
 }
 
 // Macros from moments about Uref (FP64): rho, U, T, tau and the raw heat flux.
-template <int D, bool H>
+// FAST_TAU: the viscosity power (T/Tref)^omega by the FP32 hardware log2 /
+// exp2 (relative error ~1e-7, against the FP64 exp(omega log) of the FP64
+// pipelines); for the face macros of the FP32 pipeline, whose face
+// relaxation weights are FP32 (the cell macros keep the FP64 power: the cell
+// values are the reported fields).
+template <int D, bool H, bool FAST_TAU = false>
 __device__ __forceinline__ void macros_from_moments(const double* M, const double* Uref, const StepArgs& b,
                                                     double& rho, double* U, double& T, double& tau, double* qraw) {
     using SL = Slots<D, H>;
@@ -362,7 +367,15 @@ __device__ __forceinline__ void macros_from_moments(const double* M, const doubl
     const double h0 = H ? M[SL::H0] : 0.0;
     const double eint = 0.5 * (tr - m1d + h0);  // sum w |c|^2 g = tr M2 - |M1|^2/M0
     T = eint / ((b.K + 3) / 2.0 * b.R * rho);
-    tau = tau_ref(T, rho, b.muRef, b.omega, b.Tref, b.R);
+    if (FAST_TAU) {
+        float p;
+        asm("lg2.approx.f32 %0, %1;" : "=f"(p) : "f"((float)(T / b.Tref)));
+        p *= (float)b.omega;
+        asm("ex2.approx.f32 %0, %1;" : "=f"(p) : "f"(p));
+        tau = b.muRef * (double)p / (rho * T * b.R);
+    } else {
+        tau = tau_ref(T, rho, b.muRef, b.omega, b.Tref, b.R);
+    }
     for (int i = 0; i < 3; ++i) qraw[i] = 0.0;
     for (int i = 0; i < D; ++i) {
         double m2d = 0;
