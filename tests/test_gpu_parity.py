@@ -264,3 +264,26 @@ def test_fp32_delaunay24k_500_steps_against_fp64(built_lib):
     for k in FIELDS:
         einf, el2 = rel_err(out["fp32"][k], out["fp64"][k])
         assert einf <= TOL32 and el2 <= TOL32, (k, einf, el2)
+
+
+@pytest.mark.parametrize("name,env", [
+    ("tri", {"DUGKS_TILE_CELLS": "6"}),                           # many tiles: halo rows, one-sided faces
+    ("tri", {"DUGKS_TILE_CELLS": "6", "DUGKS_FACE_GRAD": "1"}),  # per-cell gradients, halo rows apart
+    ("hex8", {"DUGKS_TILE_CELLS": "10"}),                         # 3D: per-cell gradients, halo rows apart
+])
+def test_fused_fp32_small_tiles_match_oracle(built_lib, oracle_lib, monkeypatch, name, env):
+    """FP32 face sweep on tiles capped far below what shared memory holds, so
+    every tile has halo rows and faces across its boundary (and, with
+    per-cell gradients, the single-buffered halo rows refilled after the
+    gradient pass), against the FP64 oracle."""
+    from dugksfoam_gb300 import cases, solver
+
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    case, steps = _small_cases()[name] if name != "hex8" else (cases.cavity3d(n=8, nxi=6), 10)
+    s, ref = _run_pair(case, steps, solver.FP32_FP64MOM, solver.PIPE_FUSED)
+    got, want = s.macros(), ref.cell()
+    for k in FIELDS:
+        einf, el2 = rel_err(got[k], want[k])
+        assert einf <= TOL32 and el2 <= TOL32, (name, env, k, einf, el2)
+    s.close()
