@@ -203,7 +203,31 @@ struct Lane32 {
         ldp<NP>(w, A.w + v);
         ldp<NP>(mr, A.mref + v);
     }
+    // from a shared-memory copy [x | y | (z) | w | mref], Vp each (dv_table32)
+    __device__ __forceinline__ void load_tab(const float* tab, int Vp, int v0, int lane) {
+        const int v = v0 + lane * NPL;
+        ldp<NP>(x, tab + v);
+        ldp<NP>(y, tab + Vp + v);
+        if (D == 3) ldp<NP>(z, tab + 2 * Vp + v);
+        else
+#pragma unroll
+            for (int p = 0; p < NP; ++p) z[p] = f2(0.0f);
+        ldp<NP>(w, tab + D * Vp + v);
+        ldp<NP>(mr, tab + (D + 1) * Vp + v);
+    }
 };
+
+// The velocity constants of Lane32 for all Vp velocities, copied by a block
+// into shared memory (caller synchronises); its size in bytes.
+__host__ __device__ inline size_t dv_table32_bytes(int D, int Vp) { return (size_t)(D + 2) * Vp * sizeof(float); }
+template <int D>
+__device__ __forceinline__ void dv_table32(const FusedArgs<float>& A, float* tab) {
+    const int Vp = A.b.Vp;
+    for (int q = threadIdx.x; q < (D + 2) * Vp; q += blockDim.x) {
+        const int k = q / Vp, v = q - k * Vp;
+        tab[q] = k < D ? A.xi[k * Vp + v] : (k == D ? A.w[v] : A.mref[v]);
+    }
+}
 
 // Shakhov relaxation in deviation form: out = G - a (G + Mref) + a g^S, with
 //   a g^S = aA e [1 + phi u],   e = exp(-c^2 / 2RT),  u = c^2/RT - (D+2),
@@ -1181,8 +1205,8 @@ __host__ __device__ inline size_t gather_smem(int nw, int mf, int kc, bool h) {
 }
 
 // Cell macros (FP64) from the deviation moment totals M (slots as Slots<D,H>).
-template <int D, bool H>
-__device__ __forceinline__ void finalize_cell32(const FusedArgs<float>& A, int c, const double* tot) {
+template <int D, bool H, typename TT = double>
+__device__ __forceinline__ void finalize_cell32(const FusedArgs<float>& A, int c, const TT* tot) {
     using SL = Slots<D, H>;
     constexpr int NS = SL::NS;
     const StepArgs& b = A.b;
@@ -1211,8 +1235,10 @@ constexpr int kGatherBatch = 32;
 // offset by the lane's column.
 // OPEN: the case has open boundary faces (instantiated apart so that
 // wall-only cases run the same code as before those existed).
+// tab: the velocity constants in shared memory (dv_table32), or null.
 template <int D, bool H, int NPL, bool OPEN = false>
-__device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, int MF, float* wb, int lane) {
+__device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, int MF, float* wb, int lane,
+                                              const float* tab = nullptr) {
     using SL = Slots<D, H>;
     constexpr int NS = SL::NS, KC = 32 * NPL, NP = NPL / 2, NR = H ? 2 : 1;
     const StepArgs& b = A.b;
@@ -1259,7 +1285,8 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
         }
         const float* st = wb + (size_t)(ch & 1) * stageRows * KC;
         Lane32<D, NPL> L;
-        L.load(A, v0, lane);
+        if (tab) L.load_tab(tab, Vp, v0, lane);
+        else L.load(A, v0, lane);
         float2 g0[NP], h0[NP], t[NP], th[NP];
         ldp<NP>(g0, st);
         if (H) ldp<NP>(h0, st + KC);
@@ -1351,21 +1378,30 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
 // tiles or block barriers.  The rows of chunk k+1 are copied into the warp's
 // other stage while chunk k is computed; the FP64 macros of a batch of cells
 // are finished together, one lane per cell.
+// dvTab: the launch gave room after the stages for the velocity constants
+// (dv_table32), read from there per chunk instead of from global memory.
+// The batch of warp totals is kept in FP32: each total is an FP32 warp sum.
 template <int D, bool H, int NPL, int NW, bool OPEN = false>
-__global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A, int MF) {
+__global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A, int MF, int dvTab) {
     constexpr int NS = Slots<D, H>::NS, KC = 32 * NPL, NR = H ? 2 : 1;
-    __shared__ double sM[NW][kGatherBatch][NS];
+    __shared__ float sM[NW][kGatherBatch][NS];
     __shared__ int sC[NW][kGatherBatch];
     extern __shared__ __align__(16) float gsm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* wb = gsm + (size_t)warp * 2 * (1 + MF) * NR * KC + lane * NPL;
+    float* tab = nullptr;
+    if (dvTab) {
+        tab = gsm + gather_smem(NW, MF, KC, H) / sizeof(float);
+        dv_table32<D>(A, tab);
+        __syncthreads();
+    }
     const int myslot = slot_of<NS>(lane);
     const bool writer = NS == 16 ? (lane & 1) == 0 : true;
     const int TW = gridDim.x * NW, nC = A.b.nC;
     int nb = 0;
     for (int c = blockIdx.x * NW + warp; c < nC; c += TW) {
-        const double tot = gather_cell<D, H, NPL, OPEN>(A, c, MF, wb, lane);
-        if (writer) sM[warp][nb][myslot] = tot;
+        const double tot = gather_cell<D, H, NPL, OPEN>(A, c, MF, wb, lane, tab);
+        if (writer) sM[warp][nb][myslot] = (float)tot;
         if (lane == 0) sC[warp][nb] = c;
         ++nb;
         if (nb == kGatherBatch || c + TW >= nC) {
@@ -1383,7 +1419,7 @@ template <int D, bool H, int NPL, int NW>
 __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32_batch(const FusedArgs<float>* __restrict__ AA,
                                                                     const int* __restrict__ cellOff, int nCases, int MF) {
     constexpr int NS = Slots<D, H>::NS, KC = 32 * NPL, NR = H ? 2 : 1;
-    __shared__ double sM[NW][kGatherBatch][NS];
+    __shared__ float sM[NW][kGatherBatch][NS];  // FP32 warp totals, exact
     __shared__ int sC[NW][kGatherBatch], sI[NW][kGatherBatch];
     __shared__ FusedArgs<float> sA[NW];  // the warp's current case
     extern __shared__ __align__(16) float gsm[];
@@ -1405,7 +1441,7 @@ __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32_batch(const FusedA
             cur = i;
         }
         const double tot = gather_cell<D, H, NPL>(sA[warp], c, MF, wb, lane);
-        if (writer) sM[warp][nb][myslot] = tot;
+        if (writer) sM[warp][nb][myslot] = (float)tot;
         if (lane == 0) { sC[warp][nb] = c; sI[warp][nb] = i; }
         ++nb;
         if (nb == kGatherBatch || g + TW >= total) {

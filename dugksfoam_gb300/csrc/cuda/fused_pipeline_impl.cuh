@@ -169,6 +169,10 @@ public:
                 for (int c = 0; c < m.nC; ++c) gatherMF_ = std::max(gatherMF_, cfOff[c + 1] - cfOff[c]);
                 gatherMF_ = std::min(gatherMF_, 8);  // further faces of a cell are read directly
                 gatherSmem_ = gather_smem(kGatherWarps, gatherMF_, KC, H_);
+                // the velocity constants in shared memory when they are small
+                // (2D grids up to 1536 padded velocities: <= 24 KB per block)
+                gatherTab_ = fp32_ && D_ == 2 && dv_table32_bytes(D_, a.Vp) <= 24 * 1024;
+                if (gatherTab_) gatherSmem_ += dv_table32_bytes(D_, a.Vp);
                 allow_max_dynamic_smem(kGather_);
                 int per = 0, nsm = 0;
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kGather_, kGatherWarps * 32, gatherSmem_);
@@ -340,7 +344,7 @@ public:
         else if (k == 1) kMacros_<<<std::max(1, (a.nA + 127) / 128), 128, 0, s>>>(A);  // one face per thread
         else {
             kGather_<<<std::min((a.nC + kGatherWarps - 1) / kGatherWarps, gatherBlocks_), kGatherWarps * 32, gatherSmem_,
-                       s>>>(A, gatherMF_);
+                       s>>>(A, gatherMF_, gatherTab_ ? 1 : 0);
             if (a.zgMask || (a.bcMask & ((1 << kBcPressureIn) | (1 << kBcPressureOut)))) {
                 StepArgs n = A.b;  // zeroGradient U/T patches, then P10, from the macros this step wrote
                 n.rho = A.rhoN; n.U = A.UN; n.T = A.TN;
@@ -459,8 +463,9 @@ private:
     KernelFn kMacros_ = nullptr;
     KernelFn kOpen_ = nullptr;  // open boundary faces after sweep A (when the case has any)
     int gatherMF_ = 0, gatherBlocks_ = 1;
+    bool gatherTab_ = false;
     size_t gatherSmem_ = 0;
-    void (*kGather_)(FusedArgs<S>, int) = nullptr;
+    void (*kGather_)(FusedArgs<S>, int, int) = nullptr;
     bool H_ = true;
     TilePlan plan_;
     FusedArgs<S> args_{};
