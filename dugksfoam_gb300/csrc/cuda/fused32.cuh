@@ -1384,8 +1384,11 @@ __device__ __forceinline__ double gather_cell(const FusedArgs<float>& A, int c, 
 template <int D, bool H, int NPL, int NW, bool OPEN = false>
 __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A, int MF, int dvTab) {
     constexpr int NS = Slots<D, H>::NS, KC = 32 * NPL, NR = H ? 2 : 1;
-    __shared__ float sM[NW][kGatherBatch][NS];
-    __shared__ int sC[NW][kGatherBatch];
+    // 3D: half the batch -- the finalize is a small share of a 63-chunk cell,
+    // and the smaller buffer leaves the L1 more room (8.40 -> 8.21 ms, 48^3 hexes)
+    constexpr int GB = D == 3 ? kGatherBatch / 2 : kGatherBatch;
+    __shared__ float sM[NW][GB][NS];
+    __shared__ int sC[NW][GB];
     extern __shared__ __align__(16) float gsm[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* wb = gsm + (size_t)warp * 2 * (1 + MF) * NR * KC + lane * NPL;
@@ -1404,7 +1407,7 @@ __global__ void __launch_bounds__(NW * 32, 2) k_cell_gather32(FusedArgs<float> A
         if (writer) sM[warp][nb][myslot] = (float)tot;
         if (lane == 0) sC[warp][nb] = c;
         ++nb;
-        if (nb == kGatherBatch || c + TW >= nC) {
+        if (nb == GB || c + TW >= nC) {
             __syncwarp();
             if (lane < nb) finalize_cell32<D, H>(A, sC[warp][lane], sM[warp][lane]);
             __syncwarp();
