@@ -169,13 +169,22 @@ public:
                 for (int c = 0; c < m.nC; ++c) gatherMF_ = std::max(gatherMF_, cfOff[c + 1] - cfOff[c]);
                 gatherMF_ = std::min(gatherMF_, 8);  // further faces of a cell are read directly
                 gatherSmem_ = gather_smem(kGatherWarps, gatherMF_, KC, H_);
-                // the velocity constants in shared memory when they are small
-                // (2D grids up to 1536 padded velocities: <= 24 KB per block)
-                gatherTab_ = fp32_ && D_ == 2 && dv_table32_bytes(D_, a.Vp) <= 24 * 1024;
-                if (gatherTab_) gatherSmem_ += dv_table32_bytes(D_, a.Vp);
                 allow_max_dynamic_smem(kGather_);
                 int per = 0, nsm = 0;
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kGather_, kGatherWarps * 32, gatherSmem_);
+                // the velocity constants in shared memory when they are small
+                // (2D grids up to 1536 padded velocities: <= 24 KB per block)
+                // and the blocks per SM stay as they are without them
+                if (fp32_ && D_ == 2 && dv_table32_bytes(D_, a.Vp) <= 24 * 1024) {
+                    int perTab = 0;
+                    const size_t withTab = gatherSmem_ + dv_table32_bytes(D_, a.Vp);
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perTab, kGather_, kGatherWarps * 32, withTab);
+                    if (perTab >= per) {
+                        gatherTab_ = true;
+                        gatherSmem_ = withTab;
+                        per = perTab;
+                    }
+                }
                 cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
                 gatherBlocks_ = std::max(1, per) * std::max(1, nsm);  // persistent: one wave
                 args_.cfOff = upload(cfOff);
